@@ -1,0 +1,466 @@
+#!/usr/bin/env python3
+"""Benchmark of the cl_ops hot path on GB300.
+
+Headline workload: "satradix" sort of 2^28 uint32 keys drawn uniformly
+from splitmix64 (seed 42), keys only, through the C-ABI
+(clo_sort_with_device_data). One step = one full sort of a resident
+2^28-key array; every step sorts its own copy of the input (1 GiB each,
+larger than L2), so the timed region is exactly K sorts back to back.
+
+  value     Gkeys/s over the timed region (device events on the library
+            queue), summed over ranks (replicas; no collective).
+  e2e       the same metric through clo_sort_with_host_data from pinned
+            host memory: host->device copy, sort and device->host copy in
+            every step.
+  roofline  live per-launch device time of the dominant kernel
+            (satradix_onesweep) against its algorithmic bytes.
+  suite     the other large-size primitives (abitonic 2^26 uint32,
+            satradix 2^27 (uint64, uint32) pairs, blelloch scan 2^30
+            uint32 -> uint64, the five RNGs 2^24 states x 64 draws),
+            informational.
+  cpu_baseline  the CPU restatement (LSD radix, radix 16 as the reference
+            default, all host threads) on a 2^24-key sample.
+
+`--impl reference` times the reference's algorithm on the host cores
+instead (the reference itself needs an OpenCL runtime, GLib and cf4ocl2,
+none of which exist here); only rank 0 works under torchrun.
+"""
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "cl-ops_gb300"))
+sys.path.insert(0, str(ROOT / "tests"))
+
+METRIC = "Gkeys/s (radix/bitonic), scan GB/s vs HBM peak; batched vs plain on 1 GB300"
+WORKLOAD = "satradix sort, 2^28 uint32 keys, uniform splitmix64 seed 42, keys only"
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class Dist:
+    """Host-side barrier and max-reduction across ranks (gloo, CPU only)."""
+
+    def __init__(self, rank, world):
+        self.rank, self.world = rank, world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+            self.pg = True
+
+    def barrier(self):
+        if self.pg:
+            self.dist.barrier()
+
+    def max(self, v):
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.dist.destroy_process_group()
+
+
+def keys_u32_chunked(seed, n, chunk=1 << 24):
+    from inputs import splitmix64
+    out = np.empty(n, dtype=np.uint32)
+    for o in range(0, n, chunk):
+        m = min(chunk, n - o)
+        out[o:o + m] = (splitmix64(seed, m, offset=o) >> np.uint64(32)).astype(np.uint32)
+    return out
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(name):
+    """DRAM bytes per launch recorded from an ncu capture, if committed."""
+    p = ROOT / "profiles" / name
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("dram_bytes_per_launch_full_size:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def timed_region(clops, q, steps_fn, k):
+    """Runs steps_fn(i) for i in range(k) between two queue markers and
+    returns the device milliseconds between them."""
+    m0 = q.marker()
+    for i in range(k):
+        steps_fn(i)
+    m1 = q.marker()
+    return clops.Queue.elapsed_ms(m0, m1)
+
+
+def run_ours(args):
+    rank, world, local = dist_env()
+    dist = Dist(rank, world)
+    import clops
+    ctx = clops.Context(local)
+    q = clops.Queue(ctx, profiling=True)
+    n = 1 << args.log2n
+    K, W = args.steps, args.warmup
+
+    keys = keys_u32_chunked(42, n)
+    src = clops.Buffer.from_array(ctx, q, keys)
+    bufs = [clops.Buffer(ctx, keys.nbytes) for _ in range(K + W)]
+    for b in bufs:
+        clops.call(clops.lib.ccl_buffer_enqueue_copy, src.h, b.h, q.h, 0, 0, keys.nbytes, None)
+    q.finish()
+    sorter = clops.Sorter(ctx, "satradix", clops.CLO_UINT)
+
+    for i in range(W):
+        sorter.sort_device(q, bufs[i], n)
+    q.finish()
+    q.gc()
+
+    clops.lib.clo_gb300_timing_enable(1)
+    clops.lib.clo_gb300_timing_reset()
+    launches0 = clops.launch_count()
+    dist.barrier()
+    q.finish()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms = timed_region(clops, q, lambda i: sorter.sort_device(q, bufs[W + i], n), K)
+    q.finish()
+    clk = clocks.stop()
+    launches = clops.launch_count() - launches0
+    dist.barrier()
+    ms_max = dist.max(ms)
+    one_ms, one_bytes, one_n = clops.kernel_timing("satradix_onesweep")
+    up_ms, _, up_n = clops.kernel_timing("satradix_upsweep")
+    clops.lib.clo_gb300_timing_enable(0)
+
+    # Check the last step's output before reporting (sortedness + multiset).
+    got = bufs[-1].read(q, np.uint32, n)
+    ok = bool(np.all(got[1:] >= got[:-1])) and int(got.sum(dtype=np.uint64)) == \
+        int(keys.sum(dtype=np.uint64))
+    for b in bufs:
+        b.destroy()
+    src.destroy()
+    q.gc()
+
+    # ---- end to end: pinned host in/out, blocking host-data call ------------
+    e2e_steps = max(1, min(K, 5))
+    hin = clops.lib.clo_host_alloc(keys.nbytes, None)
+    hout = clops.lib.clo_host_alloc(keys.nbytes, None)
+    ain = np.ctypeslib.as_array((clops.C.c_uint32 * n).from_address(hin))
+    aout = np.ctypeslib.as_array((clops.C.c_uint32 * n).from_address(hout))
+    ain[:] = keys
+    for _ in range(2):
+        sorter.sort_host(q, ain, aout)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sorter.sort_host(q, ain, aout)
+    e2e_s = dist.max(time.perf_counter() - t0)
+    ok = ok and bool(np.all(aout[1:] >= aout[:-1]))
+    del ain, aout
+    clops.lib.clo_host_free(hin)
+    clops.lib.clo_host_free(hout)
+
+    suite = run_suite(clops, ctx, q, args) if (args.suite and rank == 0) else None
+
+    peak, peak_kind = measured_peaks()
+    achieved = (one_bytes / one_n) / (one_ms / one_n * 1e-3) / 1e9 if one_n else None
+    traffic = ncu_traffic("satradix_onesweep_2pow28_u32.txt")
+    out = {
+        "metric": METRIC,
+        "value": round(world * n * K / (ms_max * 1e-3) / 1e9, 3),
+        "unit": "Gkeys/s",
+        "n_gpus": world,
+        "steps": K,
+        "warmup": W,
+        "ms_per_step": round(ms_max / K, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u32",
+        "data": "synthetic (splitmix64 seed 42, uniform over [0, 2^32))",
+        "config": {"workload": WORKLOAD, "n": n, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2: a distinct 1 GiB copy per step",
+                   "result_check": "sorted+multiset ok" if ok else "FAILED"},
+        "e2e": {"value": round(world * n * e2e_steps / e2e_s / 1e9, 3), "unit": "Gkeys/s",
+                "h2d_bytes_per_step": n * 4, "d2h_bytes_per_step": n * 4,
+                "api": "clo_sort_with_host_data, pinned host buffers"},
+        "gpu_launches": int(launches),
+        "roofline": {
+            "kernel": "satradix_onesweep",
+            "bound": "hbm",
+            "achieved": round(achieved, 1) if achieved else None,
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": round(achieved / peak, 4) if achieved else None,
+            "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
+            "traffic": traffic,
+            "algorithmic_bytes_per_launch": one_bytes / one_n if one_n else None,
+            "launches": one_n,
+            "avg_launch_ms": round(one_ms / one_n, 4) if one_n else None,
+            "upsweep_avg_ms": round(up_ms / up_n, 4) if up_n else None,
+            "whole_sort_model": "36 B/key (4 B upsweep + 4 passes x 8 B)",
+            "whole_sort_frac": round((36.0 * n * K / (ms / 1e3) / 1e9) / peak, 4),
+        },
+        "clocks": clk,
+    }
+    if suite is not None:
+        out["suite"] = suite
+    if rank == 0:
+        out["cpu_baseline"] = cpu_baseline(args)
+        print(json.dumps(out), flush=True)
+    sorter.destroy()
+    q.destroy()
+    ctx.destroy()
+    dist.close()
+
+
+def run_suite(clops, ctx, q, args):
+    """The other large-size primitives, 2 warm-up + 3 timed calls each."""
+    from inputs import splitmix64, keys_u64
+    res = {}
+    peak, _ = measured_peaks()
+
+    def timed(fn, reps=3, warm=2):
+        for _ in range(warm):
+            fn()
+        q.finish()
+        return timed_region(clops, q, lambda i: fn(), reps) / reps
+
+    # abitonic 2^26 uint32
+    n = 1 << 26
+    a = keys_u32_chunked(44, n)
+    b = clops.Buffer.from_array(ctx, q, a)
+    s = clops.Sorter(ctx, "abitonic", clops.CLO_UINT)
+    pristine = clops.Buffer.from_array(ctx, q, a)
+
+    def bit():
+        clops.call(clops.lib.ccl_buffer_enqueue_copy, pristine.h, b.h, q.h, 0, 0, a.nbytes, None)
+    bit()
+    q.finish()
+    ms_copy = timed(bit)
+    ms = timed(lambda: (bit(), s.sort_device(q, b, n))) - ms_copy
+    res["abitonic_2pow26_u32"] = {"Gkeys/s": round(n / (ms * 1e-3) / 1e9, 3), "ms": round(ms, 3),
+                                  "canonical_bytes_GB": 17.7,
+                                  "frac_of_peak_canonical": round(17.7e9 / (ms * 1e-3) / 1e9 / peak, 4)}
+    s.destroy()
+    b.destroy()
+    pristine.destroy()
+
+    # satradix KV 2^27 (uint64 key, uint32 value = index)
+    n = 1 << 27
+    k = keys_u64(43, n)
+    v = np.arange(n, dtype=np.uint32)
+    kp, vp = clops.Buffer.from_array(ctx, q, k), clops.Buffer.from_array(ctx, q, v)
+    kb, vb = clops.Buffer(ctx, k.nbytes), clops.Buffer(ctx, v.nbytes)
+    s = clops.Sorter(ctx, "satradix", clops.CLO_ULONG)
+
+    def restore():
+        clops.call(clops.lib.ccl_buffer_enqueue_copy, kp.h, kb.h, q.h, 0, 0, k.nbytes, None)
+        clops.call(clops.lib.ccl_buffer_enqueue_copy, vp.h, vb.h, q.h, 0, 0, v.nbytes, None)
+    ms_copy = timed(restore)
+    ms = timed(lambda: (restore(), s.sort_kv_device(q, kb, vb, clops.CLO_UINT, n))) - ms_copy
+    res["satradix_kv_2pow27_u64_u32"] = {"Gpairs/s": round(n / (ms * 1e-3) / 1e9, 3), "ms": round(ms, 3),
+                                         "model_bytes_per_pair": 200,
+                                         "frac_of_peak": round(200.0 * n / (ms * 1e-3) / 1e9 / peak, 4)}
+    for x in (kp, vp, kb, vb, s):
+        x.destroy()
+    del k, v
+
+    # blelloch scan 2^30 uint32 in [0, 255] -> uint64
+    n = 1 << 30
+    a = np.empty(n, dtype=np.uint32)
+    for o in range(0, n, 1 << 24):
+        a[o:o + (1 << 24)] = (splitmix64(45, 1 << 24, offset=o) >> np.uint64(56)).astype(np.uint32)
+    bi = clops.Buffer.from_array(ctx, q, a)
+    bo = clops.Buffer(ctx, n * 8)
+    sc = clops.Scanner(ctx, clops.CLO_UINT, clops.CLO_ULONG)
+    ms = timed(lambda: sc.scan_device(q, bi, bo, n))
+    res["blelloch_2pow30_u32_u64"] = {"GB/s": round(12.0 * n / (ms * 1e-3) / 1e9, 1), "ms": round(ms, 3),
+                                      "frac_of_peak": round(12.0 * n / (ms * 1e-3) / 1e9 / peak, 4)}
+    for x in (bi, bo, sc):
+        x.destroy()
+    del a
+
+    # RNGs: 2^24 states from a host seed array, 64 draws
+    count, draws = 1 << 24, 64
+    out = clops.Buffer(ctx, count * draws * 4)
+    for name in ["lcg", "xorshift64", "xorshift128", "mwc64x", "parkmiller"]:
+        size = clops.RNG_SEED_SIZE[name]
+        seeds = splitmix64(46, count * size // 8 + 1).view(np.uint8)[:count * size].copy()
+        if name == "parkmiller":  # nonzero 31-bit states
+            w = seeds.view(np.uint32)
+            w[:] = (w % 2147483646) + 1
+        rng = clops.Rng(ctx, q, name, clops.CLO_RNG_SEED_EXT_HOST, count, seeds=seeds)
+        ms = timed(lambda: rng.fill(q, out, draws))
+        byts = count * draws * 4 + 2 * count * size
+        res[f"rng_{name}"] = {"Gdraws/s": round(count * draws / (ms * 1e-3) / 1e9, 2),
+                              "GB/s": round(byts / (ms * 1e-3) / 1e9, 1), "ms": round(ms, 4),
+                              "frac_of_peak": round(byts / (ms * 1e-3) / 1e9 / peak, 4)}
+        rng.destroy()
+    out.destroy()
+    q.gc()
+    return res
+
+
+def cpu_baseline(args):
+    """CPU restatement of the reference algorithm (LSD radix, 4-bit digits
+    as the reference's default radix 16) on a bounded sample, all host
+    threads."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    n = 1 << 24
+    cores = os.cpu_count() or 1
+    keys = keys_u32_chunked(42, n)
+    work = keys.copy()
+    oracle.radix_sort_u32_threaded(work, cores, 4)
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        work[:] = keys
+        oracle.radix_sort_u32_threaded(work, cores, 4)
+    dt = (time.perf_counter() - t0) / reps
+    return {"value": round(n / dt / 1e9, 4), "unit": "Gkeys/s", "cores": cores, "kind": "port",
+            "sample": "2^24 of the 2^28 uint32 keys (same generator), LSD radix 16, "
+                      f"{reps} timed sorts"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    n = 1 << 24
+    cores = os.cpu_count() or 1
+    keys = keys_u32_chunked(42, n)
+    work = keys.copy()
+    for _ in range(args.warmup):
+        work[:] = keys
+        oracle.radix_sort_u32_threaded(work, cores, 4)
+    total = 0.0
+    for _ in range(args.steps):
+        work[:] = keys
+        t0 = time.perf_counter()
+        oracle.radix_sort_u32_threaded(work, cores, 4)
+        total += time.perf_counter() - t0
+    ok = bool(np.all(work[1:] >= work[:-1]))
+    val = n * args.steps / total / 1e9
+    out = {
+        "impl": "reference",
+        "metric": METRIC, "value": round(val, 4), "unit": "Gkeys/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(total / args.steps * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (splitmix64 seed 42, uniform over [0, 2^32))",
+        "config": {"workload": WORKLOAD, "n": 1 << 28, "sample_n": n,
+                   "result_check": "sorted" if ok else "FAILED"},
+        "cpu_baseline": {"value": round(val, 4), "unit": "Gkeys/s", "cores": cores, "kind": "port",
+                         "sample": "each step sorts 2^24 of the 2^28 keys with the reference's "
+                                   "LSD radix-16 scheme on all host threads"},
+        "e2e": {"value": round(val, 4), "unit": "Gkeys/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--log2n", type=int, default=28)
+    ap.add_argument("--no-suite", dest="suite", action="store_false")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

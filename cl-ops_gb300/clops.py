@@ -1,0 +1,401 @@
+"""ctypes binding of libclops.so, the C-ABI drop-in for cl_ops.
+
+Mirrors the reference API one to one (same function names and argument
+order as src/cl_ops/*/clo_*.h and the cf4ocl2 calls the reference uses);
+`Lib` exposes the raw functions, and the small classes below wrap them the
+way the reference's tests and benchmarks use them (create a context and a
+queue, create an object, run with device or host data, destroy).
+
+Errors come back as GError* and are raised as CloError with the same
+code. The library must be built (build_lib.py); importing this module
+without it raises, there is no fallback path.
+"""
+import ctypes as C
+import pathlib
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+LIB_PATH = HERE / "libclops.so"
+
+# CloType values (clo_common.in.h:108-120).
+CLO_CHAR, CLO_UCHAR, CLO_SHORT, CLO_USHORT, CLO_INT, CLO_UINT, CLO_LONG, \
+    CLO_ULONG, CLO_HALF, CLO_FLOAT, CLO_DOUBLE = range(11)
+# Error codes (clo_common.in.h:80-95).
+CLO_SUCCESS, CLO_ERROR_OPENFILE, CLO_ERROR_ARGS, CLO_ERROR_STREAM_WRITE = 0, 1, 2, 3
+CLO_ERROR_IMPL_NOT_FOUND, CLO_ERROR_UNKNOWN_TYPE, CLO_ERROR_LIBRARY = 5, 6, 7
+# Seed types (clo_rng.in.h:78-92).
+CLO_RNG_SEED_DEV_GID, CLO_RNG_SEED_HOST_MT, CLO_RNG_SEED_EXT_DEV, \
+    CLO_RNG_SEED_EXT_HOST = range(4)
+CL_QUEUE_PROFILING_ENABLE = 1 << 1
+CL_MEM_READ_WRITE = 1 << 0
+
+NP_OF_TYPE = {
+    CLO_CHAR: np.int8, CLO_UCHAR: np.uint8, CLO_SHORT: np.int16,
+    CLO_USHORT: np.uint16, CLO_INT: np.int32, CLO_UINT: np.uint32,
+    CLO_LONG: np.int64, CLO_ULONG: np.uint64, CLO_HALF: np.float16,
+    CLO_FLOAT: np.float32, CLO_DOUBLE: np.float64,
+}
+
+RNG_NAMES = ["lcg", "xorshift64", "xorshift128", "mwc64x", "parkmiller", "tauslcg"]
+RNG_SEED_SIZE = {"lcg": 8, "xorshift64": 8, "xorshift128": 16, "mwc64x": 8,
+                 "parkmiller": 4, "tauslcg": 16}
+
+
+class GError(C.Structure):
+    _fields_ = [("domain", C.c_uint32), ("code", C.c_int), ("message", C.c_char_p)]
+
+
+class CloError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+        self.message = message
+
+
+P = C.c_void_p
+PERR = C.POINTER(C.POINTER(GError))
+SZ = C.c_size_t
+U32 = C.c_uint32
+U64 = C.c_uint64
+
+# name: (restype, [argtypes])
+_SIGS = {
+    # common
+    "clo_type_get_name": (C.c_char_p, [C.c_int]),
+    "clo_type_sizeof": (SZ, [C.c_int]),
+    "clo_type_by_name": (C.c_int, [C.c_char_p, PERR]),
+    "clo_nlpo2": (C.c_uint, [C.c_uint]),
+    "clo_ones32": (C.c_uint, [C.c_uint]),
+    "clo_tzc": (C.c_uint, [C.c_int]),
+    "clo_sum": (C.c_uint, [C.c_uint]),
+    "clo_print_to_null": (None, [C.c_char_p]),
+    "clo_error_quark": (U32, []),
+    "clo_error_free": (None, [C.POINTER(GError)]),
+    "clo_clear_error": (None, [PERR]),
+    # ccl shim
+    "ccl_context_new_any": (P, [PERR]),
+    "ccl_context_new_gpu": (P, [PERR]),
+    "ccl_context_new_from_menu_full": (P, [P, PERR]),
+    "ccl_context_new_from_device_index": (P, [C.c_int, PERR]),
+    "ccl_context_destroy": (None, [P]),
+    "ccl_context_ref": (None, [P]),
+    "ccl_context_unref": (None, [P]),
+    "ccl_context_get_num_devices": (U32, [P, PERR]),
+    "ccl_context_get_device": (P, [P, U32, PERR]),
+    "ccl_device_get_ordinal": (C.c_int, [P]),
+    "ccl_queue_new": (P, [P, P, U64, PERR]),
+    "ccl_queue_new_wrap": (P, [P, P, U64, PERR]),
+    "ccl_queue_destroy": (None, [P]),
+    "ccl_queue_finish": (U32, [P, PERR]),
+    "ccl_queue_get_device": (P, [P, PERR]),
+    "ccl_queue_get_context": (P, [P, PERR]),
+    "ccl_queue_unwrap": (P, [P]),
+    "ccl_queue_gc": (None, [P]),
+    "ccl_buffer_new": (P, [P, U64, SZ, P, PERR]),
+    "ccl_buffer_new_wrap": (P, [P, P, SZ, PERR]),
+    "ccl_buffer_destroy": (None, [P]),
+    "ccl_buffer_ref": (None, [P]),
+    "ccl_buffer_unwrap": (P, [P]),
+    "ccl_buffer_get_size": (SZ, [P]),
+    "ccl_buffer_enqueue_read": (P, [P, P, U32, SZ, SZ, P, P, PERR]),
+    "ccl_buffer_enqueue_write": (P, [P, P, U32, SZ, SZ, P, P, PERR]),
+    "ccl_buffer_enqueue_copy": (P, [P, P, P, SZ, SZ, SZ, P, PERR]),
+    "ccl_ewl": (P, None),
+    "ccl_event_wait_list_add": (None, None),
+    "ccl_event_wait_list_clear": (None, [P]),
+    "ccl_event_wait": (U32, [P, PERR]),
+    "ccl_event_set_name": (None, [P, C.c_char_p]),
+    "ccl_event_get_name": (C.c_char_p, [P]),
+    "ccl_event_get_duration": (U64, [P, PERR]),
+    "ccl_enqueue_marker": (P, [P, P, PERR]),
+    "ccl_event_elapsed_ns": (U64, [P, P, PERR]),
+    "ccl_program_get_source": (C.c_char_p, [P]),
+    "ccl_program_get_build_options": (C.c_char_p, [P]),
+    "ccl_wrapper_memcheck": (U32, []),
+    # sort
+    "clo_sort_new": (P, [C.c_char_p, C.c_char_p, P, C.POINTER(C.c_int),
+                         C.POINTER(C.c_int), C.c_char_p, C.c_char_p, C.c_char_p, PERR]),
+    "clo_sort_destroy": (None, [P]),
+    "clo_sort_with_device_data": (P, [P, P, P, P, P, SZ, SZ, PERR]),
+    "clo_sort_with_host_data": (U32, [P, P, P, P, P, SZ, SZ, PERR]),
+    "clo_sort_get_context": (P, [P]),
+    "clo_sort_get_program": (P, [P]),
+    "clo_sort_get_element_type": (C.c_int, [P]),
+    "clo_sort_get_element_size": (SZ, [P]),
+    "clo_sort_get_key_type": (C.c_int, [P]),
+    "clo_sort_get_key_size": (SZ, [P]),
+    "clo_sort_get_data": (P, [P]),
+    "clo_sort_set_data": (None, [P, P]),
+    "clo_sort_get_num_kernels": (U32, [P, PERR]),
+    "clo_sort_get_kernel_name": (C.c_char_p, [P, U32, PERR]),
+    "clo_sort_get_localmem_usage": (SZ, [P, U32, SZ, SZ, PERR]),
+    # scan
+    "clo_scan_new": (P, [C.c_char_p, C.c_char_p, P, C.c_int, C.c_int, C.c_char_p, PERR]),
+    "clo_scan_destroy": (None, [P]),
+    "clo_scan_with_device_data": (P, [P, P, P, P, P, SZ, SZ, PERR]),
+    "clo_scan_with_host_data": (U32, [P, P, P, P, P, SZ, SZ, PERR]),
+    "clo_scan_get_context": (P, [P]),
+    "clo_scan_get_program": (P, [P]),
+    "clo_scan_get_elem_type": (C.c_int, [P]),
+    "clo_scan_get_element_size": (SZ, [P]),
+    "clo_scan_get_sum_type": (C.c_int, [P]),
+    "clo_scan_get_sum_size": (SZ, [P]),
+    "clo_scan_get_data": (P, [P]),
+    "clo_scan_set_data": (None, [P, P]),
+    "clo_scan_get_num_kernels": (U32, [P, PERR]),
+    "clo_scan_get_kernel_name": (C.c_char_p, [P, U32, PERR]),
+    "clo_scan_get_localmem_usage": (SZ, [P, U32, SZ, SZ, PERR]),
+    # rng
+    "clo_rng_new": (P, [C.c_char_p, C.c_int, P, SZ, U64, C.c_char_p, P, P, PERR]),
+    "clo_rng_destroy": (None, [P]),
+    "clo_rng_get_source": (C.c_char_p, [P]),
+    "clo_rng_get_device_seeds": (P, [P]),
+    "clo_rng_get_size": (SZ, [P]),
+    # additions
+    "clo_sort_kv_with_device_data": (P, [P, P, P, P, C.c_int, SZ, PERR]),
+    "clo_sort_kv_with_host_data": (U32, [P, P, P, P, C.c_int, SZ, PERR]),
+    "clo_rng_fill": (P, [P, P, P, SZ, U32, U32, PERR]),
+    "clo_host_alloc": (P, [SZ, PERR]),
+    "clo_host_free": (None, [P]),
+    "clo_gb300_launch_count": (U64, []),
+    "clo_gb300_debug_scan_withhold": (None, [C.c_longlong]),
+    "clo_gb300_timing_enable": (None, [C.c_int]),
+    "clo_gb300_timing_reset": (None, []),
+    "clo_gb300_timing_get": (C.c_int, [C.c_char_p, C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double), C.POINTER(U64)]),
+}
+
+# Data symbols exported by the library.
+DATA_SYMBOLS = ["clo_rng_infos", "clo_sort_sbitonic_def", "clo_sort_abitonic_def",
+                "clo_sort_gselect_def", "clo_sort_satradix_def", "clo_scan_blelloch_def"]
+
+
+def _load():
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is not built (run build_lib.py)")
+    lib = C.CDLL(str(LIB_PATH))
+    for name, (res, args) in _SIGS.items():
+        f = getattr(lib, name)
+        f.restype = res
+        if args is not None:
+            f.argtypes = args
+    return lib
+
+
+lib = _load()
+
+
+def err_ptr():
+    return C.POINTER(GError)()
+
+
+def check(e, what=""):
+    """Raises CloError when the GError* holder is set (and frees it)."""
+    if e:
+        code, msg = e.contents.code, (e.contents.message or b"").decode()
+        lib.clo_error_free(e)
+        raise CloError(code, f"{what}: {msg}" if what else msg)
+
+
+def call(fn, *args, what=None):
+    """Calls fn(*args, &err) and raises on error."""
+    e = err_ptr()
+    r = fn(*args, C.byref(e))
+    check(e, what or getattr(fn, "__name__", ""))
+    return r
+
+
+def np_ptr(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+# ---------------------------------------------------------------- objects
+class Context:
+    def __init__(self, ordinal=0):
+        self.h = call(lib.ccl_context_new_from_device_index, ordinal)
+
+    def destroy(self):
+        if self.h:
+            lib.ccl_context_destroy(self.h)
+            self.h = None
+
+
+class Queue:
+    def __init__(self, ctx, profiling=False, stream=None):
+        props = CL_QUEUE_PROFILING_ENABLE if profiling else 0
+        if stream is None:
+            self.h = call(lib.ccl_queue_new, ctx.h, None, props)
+        else:
+            self.h = call(lib.ccl_queue_new_wrap, ctx.h, C.c_void_p(stream), props)
+
+    def finish(self):
+        call(lib.ccl_queue_finish, self.h)
+
+    def gc(self):
+        lib.ccl_queue_gc(self.h)
+
+    def marker(self):
+        return call(lib.ccl_enqueue_marker, self.h, None)
+
+    @staticmethod
+    def elapsed_ms(m0, m1):
+        return call(lib.ccl_event_elapsed_ns, C.c_void_p(m0), C.c_void_p(m1)) / 1e6
+
+    def destroy(self):
+        if self.h:
+            lib.ccl_queue_destroy(self.h)
+            self.h = None
+
+
+class Buffer:
+    """Device buffer; `from_array` uploads, `read` downloads."""
+
+    def __init__(self, ctx, nbytes, host=None):
+        self.ctx = ctx
+        self.nbytes = nbytes
+        self.h = call(lib.ccl_buffer_new, ctx.h, CL_MEM_READ_WRITE, nbytes, None)
+        self._host = host
+
+    @classmethod
+    def from_array(cls, ctx, q, a):
+        a = np.ascontiguousarray(a)
+        b = cls(ctx, a.nbytes)
+        if a.nbytes:
+            call(lib.ccl_buffer_enqueue_write, b.h, q.h, 1, 0, a.nbytes, np_ptr(a), None)
+        return b
+
+    def read(self, q, dtype, count):
+        out = np.empty(count, dtype=dtype)
+        if out.nbytes:
+            call(lib.ccl_buffer_enqueue_read, self.h, q.h, 1, 0, out.nbytes, np_ptr(out), None)
+        return out
+
+    def write(self, q, a):
+        a = np.ascontiguousarray(a)
+        call(lib.ccl_buffer_enqueue_write, self.h, q.h, 1, 0, a.nbytes, np_ptr(a), None)
+
+    @property
+    def ptr(self):
+        return lib.ccl_buffer_unwrap(self.h)
+
+    def destroy(self):
+        if self.h:
+            lib.ccl_buffer_destroy(self.h)
+            self.h = None
+
+
+def wait(evt):
+    """Blocks on one event (ccl_event_wait over a one-element list)."""
+    ewl = C.c_void_p(None)
+    lib.ccl_ewl(C.byref(ewl), C.c_void_p(evt), C.c_void_p(None))
+    call(lib.ccl_event_wait, C.byref(ewl))
+
+
+class Sorter:
+    def __init__(self, ctx, algo, elem_type, key_type=None, options=None,
+                 compare=None, get_key=None, compiler_opts=None):
+        et = C.c_int(elem_type)
+        kt = C.c_int(key_type) if key_type is not None else None
+        self.h = call(lib.clo_sort_new, algo.encode(),
+                      options.encode() if options else None, ctx.h, C.byref(et),
+                      C.byref(kt) if kt is not None else None,
+                      compare.encode() if compare else None,
+                      get_key.encode() if get_key else None,
+                      compiler_opts.encode() if compiler_opts else None)
+        self.elem_type = elem_type
+
+    def sort_device(self, q, buf_in, numel, buf_out=None, lws_max=0, q_comm=None):
+        return call(lib.clo_sort_with_device_data, self.h, q.h,
+                    q_comm.h if q_comm else None, buf_in.h,
+                    buf_out.h if buf_out else None, numel, lws_max)
+
+    def sort_host(self, q, a, out=None, lws_max=0, q_comm=None):
+        a = np.ascontiguousarray(a)
+        o = a if out is None else out
+        call(lib.clo_sort_with_host_data, self.h, q.h if q else None,
+             q_comm.h if q_comm else None, np_ptr(a), np_ptr(o), a.size, lws_max)
+        return o
+
+    def sort_kv_device(self, q, kbuf, vbuf, value_type, numel):
+        return call(lib.clo_sort_kv_with_device_data, self.h, q.h, kbuf.h, vbuf.h,
+                    value_type, numel)
+
+    def sort_kv_host(self, q, keys, vals, value_type):
+        call(lib.clo_sort_kv_with_host_data, self.h, q.h if q else None,
+             np_ptr(keys), np_ptr(vals), value_type, keys.size)
+
+    def destroy(self):
+        if self.h:
+            lib.clo_sort_destroy(self.h)
+            self.h = None
+
+
+class Scanner:
+    def __init__(self, ctx, elem_type, sum_type, algo="blelloch", options=None):
+        self.h = call(lib.clo_scan_new, algo.encode(),
+                      options.encode() if options else None, ctx.h, elem_type,
+                      sum_type, None)
+
+    def scan_device(self, q, buf_in, buf_out, numel, lws_max=0):
+        return call(lib.clo_scan_with_device_data, self.h, q.h, None, buf_in.h,
+                    buf_out.h, numel, lws_max)
+
+    def scan_host(self, q, a, out, lws_max=0):
+        call(lib.clo_scan_with_host_data, self.h, q.h if q else None, None,
+             np_ptr(a), np_ptr(out), a.size, lws_max)
+        return out
+
+    def destroy(self):
+        if self.h:
+            lib.clo_scan_destroy(self.h)
+            self.h = None
+
+
+class Rng:
+    def __init__(self, ctx, q, name, seed_type, count, main_seed=0, hash=None,
+                 seeds=None):
+        self.count = count
+        self.name = name
+        if seed_type == CLO_RNG_SEED_EXT_HOST and seeds is not None:
+            arr = np.ascontiguousarray(seeds)
+            sp = np_ptr(arr)
+        elif seed_type == CLO_RNG_SEED_EXT_DEV and seeds is not None:
+            sp = C.c_void_p(seeds.h)
+        else:
+            sp = None
+        self.h = call(lib.clo_rng_new, name.encode(), seed_type, sp, count,
+                      main_seed, hash.encode() if hash is not None else None,
+                      ctx.h, q.h)
+
+    @property
+    def seeds_buffer(self):
+        return lib.clo_rng_get_device_seeds(self.h)
+
+    def states(self, q):
+        size = lib.clo_rng_get_size(self.h)
+        out = np.empty(size, dtype=np.uint8)
+        if size:
+            call(lib.ccl_buffer_enqueue_read, self.seeds_buffer, q.h, 1, 0, size,
+                 np_ptr(out), None)
+        return out
+
+    def fill(self, q, out_buf, draws, bits=32, maxint=0):
+        return call(lib.clo_rng_fill, self.h, q.h, out_buf.h, draws, bits, maxint)
+
+    def destroy(self):
+        if self.h:
+            lib.clo_rng_destroy(self.h)
+            self.h = None
+
+
+def launch_count():
+    return int(lib.clo_gb300_launch_count())
+
+
+def kernel_timing(name):
+    """(total_ms, total_algorithmic_bytes, launches) of one kernel."""
+    ms, by, n = C.c_double(), C.c_double(), U64()
+    if not lib.clo_gb300_timing_get(name.encode(), C.byref(ms), C.byref(by), C.byref(n)):
+        return 0.0, 0.0, 0
+    return ms.value, by.value, int(n.value)

@@ -1,0 +1,374 @@
+// "sbitonic" and "abitonic": the reference's bitonic sorting network,
+// replayed exactly on sm_103a.
+//
+// Network (src/cl_ops/sort/clo_sort_sbitonic.cl:38-69 and the grouped
+// kernels of clo_sort_abitonic.cl:31-1067): over N = nlpo2(n) elements,
+// for stage s = 1..log2 N and step t = s..1, elements i and i + 2^(t-1)
+// with bit t-1 of i clear are compared; the block direction is bit s of i
+// (1 = descending); they swap iff COMPARE(key_i, key_j) XOR desc, with
+// COMPARE(a, b) = a > b. Every step touches disjoint pairs, so any
+// implementation that applies the same steps in the same order produces
+// the same array, bit for bit, including where the compare is not a total
+// order (equal keys, NaN, -0.0/+0.0).
+//
+// sbitonic keeps the reference's one-step-per-launch structure.
+// abitonic groups the steps:
+//   - abitonic_tile_sort: each shared-memory tile of 2^t elements runs
+//     stages 1..t (the stage-t direction comes from the tile's index);
+//   - abitonic_global_steps<g>: g (<= 4) consecutive steps with strides
+//     >= the tile, 2^g elements per thread held in registers;
+//   - abitonic_tile_finish: the remaining steps t..1 of a stage in shared
+//     memory.
+// Inside the tile kernels steps are also applied 4 at a time on 16
+// registers per thread between barriers.
+// Sizes that are not a power of two are padded (in a temporary buffer)
+// with the element type's maximum, which the final ascending stage moves
+// past the real elements; the reference requires power-of-two sizes.
+//
+// HBM roofline: 2 x sizeof(T) x N bytes per launch (one read, one write).
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <climits>
+
+#include "clo_internal.h"
+#include "dev_common.cuh"
+#include "timing.h"
+
+namespace clo {
+namespace {
+
+struct Half16 {
+	uint16_t bits;
+};
+
+template <typename T>
+struct BT {
+	__device__ __forceinline__ static bool gt(T a, T b) { return a > b; }
+};
+template <>
+struct BT<Half16> {
+	__device__ __forceinline__ static bool gt(Half16 a, Half16 b) {
+		return __half2float(__ushort_as_half(a.bits)) >
+			__half2float(__ushort_as_half(b.bits));
+	}
+};
+
+template <typename T>
+__device__ __forceinline__ void cmpxchg(T &a, T &b, bool desc) {
+	if (BT<T>::gt(a, b) != desc) {
+		T t = a;
+		a = b;
+		b = t;
+	}
+}
+
+// ------------------------------------------------------------ sbitonic
+template <typename T>
+__global__ void __launch_bounds__(256)
+sbitonic_step(T *data, size_t half_n, int stage, int step) {
+	size_t gid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+	if (gid >= half_n) return;
+	size_t stride = (size_t)1 << (step - 1);
+	size_t i1 = gid + (gid & ~(stride - 1));
+	size_t i2 = i1 + stride;
+	bool desc = (gid >> (stage - 1)) & 1;
+	T a = data[i1], b = data[i2];
+	if (BT<T>::gt(a, b) != desc) {
+		data[i1] = b;
+		data[i2] = a;
+	}
+}
+
+// ------------------------------------------------- abitonic global steps
+// Steps step .. step-G+1 of `stage`, 2^G elements per thread.
+template <typename T, int G>
+__global__ void __launch_bounds__(256)
+abitonic_global_steps(T *data, size_t groups, int stage, int step) {
+	size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+	if (q >= groups) return;
+	const int lo_bits = step - G;
+	size_t low = q & (((size_t)1 << lo_bits) - 1);
+	size_t high = q >> lo_bits;
+	size_t base = (high << step) | low;
+	const size_t inc = (size_t)1 << lo_bits;
+	const bool desc = (base >> stage) & 1;
+	T r[1 << G];
+#pragma unroll
+	for (int m = 0; m < (1 << G); ++m) r[m] = data[base + m * inc];
+#pragma unroll
+	for (int s = G - 1; s >= 0; --s) {
+#pragma unroll
+		for (int m = 0; m < (1 << G); ++m)
+			if (!(m & (1 << s))) cmpxchg(r[m], r[m | (1 << s)], desc);
+	}
+#pragma unroll
+	for (int m = 0; m < (1 << G); ++m) data[base + m * inc] = r[m];
+}
+
+// ------------------------------------------------- shared-memory tiles
+constexpr int kTileThreads = 512;
+
+__device__ __forceinline__ uint32_t spad(uint32_t i) { return i + (i >> 5); }
+
+// Applies steps j .. j-g+1 of a stage to the tile in shared memory, in
+// groups of 2^g elements held in registers. `desc_fn(i)` gives the
+// direction of element i (tile-local index).
+template <typename T, int G, typename DescFn>
+__device__ __forceinline__ void smem_steps(T *s, uint32_t tile_n, int j,
+	DescFn desc_fn) {
+	const int lo_bits = j - G;
+	const uint32_t groups = tile_n >> G;
+	const uint32_t inc = 1u << lo_bits;
+	for (uint32_t q = threadIdx.x; q < groups; q += blockDim.x) {
+		uint32_t low = q & (inc - 1);
+		uint32_t base = ((q >> lo_bits) << j) | low;
+		bool desc = desc_fn(base);
+		T r[1 << G];
+#pragma unroll
+		for (int m = 0; m < (1 << G); ++m) r[m] = s[spad(base + m * inc)];
+#pragma unroll
+		for (int b = G - 1; b >= 0; --b) {
+#pragma unroll
+			for (int m = 0; m < (1 << G); ++m)
+				if (!(m & (1 << b))) cmpxchg(r[m], r[m | (1 << b)], desc);
+		}
+#pragma unroll
+		for (int m = 0; m < (1 << G); ++m) s[spad(base + m * inc)] = r[m];
+	}
+}
+
+// Steps j..1 of one stage, at most 4 per barrier interval.
+template <typename T, typename DescFn>
+__device__ __forceinline__ void smem_stage_tail(T *s, uint32_t tile_n, int j,
+	int maxg, DescFn desc_fn) {
+	while (j >= 1) {
+		int g = j < maxg ? j : maxg;
+		switch (g) {
+		case 4: smem_steps<T, 4>(s, tile_n, j, desc_fn); break;
+		case 3: smem_steps<T, 3>(s, tile_n, j, desc_fn); break;
+		case 2: smem_steps<T, 2>(s, tile_n, j, desc_fn); break;
+		default: smem_steps<T, 1>(s, tile_n, j, desc_fn); break;
+		}
+		__syncthreads();
+		j -= g;
+	}
+}
+
+template <typename T>
+__device__ __forceinline__ void tile_load(T *s, const T *g, uint32_t tile_n) {
+	for (uint32_t i = threadIdx.x; i < tile_n; i += blockDim.x) s[spad(i)] = g[i];
+	__syncthreads();
+}
+
+template <typename T>
+__device__ __forceinline__ void tile_store(T *g, const T *s, uint32_t tile_n) {
+	for (uint32_t i = threadIdx.x; i < tile_n; i += blockDim.x) g[i] = s[spad(i)];
+}
+
+// Stages 1..t of every tile of 2^t elements.
+template <typename T>
+__global__ void __launch_bounds__(kTileThreads)
+abitonic_tile_sort(T *data, int t, int maxg) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	T *s = reinterpret_cast<T *>(smem_raw);
+	const uint32_t tile_n = 1u << t;
+	const size_t tile_base = (size_t)blockIdx.x << t;
+	T *g = data + tile_base;
+	tile_load(s, g, tile_n);
+	for (int stage = 1; stage <= t; ++stage) {
+		if (stage < t) {
+			smem_stage_tail(s, tile_n, stage, maxg,
+				[stage](uint32_t i) { return (bool)((i >> stage) & 1); });
+		} else {
+			const bool d = (tile_base >> stage) & 1;
+			smem_stage_tail(s, tile_n, stage, maxg, [d](uint32_t) { return d; });
+		}
+	}
+	tile_store(g, s, tile_n);
+}
+
+// Steps t..1 of `stage` (> t) for every tile.
+template <typename T>
+__global__ void __launch_bounds__(kTileThreads)
+abitonic_tile_finish(T *data, int t, int stage, int maxg) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	T *s = reinterpret_cast<T *>(smem_raw);
+	const uint32_t tile_n = 1u << t;
+	const size_t tile_base = (size_t)blockIdx.x << t;
+	T *g = data + tile_base;
+	const bool d = (tile_base >> stage) & 1;
+	tile_load(s, g, tile_n);
+	smem_stage_tail(s, tile_n, t, maxg, [d](uint32_t) { return d; });
+	tile_store(g, s, tile_n);
+}
+
+template <typename T>
+__global__ void fill_value(T *p, size_t n, T v) {
+	size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+	if (i < n) p[i] = v;
+}
+
+template <typename T> T max_value();
+template <> int8_t max_value<int8_t>() { return INT8_MAX; }
+template <> uint8_t max_value<uint8_t>() { return UINT8_MAX; }
+template <> int16_t max_value<int16_t>() { return INT16_MAX; }
+template <> uint16_t max_value<uint16_t>() { return UINT16_MAX; }
+template <> int32_t max_value<int32_t>() { return INT32_MAX; }
+template <> uint32_t max_value<uint32_t>() { return UINT32_MAX; }
+template <> int64_t max_value<int64_t>() { return INT64_MAX; }
+template <> uint64_t max_value<uint64_t>() { return UINT64_MAX; }
+template <> Half16 max_value<Half16>() { return Half16{0x7c00}; }  // +inf
+template <> float max_value<float>() { return __builtin_huge_valf(); }
+template <> double max_value<double>() { return __builtin_huge_val(); }
+
+int ilog2(size_t v) {
+	int r = 0;
+	while (((size_t)1 << r) < v) ++r;
+	return r;
+}
+
+// Tile exponent: 2^14 elements (<= 4-byte types) or 2^13 (8-byte), so a
+// tile takes 64 KB of shared memory; capped by the abitonic maxsfs option.
+template <typename T>
+int default_tile_log2() {
+	return sizeof(T) >= 8 ? 13 : 14;
+}
+
+template <typename T>
+cudaError_t run_abitonic(T *d, size_t N, int max_ps, int max_sfs,
+	cudaStream_t s, unsigned &launches) {
+	const int logN = ilog2(N);
+	int t = std::min(default_tile_log2<T>(), logN);
+	if (max_sfs >= 1 && max_sfs < t) t = max_sfs;
+	const int maxg = std::max(1, std::min(4, max_ps));
+	const uint32_t tile_n = 1u << t;
+	const size_t smem = (size_t)(tile_n + tile_n / 32 + 1) * sizeof(T);
+	const int threads = (int)std::min<uint32_t>(kTileThreads, std::max<uint32_t>(tile_n / 2, 32));
+	cudaError_t e = cudaFuncSetAttribute(abitonic_tile_sort<T>,
+		cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (e == cudaSuccess)
+		e = cudaFuncSetAttribute(abitonic_tile_finish<T>,
+			cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (e != cudaSuccess) return e;
+	const size_t tiles = N >> t;
+	const double pass_bytes = 2.0 * (double)N * sizeof(T);
+	{
+		KernelTimer tm("abitonic_tile_sort", s, pass_bytes);
+		abitonic_tile_sort<T><<<(unsigned)tiles, threads, smem, s>>>(d, t, maxg);
+		tm.stop();
+	}
+	launches++;
+	for (int stage = t + 1; stage <= logN && e == cudaSuccess; ++stage) {
+		int j = stage;
+		while (j > t) {
+			int g = std::min(maxg, j - t);
+			size_t groups = N >> g;
+			unsigned blocks = (unsigned)((groups + 255) / 256);
+			KernelTimer tm("abitonic_global_steps", s, pass_bytes);
+			switch (g) {
+			case 4: abitonic_global_steps<T, 4><<<blocks, 256, 0, s>>>(d, groups, stage, j); break;
+			case 3: abitonic_global_steps<T, 3><<<blocks, 256, 0, s>>>(d, groups, stage, j); break;
+			case 2: abitonic_global_steps<T, 2><<<blocks, 256, 0, s>>>(d, groups, stage, j); break;
+			default: abitonic_global_steps<T, 1><<<blocks, 256, 0, s>>>(d, groups, stage, j); break;
+			}
+			tm.stop();
+			launches++;
+			j -= g;
+		}
+		KernelTimer tf("abitonic_tile_finish", s, pass_bytes);
+		abitonic_tile_finish<T><<<(unsigned)tiles, threads, smem, s>>>(d, t, stage, maxg);
+		tf.stop();
+		launches++;
+		e = cudaGetLastError();
+	}
+	if (e == cudaSuccess) e = cudaGetLastError();
+	return e;
+}
+
+template <typename T>
+cudaError_t run_sbitonic(T *d, size_t N, cudaStream_t s, unsigned &launches) {
+	const int logN = ilog2(N);
+	const size_t half = N / 2;
+	const unsigned blocks = (unsigned)((half + 255) / 256);
+	for (int stage = 1; stage <= logN; ++stage)
+		for (int step = stage; step >= 1; --step) {
+			sbitonic_step<T><<<blocks, 256, 0, s>>>(d, half, stage, step);
+			launches++;
+		}
+	return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t bitonic_typed(void *data, size_t n, bool simple, int max_ps,
+	int max_sfs, CCLContext *ctx, cudaStream_t s, GError **err) {
+	if (n < 2) return cudaSuccess;
+	size_t N = (size_t)1 << ilog2(n);
+	T *d = (T *)data;
+	T *tmp = nullptr;
+	unsigned launches = 0;
+	cudaError_t e = cudaSuccess;
+	if (N != n) {
+		tmp = (T *)tmp_alloc(ctx, N * sizeof(T), s, err);
+		if (!tmp) return cudaErrorMemoryAllocation;
+		e = cudaMemcpyAsync(tmp, data, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
+		if (e == cudaSuccess) {
+			size_t pad = N - n;
+			fill_value<T><<<(unsigned)((pad + 255) / 256), 256, 0, s>>>(tmp + n, pad,
+				max_value<T>());
+			launches++;
+			e = cudaGetLastError();
+		}
+		d = tmp;
+	}
+	if (e == cudaSuccess)
+		e = simple ? run_sbitonic<T>(d, N, s, launches)
+				   : run_abitonic<T>(d, N, max_ps, max_sfs, s, launches);
+	if (tmp) {
+		if (e == cudaSuccess)
+			e = cudaMemcpyAsync(data, tmp, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
+		tmp_free(tmp, s);
+	}
+	count_launches(launches);
+	if (e != cudaSuccess) cuda_ok(e, err, simple ? "sbitonic" : "abitonic");
+	return e;
+}
+
+cudaError_t bitonic_dispatch(void *data, size_t n, CloType type, bool simple,
+	int max_ps, int max_sfs, CCLContext *ctx, cudaStream_t s, GError **err) {
+	switch (type) {
+	case CLO_CHAR: return bitonic_typed<int8_t>(data, n, simple, max_ps, max_sfs, ctx, s, err);
+	case CLO_UCHAR: return bitonic_typed<uint8_t>(data, n, simple, max_ps, max_sfs, ctx, s, err);
+	case CLO_SHORT: return bitonic_typed<int16_t>(data, n, simple, max_ps, max_sfs, ctx, s, err);
+	case CLO_USHORT: return bitonic_typed<uint16_t>(data, n, simple, max_ps, max_sfs, ctx, s, err);
+	case CLO_INT: return bitonic_typed<int32_t>(data, n, simple, max_ps, max_sfs, ctx, s, err);
+	case CLO_UINT: return bitonic_typed<uint32_t>(data, n, simple, max_ps, max_sfs, ctx, s, err);
+	case CLO_LONG: return bitonic_typed<int64_t>(data, n, simple, max_ps, max_sfs, ctx, s, err);
+	case CLO_ULONG: return bitonic_typed<uint64_t>(data, n, simple, max_ps, max_sfs, ctx, s, err);
+	case CLO_HALF: return bitonic_typed<Half16>(data, n, simple, max_ps, max_sfs, ctx, s, err);
+	case CLO_FLOAT: return bitonic_typed<float>(data, n, simple, max_ps, max_sfs, ctx, s, err);
+	case CLO_DOUBLE: return bitonic_typed<double>(data, n, simple, max_ps, max_sfs, ctx, s, err);
+	}
+	set_error(err, CLO_ERROR_ARGS, "Unsupported element type %d", (int)type);
+	return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+cudaError_t bitonic_sort(void *data, size_t n, CloType type, CCLContext *ctx,
+	cudaStream_t s, GError **err) {
+	return bitonic_dispatch(data, n, type, false, 4, 0, ctx, s, err);
+}
+
+cudaError_t bitonic_sort_tuned(void *data, size_t n, CloType type, int max_ps,
+	int max_sfs, CCLContext *ctx, cudaStream_t s, GError **err) {
+	return bitonic_dispatch(data, n, type, false, max_ps, max_sfs, ctx, s, err);
+}
+
+cudaError_t bitonic_sort_simple(void *data, size_t n, CloType type,
+	CCLContext *ctx, cudaStream_t s, GError **err) {
+	return bitonic_dispatch(data, n, type, true, 1, 0, ctx, s, err);
+}
+
+}  // namespace clo

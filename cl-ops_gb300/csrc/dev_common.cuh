@@ -1,0 +1,74 @@
+// Device helpers shared by the sm_103a kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace clo {
+namespace dev {
+
+__device__ __forceinline__ uint32_t lane_id() {
+	return threadIdx.x & 31u;
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+	uint32_t m;
+	asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+	return m;
+}
+
+// Relaxed/acquire/release accesses at GPU scope for lookback flags.
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t *p) {
+	uint32_t v;
+	asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+}
+__device__ __forceinline__ uint64_t ld_relaxed_u64(const uint64_t *p) {
+	uint64_t v;
+	asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+	return v;
+}
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p) {
+	uint32_t v;
+	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+}
+__device__ __forceinline__ void st_relaxed_u32(uint32_t *p, uint32_t v) {
+	asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed_u64(uint64_t *p, uint64_t v) {
+	asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" :: "l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void st_release_u32(uint32_t *p, uint32_t v) {
+	asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
+// Streaming (evict-first) 16-byte load/store for data touched once.
+__device__ __forceinline__ uint4 ld_stream_v4(const uint4 *p) {
+	uint4 v;
+	asm volatile("ld.global.cs.v4.u32 {%0,%1,%2,%3}, [%4];"
+		: "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
+	return v;
+}
+__device__ __forceinline__ void st_stream_v4(uint4 *p, uint4 v) {
+	asm volatile("st.global.cs.v4.u32 [%0], {%1,%2,%3,%4};"
+		:: "l"(p), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w) : "memory");
+}
+
+// Spin budget of every bounded wait: with the nanosleep back-off below and
+// the re-read of the flag each round this is about a second of waiting
+// before a wait gives up.
+constexpr uint32_t kSpinLimit = 1u << 20;
+
+__device__ __forceinline__ void backoff(uint32_t iter) {
+	if (iter > 8) __nanosleep(iter < 64 ? 64 : 256);
+}
+
+// Records a watchdog failure (first writer wins) in the context's status.
+__device__ __forceinline__ void report_timeout(int *status, int code,
+	int detail) {
+	if (atomicCAS(status, 0, code) == 0) atomicExch(status + 1, detail);
+}
+
+}  // namespace dev
+}  // namespace clo

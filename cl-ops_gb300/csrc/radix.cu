@@ -1,0 +1,424 @@
+// "satradix": stable LSD radix sort, onesweep style, 8-bit digits.
+//
+// Result contract (src/cl_ops/sort/clo_sort_satradix.c:117-335 with the
+// kernels of clo_sort_satradix.cl:34-258): a stable sort, ascending by the
+// unsigned bit pattern of the key. The reference sorts with
+// log2(radix)-bit digits; any digit width gives the same stable order, so
+// the width here is a tuning choice (8 bits: 4 passes for 32-bit keys).
+//
+// Per sort:
+//   1. radix_upsweep: one read of the keys builds the 256-bin histogram
+//      of every digit position at once.
+//   2. per digit position, radix_onesweep (one launch per pass):
+//      a. a tile of keys (8192 x 32-bit or 4096 x 64-bit) is loaded
+//         warp-striped, so that each warp's keys are in index order;
+//      b. warp-level multisplit ranks every key among equal digits of its
+//         warp (stable: lanes in order, rounds in order), with per-warp
+//         counters in shared memory;
+//      c. per-digit counts are combined across warps, published for the
+//         tile, and a decoupled lookback (one thread per digit, bounded
+//         waits) yields each digit's global offset;
+//      d. keys (then values) are staged in shared memory in tile-sorted
+//         order and written out so that consecutive threads write
+//         consecutive addresses of a digit's run.
+// Passes whose digit has a single populated bin are skipped (the order of
+// a stable sort by a constant digit is the identity).
+//
+// HBM roofline per 32-bit key: 4 B (upsweep) + P x 8 B (passes), i.e.
+// 36 B/key for P = 4.
+#include <algorithm>
+#include <vector>
+
+#include "clo_internal.h"
+#include "dev_common.cuh"
+#include "timing.h"
+
+namespace clo {
+namespace {
+
+constexpr int kRadixBits = 8;
+constexpr int kRadix = 1 << kRadixBits;
+constexpr int kThreads = 512;
+constexpr int kWarps = kThreads / 32;
+
+// Tile status word: 2-bit flag | 30-bit count.
+constexpr uint32_t kStAgg = 1u << 30;
+constexpr uint32_t kStPrefix = 2u << 30;
+constexpr uint32_t kStValue = (1u << 30) - 1u;
+
+template <typename K>
+struct KeyCfg {
+	static constexpr int kKpt = sizeof(K) <= 4 ? 16 : 8;
+	static constexpr int kTile = kThreads * kKpt;
+};
+
+template <typename K>
+__device__ __forceinline__ uint32_t digit_of(K k, int shift) {
+	return (uint32_t)(k >> shift) & (kRadix - 1);
+}
+
+// ----------------------------------------------------------- upsweep
+// Histograms of all `passes` digit positions in one read. Warps whose
+// lanes share a digit (sorted or constant input) add once per warp.
+template <typename K>
+__global__ void __launch_bounds__(256)
+radix_upsweep(const K *__restrict__ keys, size_t n, int passes,
+	uint32_t *__restrict__ hist) {
+	__shared__ uint32_t h[8][kRadix];
+	for (int i = threadIdx.x; i < 8 * kRadix; i += blockDim.x) (&h[0][0])[i] = 0;
+	__syncthreads();
+	const int lane = threadIdx.x & 31;
+	const size_t warp_global = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
+	const size_t warps_total = ((size_t)gridDim.x * blockDim.x) >> 5;
+	constexpr int PER = 16 / sizeof(K);  // keys per 16-byte load
+	const size_t chunks = (n + PER - 1) / PER;
+	const bool aligned = ((uintptr_t)keys % 16) == 0;
+	for (size_t base = warp_global * 32; base < chunks; base += warps_total * 32) {
+		const size_t c = base + lane;
+		K kv[PER];
+		bool valid[PER];
+		if (aligned && (c + 1) * PER <= n) {
+			uint4 v = dev::ld_stream_v4(reinterpret_cast<const uint4 *>(keys) + c);
+			const K *e = reinterpret_cast<const K *>(&v);
+#pragma unroll
+			for (int q = 0; q < PER; ++q) {
+				kv[q] = e[q];
+				valid[q] = true;
+			}
+		} else {
+#pragma unroll
+			for (int q = 0; q < PER; ++q) {
+				size_t i = c * PER + q;
+				valid[q] = i < n;
+				kv[q] = valid[q] ? keys[i] : (K)0;
+			}
+		}
+#pragma unroll
+		for (int q = 0; q < PER; ++q) {
+			for (int p = 0; p < passes; ++p) {
+				uint32_t d = digit_of(kv[q], p * kRadixBits);
+				uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
+				bool v0 = __shfl_sync(0xffffffffu, valid[q], 0);
+				if (__all_sync(0xffffffffu, valid[q] && d == d0) && v0) {
+					if (lane == 0) atomicAdd(&h[p][d], 32u);
+				} else if (valid[q]) {
+					atomicAdd(&h[p][d], 1u);
+				}
+			}
+		}
+	}
+	__syncthreads();
+	for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) {
+		uint32_t v = (&h[0][0])[i];
+		if (v) atomicAdd(hist + i, v);
+	}
+}
+
+// ----------------------------------------------------------- onesweep pass
+struct PassArgs {
+	const uint32_t *hist;   // 256 bins of this digit position
+	uint32_t *status;       // num_tiles * 256 words used by this pass
+	uint32_t *status_next;  // the other buffer, cleared for the next pass
+	uint32_t *tile_counter;
+	int *dev_status;
+	size_t n;
+	int shift;
+};
+
+template <typename K>
+__device__ __forceinline__ uint32_t peer_mask(uint32_t d) {
+	return __match_any_sync(0xffffffffu, d);
+}
+
+template <typename K, typename V, bool HAS_V>
+__global__ void __launch_bounds__(kThreads, 2)
+radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
+	const V *__restrict__ vin, V *__restrict__ vout, PassArgs a) {
+	constexpr int KPT = KeyCfg<K>::kKpt;
+	constexpr int TILE = KeyCfg<K>::kTile;
+	extern __shared__ __align__(16) unsigned char smem[];
+	uint32_t *s_hist = reinterpret_cast<uint32_t *>(smem);        // [kWarps][256]
+	uint32_t *s_tile_off = s_hist + kWarps * kRadix;               // [256]
+	uint32_t *s_glob = s_tile_off + kRadix;                        // [256]
+	uint32_t *s_misc = s_glob + kRadix;                            // [64]
+	unsigned char *s_stage = reinterpret_cast<unsigned char *>(s_misc + 64);
+
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	if (tid == 0) s_misc[0] = atomicAdd(a.tile_counter, 1u);
+	for (int i = lane; i < kRadix; i += 32) s_hist[warp * kRadix + i] = 0;
+	__syncthreads();
+	const uint32_t tile = s_misc[0];
+	const size_t tile_base = (size_t)tile * TILE;
+	const size_t wbase = tile_base + (size_t)warp * (KPT * 32);
+	const int shift = a.shift;
+
+	// a. load keys, warp-striped (out-of-range keys read as all-ones so they
+	//    rank last within digit 255 and are never written).
+	K k[KPT];
+#pragma unroll
+	for (int j = 0; j < KPT; ++j) {
+		size_t idx = wbase + (size_t)j * 32 + lane;
+		k[j] = idx < a.n ? kin[idx] : (K)~(K)0;
+	}
+
+	// b. warp multisplit ranks.
+	uint32_t rank[KPT];
+	uint32_t *my_hist = s_hist + warp * kRadix;
+#pragma unroll
+	for (int j = 0; j < KPT; ++j) {
+		uint32_t d = digit_of(k[j], shift);
+		uint32_t peers = peer_mask<K>(d);
+		uint32_t leader = __ffs(peers) - 1;
+		uint32_t cnt = __popc(peers);
+		uint32_t old = 0;
+		if (lane == (int)leader) old = atomicAdd(my_hist + d, cnt);
+		old = __shfl_sync(peers, old, leader);
+		rank[j] = old + __popc(peers & dev::lanemask_lt());
+	}
+	__syncthreads();
+
+	// c. per-digit tile counts, warp prefixes, publication and lookback.
+	uint32_t tile_cnt = 0;
+	if (tid < kRadix) {
+		uint32_t sum = 0;
+#pragma unroll
+		for (int w = 0; w < kWarps; ++w) {
+			uint32_t c = s_hist[w * kRadix + tid];
+			s_hist[w * kRadix + tid] = sum;
+			sum += c;
+		}
+		tile_cnt = sum;
+		uint32_t *st = a.status + (size_t)tile * kRadix + tid;
+		if (tile == 0) dev::st_relaxed_u32(st, kStPrefix | tile_cnt);
+		else dev::st_relaxed_u32(st, kStAgg | tile_cnt);
+		a.status_next[(size_t)tile * kRadix + tid] = 0;
+		// Exclusive scan of the tile counts over digits (warps 0..7).
+		uint32_t inc = tile_cnt;
+#pragma unroll
+		for (int d = 1; d < 32; d <<= 1) {
+			uint32_t t = __shfl_up_sync(0xffffffffu, inc, d);
+			if (lane >= d) inc += t;
+		}
+		if (lane == 31) s_misc[8 + warp] = inc;
+		s_tile_off[tid] = inc - tile_cnt;
+	}
+	// Global digit base: exclusive scan of this pass's histogram.
+	if (tid >= kRadix && tid < 2 * kRadix) {
+		int d = tid - kRadix;
+		uint32_t hv = a.hist[d];
+		uint32_t inc = hv;
+#pragma unroll
+		for (int s = 1; s < 32; s <<= 1) {
+			uint32_t t = __shfl_up_sync(0xffffffffu, inc, s);
+			if (lane >= s) inc += t;
+		}
+		if (lane == 31) s_misc[16 + (warp - 8)] = inc;
+		s_glob[d] = inc - hv;
+	}
+	__syncthreads();
+	if (tid < kRadix) {
+		uint32_t woff = 0, goff = 0;
+#pragma unroll
+		for (int w = 0; w < 8; ++w) {
+			if (w < warp) {
+				woff += s_misc[8 + w];
+				goff += s_misc[16 + w];
+			}
+		}
+		s_tile_off[tid] += woff;
+		uint32_t digit_base = s_glob[tid] + goff;
+		// Lookback over predecessor tiles for digit tid.
+		uint32_t excl = 0;
+		if (tile > 0) {
+			long long j = (long long)tile - 1;
+			uint32_t iter = 0;
+			while (j >= 0) {
+				uint32_t sv = dev::ld_relaxed_u32(a.status + (size_t)j * kRadix + tid);
+				if ((sv & ~kStValue) == 0) {
+					if (++iter >= dev::kSpinLimit) {
+						dev::report_timeout(a.dev_status, DEV_ERR_LOOKBACK_TIMEOUT,
+							(int)tile);
+						break;
+					}
+					dev::backoff(iter);
+					continue;
+				}
+				excl += sv & kStValue;
+				if (sv & kStPrefix) break;
+				--j;
+			}
+			dev::st_relaxed_u32(a.status + (size_t)tile * kRadix + tid,
+				kStPrefix | (excl + tile_cnt));
+		}
+		s_glob[tid] = digit_base + excl - s_tile_off[tid];
+	}
+	__syncthreads();
+
+	// d. stage keys in tile order, then write each digit run coalesced.
+	K *sk = reinterpret_cast<K *>(s_stage);
+#pragma unroll
+	for (int j = 0; j < KPT; ++j) {
+		uint32_t d = digit_of(k[j], shift);
+		uint32_t pos = s_tile_off[d] + s_hist[warp * kRadix + d] + rank[j];
+		rank[j] = pos;  // keep the tile position for the value pass
+		sk[pos] = k[j];
+	}
+	__syncthreads();
+	uint32_t outpos[HAS_V ? KPT : 1];
+#pragma unroll
+	for (int i = 0; i < KPT; ++i) {
+		int p = i * kThreads + tid;
+		K key = sk[p];
+		size_t o = (size_t)s_glob[digit_of(key, shift)] + p;
+		if (o < a.n) kout[o] = key;
+		if (HAS_V) outpos[i] = (uint32_t)o;
+	}
+	if (HAS_V) {
+		V v[KPT];
+#pragma unroll
+		for (int j = 0; j < KPT; ++j) {
+			size_t idx = wbase + (size_t)j * 32 + lane;
+			v[j] = idx < a.n ? vin[idx] : (V)0;
+		}
+		__syncthreads();
+		V *sv = reinterpret_cast<V *>(s_stage);
+#pragma unroll
+		for (int j = 0; j < KPT; ++j) sv[rank[j]] = v[j];
+		__syncthreads();
+#pragma unroll
+		for (int i = 0; i < KPT; ++i) {
+			int p = i * kThreads + tid;
+			if (outpos[i] < a.n) vout[outpos[i]] = sv[p];
+		}
+	}
+}
+
+template <typename K, typename V, bool HAS_V>
+size_t onesweep_smem() {
+	constexpr int TILE = KeyCfg<K>::kTile;
+	size_t stage = (size_t)TILE * (sizeof(K) > sizeof(V) || !HAS_V ? sizeof(K) : sizeof(V));
+	return (kWarps * kRadix + 2 * kRadix + 64) * sizeof(uint32_t) + stage;
+}
+
+template <typename K, typename V, bool HAS_V>
+cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
+	CCLContext *ctx, cudaStream_t s, bool allow_skip, GError **err) {
+	constexpr int TILE = KeyCfg<K>::kTile;
+	const int passes = sort_bits / kRadixBits;
+	if (n < 2 || passes == 0) return cudaSuccess;
+	if (n >= (size_t)kStValue) {
+		set_error(err, CLO_ERROR_ARGS,
+			"satradix: %zu elements exceed the single-sort limit of 2^30 - 1", n);
+		return cudaErrorInvalidValue;
+	}
+	const size_t tiles = (n + TILE - 1) / TILE;
+	const size_t status_words = tiles * kRadix;
+	// Scratch: [hist passes*256][counters 8][status0][status1][alt keys][alt vals]
+	size_t off_hist = 0;
+	size_t off_cnt = off_hist + (size_t)passes * kRadix * 4;
+	size_t off_st0 = off_cnt + 8 * 4;
+	size_t off_st1 = off_st0 + status_words * 4;
+	size_t off_keys = (off_st1 + status_words * 4 + 255) / 256 * 256;
+	size_t off_vals = (off_keys + n * sizeof(K) + 255) / 256 * 256;
+	size_t total = off_vals + (HAS_V ? n * sizeof(V) : 0);
+	char *tmp = (char *)tmp_alloc(ctx, total, s, err);
+	if (!tmp) return cudaErrorMemoryAllocation;
+	uint32_t *hist = (uint32_t *)(tmp + off_hist);
+	uint32_t *cnt = (uint32_t *)(tmp + off_cnt);
+	uint32_t *st[2] = {(uint32_t *)(tmp + off_st0), (uint32_t *)(tmp + off_st1)};
+	K *alt_k = (K *)(tmp + off_keys);
+	V *alt_v = (V *)(tmp + off_vals);
+	cudaError_t e = cudaMemsetAsync(tmp, 0, off_st1, s);
+	unsigned launches = 0;
+	if (e == cudaSuccess) {
+		int grid = ctx->sm_count * 4;
+		size_t chunks = (n * sizeof(K) + 15) / 16;
+		size_t need = (chunks + 255) / 256;
+		if ((size_t)grid > need) grid = (int)std::max<size_t>(need, 1);
+		KernelTimer t("satradix_upsweep", s, (double)n * sizeof(K));
+		radix_upsweep<K><<<grid, 256, 0, s>>>((const K *)keys, n, passes, hist);
+		t.stop();
+		launches++;
+		e = cudaGetLastError();
+	}
+	std::vector<int> active;
+	if (e == cudaSuccess) {
+		if (allow_skip && n >= (1u << 16)) {
+			std::vector<uint32_t> h((size_t)passes * kRadix);
+			e = cudaMemcpyAsync(h.data(), hist, h.size() * 4, cudaMemcpyDeviceToHost, s);
+			if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+			for (int p = 0; p < passes && e == cudaSuccess; ++p) {
+				bool trivial = false;
+				for (int d = 0; d < kRadix; ++d)
+					if (h[(size_t)p * kRadix + d] == n) trivial = true;
+				if (!trivial) active.push_back(p);
+			}
+		} else {
+			for (int p = 0; p < passes; ++p) active.push_back(p);
+		}
+	}
+	if (e == cudaSuccess) {
+		size_t smem = onesweep_smem<K, V, HAS_V>();
+		auto kern = radix_onesweep<K, V, HAS_V>;
+		e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			(int)smem);
+		K *src_k = (K *)keys, *dst_k = alt_k;
+		V *src_v = (V *)vals, *dst_v = alt_v;
+		for (size_t q = 0; q < active.size() && e == cudaSuccess; ++q) {
+			PassArgs pa;
+			pa.hist = hist + (size_t)active[q] * kRadix;
+			pa.status = st[q & 1];
+			pa.status_next = st[(q + 1) & 1];
+			pa.tile_counter = cnt + active[q];
+			pa.dev_status = ctx->d_status;
+			pa.n = n;
+			pa.shift = active[q] * kRadixBits;
+			KernelTimer t("satradix_onesweep", s,
+				2.0 * (double)n * (sizeof(K) + (HAS_V ? sizeof(V) : 0)));
+			kern<<<(unsigned)tiles, kThreads, smem, s>>>(src_k, dst_k, src_v, dst_v, pa);
+			t.stop();
+			launches++;
+			e = cudaGetLastError();
+			std::swap(src_k, dst_k);
+			std::swap(src_v, dst_v);
+		}
+		if (e == cudaSuccess && (active.size() & 1)) {
+			e = cudaMemcpyAsync(keys, alt_k, n * sizeof(K), cudaMemcpyDeviceToDevice, s);
+			if (e == cudaSuccess && HAS_V)
+				e = cudaMemcpyAsync(vals, alt_v, n * sizeof(V), cudaMemcpyDeviceToDevice, s);
+		}
+	}
+	count_launches(launches);
+	tmp_free(tmp, s);
+	if (e != cudaSuccess) cuda_ok(e, err, "satradix");
+	return e;
+}
+
+template <typename K>
+cudaError_t sort_keys_vals(void *keys, void *vals, size_t n, int val_bytes,
+	int sort_bits, CCLContext *ctx, cudaStream_t s, bool skip, GError **err) {
+	switch (val_bytes) {
+	case 0: return sort_typed<K, uint32_t, false>(keys, nullptr, n, sort_bits, ctx, s, skip, err);
+	case 4: return sort_typed<K, uint32_t, true>(keys, vals, n, sort_bits, ctx, s, skip, err);
+	case 8: return sort_typed<K, uint64_t, true>(keys, vals, n, sort_bits, ctx, s, skip, err);
+	}
+	set_error(err, CLO_ERROR_ARGS, "Unsupported value width %d", val_bytes);
+	return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+cudaError_t radix_sort(void *keys, void *vals, size_t n, int key_bytes,
+	int val_bytes, int sort_bits, CCLContext *ctx, cudaStream_t s,
+	bool allow_skip, GError **err) {
+	switch (key_bytes) {
+	case 1: return sort_keys_vals<uint8_t>(keys, vals, n, val_bytes, sort_bits, ctx, s, allow_skip, err);
+	case 2: return sort_keys_vals<uint16_t>(keys, vals, n, val_bytes, sort_bits, ctx, s, allow_skip, err);
+	case 4: return sort_keys_vals<uint32_t>(keys, vals, n, val_bytes, sort_bits, ctx, s, allow_skip, err);
+	case 8: return sort_keys_vals<uint64_t>(keys, vals, n, val_bytes, sort_bits, ctx, s, allow_skip, err);
+	}
+	set_error(err, CLO_ERROR_ARGS, "Unsupported key width %d", key_bytes);
+	return cudaErrorInvalidValue;
+}
+
+}  // namespace clo

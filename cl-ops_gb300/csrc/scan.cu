@@ -1,0 +1,291 @@
+// Exclusive prefix sum ("blelloch" scanner) as one single-pass kernel with
+// decoupled lookback.
+//
+// Semantics follow src/cl_ops/scan/clo_scan_blelloch.cl:49-211: out[0] = 0
+// and out[i] = sum_{j<i} (SUM_TYPE) in[j], with the element converted to
+// the sum type by C rules and the sum wrapping modulo 2^(8*sizeof(SUM)).
+// Integer addition is associative, so the result is bit-identical to the
+// reference's work-group Blelloch trees whatever the summation order.
+//
+// Layout: tiles of 4096 elements, 256 threads, 16 consecutive elements per
+// thread. Each warp moves its 512-element segment between global memory
+// and registers through a padded shared-memory transpose, so every global
+// access is a coalesced 16-byte vector access. Tiles take ids from an
+// atomic counter (so a tile only ever waits on tiles already running),
+// publish their aggregate, then warp 0 looks back over a 32-tile window
+// per step until it meets an inclusive prefix. Every wait is bounded.
+//
+// HBM roofline: sizeof(in) + sizeof(out) bytes per element (12 B for
+// uint -> ulong), plus 20 B of tile status per 4096 elements.
+#include <type_traits>
+
+#include "clo_internal.h"
+#include "dev_common.cuh"
+#include "timing.h"
+
+namespace clo {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kItems = 16;
+constexpr int kWarpElems = 32 * kItems;
+constexpr int kTile = kWarps * kWarpElems;
+constexpr int kPadded = kWarpElems + kWarpElems / 32;
+
+constexpr uint32_t kFlagAgg = 1, kFlagPrefix = 2;
+
+__device__ __forceinline__ int pidx(int i) { return i + (i >> 5); }
+
+template <typename Acc>
+struct TileStatus {
+	uint32_t *flags;  // num_tiles + 1 (the last word is the tile counter)
+	Acc *agg;
+	Acc *pre;
+};
+
+template <typename Acc>
+__device__ __forceinline__ Acc shfl_up(Acc v, int d) {
+	return __shfl_up_sync(0xffffffffu, v, d);
+}
+
+template <typename Acc>
+__device__ __forceinline__ Acc warp_sum(Acc v) {
+#pragma unroll
+	for (int d = 16; d >= 1; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+	return v;
+}
+
+template <typename InT, typename OutT>
+__global__ void __launch_bounds__(kThreads)
+scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, size_t n,
+	TileStatus<typename std::conditional<(sizeof(OutT) <= 4), uint32_t,
+		uint64_t>::type> ts,
+	int *dev_status, bool vec_ok, long long debug_skip_tile) {
+	using Acc = typename std::conditional<(sizeof(OutT) <= 4), uint32_t,
+		uint64_t>::type;
+	constexpr int ESZ = sizeof(InT) > sizeof(OutT) ? sizeof(InT) : sizeof(OutT);
+	__shared__ __align__(16) unsigned char s_buf[kWarps][kPadded * ESZ];
+	__shared__ Acc s_warp_tot[kWarps];
+	__shared__ Acc s_excl;
+	__shared__ uint32_t s_tile;
+
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const uint32_t num_tiles = (uint32_t)((n + kTile - 1) / kTile);
+	if (tid == 0) s_tile = atomicAdd(ts.flags + num_tiles, 1u);
+	__syncthreads();
+	const uint32_t tile = s_tile;
+	const size_t seg = (size_t)tile * kTile + (size_t)warp * kWarpElems;
+	const bool full = seg + kWarpElems <= n;
+
+	// ---- load the warp's segment (coalesced) into padded smem -----------
+	InT *sin = reinterpret_cast<InT *>(s_buf[warp]);
+	if (full && vec_ok) {
+		constexpr int EPC = 16 / sizeof(InT);
+		constexpr int CHUNKS = kWarpElems / EPC;
+		const uint4 *src = reinterpret_cast<const uint4 *>(in + seg);
+#pragma unroll
+		for (int c = lane; c < CHUNKS; c += 32) {
+			uint4 v = dev::ld_stream_v4(src + c);
+			const InT *e = reinterpret_cast<const InT *>(&v);
+#pragma unroll
+			for (int k = 0; k < EPC; ++k) sin[pidx(c * EPC + k)] = e[k];
+		}
+	} else {
+		for (int i = lane; i < kWarpElems; i += 32)
+			sin[pidx(i)] = (seg + i < n) ? in[seg + i] : (InT)0;
+	}
+	__syncwarp();
+
+	// ---- per-thread sequential scan of 16 consecutive elements ----------
+	Acc x[kItems];
+	Acc run = 0;
+#pragma unroll
+	for (int j = 0; j < kItems; ++j) {
+		Acc v = (Acc)(OutT)sin[pidx(lane * kItems + j)];
+		x[j] = run;  // exclusive within the thread
+		run += v;
+	}
+	// Warp inclusive scan of thread totals.
+	Acc inc = run;
+#pragma unroll
+	for (int d = 1; d < 32; d <<= 1) {
+		Acc t = shfl_up(inc, d);
+		if (lane >= d) inc += t;
+	}
+	const Acc lane_excl = inc - run;
+	if (lane == 31) s_warp_tot[warp] = inc;
+	__syncthreads();
+
+	// ---- tile aggregate, publication and lookback (warp 0) --------------
+	if (warp == 0) {
+		Acc wt = lane < kWarps ? s_warp_tot[lane] : (Acc)0;
+		Acc winc = wt;
+#pragma unroll
+		for (int d = 1; d < kWarps; d <<= 1) {
+			Acc t = shfl_up(winc, d);
+			if (lane >= d) winc += t;
+		}
+		const Acc aggregate = __shfl_sync(0xffffffffu, winc, kWarps - 1);
+		if (lane < kWarps) s_warp_tot[lane] = winc - wt;  // warp exclusive
+		const bool publish = (long long)tile != debug_skip_tile;
+		Acc excl = 0;
+		if (tile == 0) {
+			if (lane == 0 && publish) {
+				ts.pre[0] = aggregate;
+				dev::st_release_u32(ts.flags + 0, kFlagPrefix);
+			}
+		} else {
+			if (lane == 0 && publish) {
+				ts.agg[tile] = aggregate;
+				dev::st_release_u32(ts.flags + tile, kFlagAgg);
+			}
+			long long pred = (long long)tile - 1;
+			for (;;) {
+				const long long t = pred - lane;
+				uint32_t f = t >= 0 ? dev::ld_relaxed_u32(ts.flags + t) : kFlagPrefix;
+				bool gave_up = false;
+				uint32_t iter = 0;
+				while (__any_sync(0xffffffffu, f == 0)) {
+					if (f == 0) {
+						if (iter >= dev::kSpinLimit) {
+							// Give up: record the failure and treat the
+							// predecessor as a zero prefix so the kernel ends.
+							dev::report_timeout(dev_status, DEV_ERR_LOOKBACK_TIMEOUT,
+								(int)tile);
+							f = kFlagPrefix;
+							gave_up = true;
+						} else {
+							dev::backoff(iter);
+							f = dev::ld_relaxed_u32(ts.flags + t);
+						}
+					}
+					++iter;
+				}
+				__threadfence();
+				Acc v = 0;
+				if (t >= 0 && !gave_up) v = f == kFlagPrefix ? ts.pre[t] : ts.agg[t];
+				const uint32_t pmask = __ballot_sync(0xffffffffu, f == kFlagPrefix);
+				if (pmask) {
+					const int first = __ffs(pmask) - 1;
+					excl += warp_sum<Acc>(lane <= first ? v : (Acc)0);
+					break;
+				}
+				excl += warp_sum<Acc>(v);
+				pred -= 32;
+			}
+			if (lane == 0 && publish) {
+				ts.pre[tile] = excl + aggregate;
+				dev::st_release_u32(ts.flags + tile, kFlagPrefix);
+			}
+		}
+		if (lane == 0) s_excl = excl;
+	}
+	__syncthreads();
+
+	// ---- outputs through padded smem, coalesced stores -------------------
+	const Acc base = s_excl + s_warp_tot[warp] + lane_excl;
+	OutT *sout = reinterpret_cast<OutT *>(s_buf[warp]);
+#pragma unroll
+	for (int j = 0; j < kItems; ++j) sout[pidx(lane * kItems + j)] = (OutT)(base + x[j]);
+	__syncwarp();
+	if (full && vec_ok) {
+		constexpr int EPC = 16 / sizeof(OutT);
+		constexpr int CHUNKS = kWarpElems / EPC;
+		uint4 *dst = reinterpret_cast<uint4 *>(out + seg);
+#pragma unroll
+		for (int c = lane; c < CHUNKS; c += 32) {
+			uint4 v;
+			OutT *e = reinterpret_cast<OutT *>(&v);
+#pragma unroll
+			for (int k = 0; k < EPC; ++k) e[k] = sout[pidx(c * EPC + k)];
+			dev::st_stream_v4(dst + c, v);
+		}
+	} else {
+		for (int i = lane; i < kWarpElems; i += 32)
+			if (seg + i < n) out[seg + i] = sout[pidx(i)];
+	}
+}
+
+template <typename InT, typename OutT>
+cudaError_t launch_scan(const void *in, void *out, size_t n, CCLContext *ctx,
+	cudaStream_t s, GError **err, long long debug_skip_tile) {
+	using Acc = typename std::conditional<(sizeof(OutT) <= 4), uint32_t,
+		uint64_t>::type;
+	const size_t tiles = (n + kTile - 1) / kTile;
+	if (tiles >= (1ull << 31)) {
+		set_error(err, CLO_ERROR_ARGS, "Scan of %zu elements is too large", n);
+		return cudaErrorInvalidValue;
+	}
+	size_t flag_bytes = ((tiles + 1) * sizeof(uint32_t) + 15) / 16 * 16;
+	size_t bytes = flag_bytes + 2 * tiles * sizeof(Acc);
+	char *tmp = (char *)tmp_alloc(ctx, bytes, s, err);
+	if (!tmp) return cudaErrorMemoryAllocation;
+	TileStatus<Acc> ts;
+	ts.flags = (uint32_t *)tmp;
+	ts.agg = (Acc *)(tmp + flag_bytes);
+	ts.pre = ts.agg + tiles;
+	cudaError_t e = cudaMemsetAsync(tmp, 0, (tiles + 1) * sizeof(uint32_t), s);
+	bool vec_ok = ((uintptr_t)in % 16 == 0) && ((uintptr_t)out % 16 == 0);
+	if (e == cudaSuccess) {
+		KernelTimer t("scan_lookback", s, (double)n * (sizeof(InT) + sizeof(OutT)));
+		scan_lookback<InT, OutT><<<(unsigned)tiles, kThreads, 0, s>>>(
+			(const InT *)in, (OutT *)out, n, ts, ctx->d_status, vec_ok,
+			debug_skip_tile);
+		t.stop();
+		count_launches(1);
+		e = cudaGetLastError();
+	}
+	tmp_free(tmp, s);
+	if (e != cudaSuccess) cuda_ok(e, err, "scan_lookback");
+	return e;
+}
+
+template <typename InT>
+cudaError_t dispatch_out(const void *in, void *out, size_t n, int out_bytes,
+	CCLContext *ctx, cudaStream_t s, GError **err, long long dbg) {
+	switch (out_bytes) {
+	case 1: return launch_scan<InT, uint8_t>(in, out, n, ctx, s, err, dbg);
+	case 2: return launch_scan<InT, uint16_t>(in, out, n, ctx, s, err, dbg);
+	case 4: return launch_scan<InT, uint32_t>(in, out, n, ctx, s, err, dbg);
+	case 8: return launch_scan<InT, uint64_t>(in, out, n, ctx, s, err, dbg);
+	}
+	set_error(err, CLO_ERROR_ARGS, "Unsupported sum width %d", out_bytes);
+	return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+// Tile whose publication is withheld (-1: none). Only the watchdog test
+// sets it, through clo_gb300_debug_scan_withhold().
+static long long g_debug_skip_tile = -1;
+
+cudaError_t scan_exclusive(const void *in, void *out, size_t n,
+	CloType in_type, int out_bytes, CCLContext *ctx, cudaStream_t s,
+	GError **err) {
+	if (n == 0) return cudaSuccess;
+	long long dbg = g_debug_skip_tile;
+	switch (in_type) {
+	case CLO_CHAR: return dispatch_out<int8_t>(in, out, n, out_bytes, ctx, s, err, dbg);
+	case CLO_UCHAR: return dispatch_out<uint8_t>(in, out, n, out_bytes, ctx, s, err, dbg);
+	case CLO_SHORT: return dispatch_out<int16_t>(in, out, n, out_bytes, ctx, s, err, dbg);
+	case CLO_USHORT: return dispatch_out<uint16_t>(in, out, n, out_bytes, ctx, s, err, dbg);
+	case CLO_INT: return dispatch_out<int32_t>(in, out, n, out_bytes, ctx, s, err, dbg);
+	case CLO_UINT: return dispatch_out<uint32_t>(in, out, n, out_bytes, ctx, s, err, dbg);
+	case CLO_LONG: return dispatch_out<int64_t>(in, out, n, out_bytes, ctx, s, err, dbg);
+	case CLO_ULONG: return dispatch_out<uint64_t>(in, out, n, out_bytes, ctx, s, err, dbg);
+	default: break;
+	}
+	set_error(err, CLO_ERROR_ARGS, "Unsupported scan element type %d", (int)in_type);
+	return cudaErrorInvalidValue;
+}
+
+}  // namespace clo
+
+// Test hook for the lookback watchdog: the given tile of the next scans
+// never publishes its status, so its successor's bounded wait runs out
+// and reports through the context status word. -1 restores normal
+// operation.
+extern "C" void clo_gb300_debug_scan_withhold(long long tile) {
+	clo::g_debug_skip_tile = tile;
+}

@@ -1,0 +1,743 @@
+// Sorter objects: registry, option parsing, device-data and host-data
+// entry points for "sbitonic", "abitonic", "gselect" and "satradix".
+// Reference behaviour: src/cl_ops/sort/clo_sort_abstract.c:91-631 and the
+// per-implementation drivers clo_sort_{sbitonic,abitonic,gselect,
+// satradix}.c.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "clo_internal.h"
+
+using clo::cuda_ok;
+using clo::set_error;
+
+struct clo_sort {
+	CloSortImplDef impl_def;
+	CCLContext *ctx;
+	CCLProgram *prg;
+	CloType elem_type;
+	CloType key_type;
+	void *data;
+};
+
+namespace {
+
+// Removes blanks so that "((a) > (b))" and "((a)>(b))" compare equal.
+std::string squeeze(const char *s) {
+	std::string r;
+	for (; s && *s; ++s)
+		if (*s != ' ' && *s != '\t' && *s != '\n' && *s != '\r') r += *s;
+	return r;
+}
+
+bool compare_is_default(const char *c) {
+	if (c == nullptr) return true;
+	std::string s = squeeze(c);
+	return s == "((a)>(b))" || s == "(a>b)" || s == "a>b" || s == "(a)>(b)";
+}
+
+bool get_key_is_default(const char *k) {
+	if (k == nullptr) return true;
+	std::string s = squeeze(k);
+	return s == "(x)" || s == "x";
+}
+
+// Splits "k1=v1,k2=v2" like the reference's g_strsplit_set(",") then
+// g_strsplit_set("=", 2); empty tokens are skipped. Calls f(key, value,
+// token) and stops at the first false.
+template <typename F>
+bool for_each_option(const char *options, F f) {
+	if (!options) return true;
+	std::string all(options);
+	size_t pos = 0;
+	while (pos <= all.size()) {
+		size_t comma = all.find(',', pos);
+		if (comma == std::string::npos) comma = all.size();
+		std::string tok = all.substr(pos, comma - pos);
+		pos = comma + 1;
+		if (tok.empty()) continue;
+		size_t eq = tok.find('=');
+		std::string key = eq == std::string::npos ? tok : tok.substr(0, eq);
+		std::string val = eq == std::string::npos ? std::string() : tok.substr(eq + 1);
+		if (!f(key, val, tok, eq != std::string::npos)) return false;
+	}
+	return true;
+}
+
+bool check_numel(CloSort *s, CCLBuffer *b, size_t numel, GError **err) {
+	size_t need = numel * clo_type_sizeof(s->elem_type);
+	if (b == nullptr) {
+		set_error(err, CLO_ERROR_ARGS, "NULL data buffer");
+		return false;
+	}
+	if (need > b->size) {
+		set_error(err, CLO_ERROR_ARGS,
+			"Buffer of %zu bytes cannot hold %zu elements of type %s",
+			b->size, numel, clo_type_get_name(s->elem_type));
+		return false;
+	}
+	return true;
+}
+
+// Copies data_in to data_out (when given) and returns the buffer to sort.
+CCLBuffer *target_buffer(CloSort *s, CCLQueue *q, CCLBuffer *in,
+	CCLBuffer *out, size_t numel, GError **err) {
+	if (out == nullptr || out == in) return in;
+	if (!check_numel(s, out, numel, err)) return nullptr;
+	size_t bytes = numel * clo_type_sizeof(s->elem_type);
+	if (bytes && !cuda_ok(cudaMemcpyAsync(out->ptr, in->ptr, bytes,
+			cudaMemcpyDeviceToDevice, q->stream), err, "sort copy"))
+		return nullptr;
+	return out;
+}
+
+// ============================================================ satradix
+struct SatradixData {
+	unsigned radix;
+	std::string scan_type;
+	std::string scan_opts;
+	CloScan *scanner;
+};
+
+const char *kSatradixKernels[] = {"satradix_upsweep", "satradix_onesweep"};
+
+CloScan *satradix_get_scanner(CloSort *s, GError **err) {
+	SatradixData *d = (SatradixData *)s->data;
+	if (d->scanner == nullptr) {
+		d->scanner = clo_scan_new(d->scan_type.c_str(), d->scan_opts.c_str(),
+			s->ctx, CLO_UINT, CLO_UINT, s->prg ? s->prg->opts.c_str() : nullptr,
+			err);
+	}
+	return d->scanner;
+}
+
+// Number of low key bits the reference's satradix passes actually order:
+// passes run over the *element* width (clo_sort_satradix.c:167-169) but
+// shift the *key*, whose shift count OpenCL masks to the key width, so
+// the sorted bits are the low min(key, element) bits of the key.
+int satradix_sort_bits(CloSort *s) {
+	size_t eb = clo_type_sizeof(s->elem_type), kb = clo_type_sizeof(s->key_type);
+	return (int)(8 * (eb < kb ? eb : kb));
+}
+
+const char *satradix_init(CloSort *s, const char *options, GError **err) {
+	SatradixData *d = new SatradixData();
+	d->radix = 16;
+	d->scanner = nullptr;
+	s->data = d;
+	bool ok = for_each_option(options, [&](const std::string &k,
+		const std::string &v, const std::string &tok, bool has_eq) {
+		if (!has_eq) {
+			set_error(err, CLO_ERROR_ARGS,
+				"Invalid option '%s' for satradix sort.", tok.c_str());
+			return false;
+		}
+		if (k == "radix") {
+			d->radix = (unsigned)atoi(v.c_str());
+			if (clo_ones32(d->radix) != 1) {
+				set_error(err, CLO_ERROR_ARGS, "Radix must be a power of 2.");
+				return false;
+			}
+		} else if (k.size() >= 4 && strncasecmp(k.c_str(), "scan", 4) == 0) {
+			if (k.size() == 4) d->scan_type = v;
+			else d->scan_opts += tok.substr(4) + ",";
+		} else {
+			set_error(err, CLO_ERROR_ARGS,
+				"Invalid option key '%s' for satradix sort.", k.c_str());
+			return false;
+		}
+		return true;
+	});
+	if (!ok) return nullptr;
+	if (d->scan_type.empty()) d->scan_type = "blelloch";
+	if (!clo::type_is_integer(s->elem_type) ||
+		!clo::type_is_integer(s->key_type)) {
+		set_error(err, CLO_ERROR_ARGS,
+			"satradix sorts integer keys only (element '%s', key '%s')",
+			clo_type_get_name(s->elem_type), clo_type_get_name(s->key_type));
+		return nullptr;
+	}
+	return "sm_103a:satradix(onesweep, 8-bit digits)";
+}
+
+void satradix_finalize(CloSort *s) {
+	SatradixData *d = (SatradixData *)s->data;
+	if (!d) return;
+	if (d->scanner) clo_scan_destroy(d->scanner);
+	delete d;
+	s->data = nullptr;
+}
+
+CCLEvent *satradix_sort(CloSort *s, CCLQueue *cq_exec, CCLQueue *cq_comm,
+	CCLBuffer *in, CCLBuffer *out, size_t numel, size_t lws_max,
+	GError **err) {
+	(void)cq_comm;
+	(void)lws_max;
+	if (!check_numel(s, in, numel, err)) return nullptr;
+	GError *e2 = nullptr;
+	// The reference creates its scanner on the first sort; doing the same
+	// validates the scan= options at the same point.
+	if (!satradix_get_scanner(s, &e2)) {
+		clo::propagate_error(err, e2);
+		return nullptr;
+	}
+	ccl_event *ev = clo::event_begin(cq_exec, "satradix");
+	CCLBuffer *tgt = target_buffer(s, cq_exec, in, out, numel, err);
+	if (!tgt) return nullptr;
+	int kb = (int)clo_type_sizeof(s->elem_type);
+	bool skip = !clo::stream_capturing(cq_exec->stream);
+	if (clo::radix_sort(tgt->ptr, nullptr, numel, kb, 0, satradix_sort_bits(s),
+			s->ctx, cq_exec->stream, skip, err) != cudaSuccess)
+		return nullptr;
+	clo::event_end(ev);
+	return ev;
+}
+
+cl_uint satradix_num_kernels(CloSort *s, GError **err) {
+	CloScan *sc = satradix_get_scanner(s, err);
+	if (!sc) return 0;
+	return 2 + clo_scan_get_num_kernels(sc, err);
+}
+
+const char *satradix_kernel_name(CloSort *s, cl_uint i, GError **err) {
+	if (i < 2) return kSatradixKernels[i];
+	CloScan *sc = satradix_get_scanner(s, err);
+	if (!sc) return nullptr;
+	return clo_scan_get_kernel_name(sc, i - 2, err);
+}
+
+// Shared-memory footprint of the onesweep kernels (fixed tile shapes).
+size_t radix_localmem(size_t elem, cl_uint i) {
+	if (i == 0) return 4 * 256 * sizeof(cl_uint);
+	size_t tile = elem <= 4 ? 8192 : 4096;
+	return tile * elem + 16 * 256 * sizeof(cl_uint) + 4 * 256 * sizeof(cl_uint);
+}
+
+size_t satradix_localmem(CloSort *s, cl_uint i, size_t lws_max, size_t numel,
+	GError **err) {
+	if (i < 2) return radix_localmem(clo_sort_get_element_size(s), i);
+	CloScan *sc = satradix_get_scanner(s, err);
+	if (!sc) return 0;
+	return clo_scan_get_localmem_usage(sc, i - 2, lws_max, numel, err);
+}
+
+// ============================================================ bitonic
+struct AbitonicData {
+	unsigned max_ps;
+	unsigned min_ps;
+	unsigned max_sfs;
+};
+
+const char *sbitonic_init(CloSort *s, const char *options, GError **err) {
+	(void)options;
+	s->data = nullptr;
+	if (s->key_type != s->elem_type) {
+		set_error(err, CLO_ERROR_ARGS,
+			"sbitonic: a key type different from the element type needs a "
+			"get_key snippet, which the compiled-in kernels do not take");
+		return nullptr;
+	}
+	return "sm_103a:sbitonic(one network step per launch)";
+}
+
+const char *abitonic_init(CloSort *s, const char *options, GError **err) {
+	AbitonicData *d = new AbitonicData{4, 1, 0xffffffffu};
+	s->data = d;
+	bool ok = for_each_option(options, [&](const std::string &k,
+		const std::string &v, const std::string &tok, bool has_eq) {
+		if (!has_eq) {
+			set_error(err, CLO_ERROR_ARGS,
+				"Invalid option '%s' for abitonic sort.", tok.c_str());
+			return false;
+		}
+		unsigned value = (unsigned)atoi(v.c_str());
+		if (k == "minps") {
+			if (value > 4 || value < 1) {
+				set_error(err, CLO_ERROR_ARGS,
+					"Option 'minps' must be between 1 and 4.");
+				return false;
+			}
+			d->min_ps = value;
+		} else if (k == "maxps") {
+			if (value > 4 || value < 1) {
+				set_error(err, CLO_ERROR_ARGS,
+					"Option 'maxps' must be between 1 and 4.");
+				return false;
+			}
+			d->max_ps = value;
+		} else if (k == "maxsfs") {
+			d->max_sfs = value;
+		} else {
+			set_error(err, CLO_ERROR_ARGS,
+				"Invalid option key '%s' for abitonic sort.", k.c_str());
+			return false;
+		}
+		return true;
+	});
+	if (!ok) return nullptr;
+	if (options && d->max_ps < d->min_ps) {
+		set_error(err, CLO_ERROR_ARGS,
+			"'minps' (%u) must be less or equal than 'maxps' (%u).",
+			d->min_ps, d->max_ps);
+		return nullptr;
+	}
+	if (s->key_type != s->elem_type) {
+		set_error(err, CLO_ERROR_ARGS,
+			"abitonic: a key type different from the element type needs a "
+			"get_key snippet, which the compiled-in kernels do not take");
+		return nullptr;
+	}
+	return "sm_103a:abitonic(shared-memory tiles + register passes)";
+}
+
+void bitonic_finalize(CloSort *s) {
+	delete (AbitonicData *)s->data;
+	s->data = nullptr;
+}
+
+}  // namespace
+
+namespace clo {
+// Implemented in bitonic.cu: one global compare-exchange step per launch,
+// and the grouped form with explicit grouping limits.
+cudaError_t bitonic_sort_simple(void *data, size_t n, CloType type,
+	CCLContext *ctx, cudaStream_t s, GError **err);
+cudaError_t bitonic_sort_tuned(void *data, size_t n, CloType type, int max_ps,
+	int max_sfs, CCLContext *ctx, cudaStream_t s, GError **err);
+}
+
+namespace {
+
+CCLEvent *bitonic_sort_common(CloSort *s, CCLQueue *q, CCLBuffer *in,
+	CCLBuffer *out, size_t numel, bool simple, GError **err) {
+	if (!check_numel(s, in, numel, err)) return nullptr;
+	ccl_event *ev = clo::event_begin(q, simple ? "sbitonic" : "abitonic");
+	CCLBuffer *tgt = target_buffer(s, q, in, out, numel, err);
+	if (!tgt) return nullptr;
+	// abitonic's maxps bounds the steps grouped per global pass and maxsfs
+	// the largest step finished in shared memory (clo_sort_abitonic.c:
+	// 155-157); neither changes the result.
+	AbitonicData *d = (AbitonicData *)s->data;
+	cudaError_t e = simple
+		? clo::bitonic_sort_simple(tgt->ptr, numel, s->elem_type, s->ctx,
+			q->stream, err)
+		: clo::bitonic_sort_tuned(tgt->ptr, numel, s->elem_type,
+			d ? (int)d->max_ps : 4,
+			d && d->max_sfs < 64 ? (int)d->max_sfs : 0, s->ctx, q->stream, err);
+	if (e != cudaSuccess) return nullptr;
+	clo::event_end(ev);
+	return ev;
+}
+
+CCLEvent *sbitonic_sort(CloSort *s, CCLQueue *cq_exec, CCLQueue *cq_comm,
+	CCLBuffer *in, CCLBuffer *out, size_t numel, size_t lws_max,
+	GError **err) {
+	(void)cq_comm;
+	(void)lws_max;
+	return bitonic_sort_common(s, cq_exec, in, out, numel, true, err);
+}
+
+CCLEvent *abitonic_sort(CloSort *s, CCLQueue *cq_exec, CCLQueue *cq_comm,
+	CCLBuffer *in, CCLBuffer *out, size_t numel, size_t lws_max,
+	GError **err) {
+	(void)cq_comm;
+	(void)lws_max;
+	return bitonic_sort_common(s, cq_exec, in, out, numel, false, err);
+}
+
+const char *kSbitonicKernels[] = {"sbitonic_step"};
+const char *kAbitonicKernels[] = {"abitonic_tile_sort", "abitonic_global_steps",
+	"abitonic_tile_finish"};
+
+cl_uint sbitonic_num_kernels(CloSort *, GError **) { return 1; }
+const char *sbitonic_kernel_name(CloSort *, cl_uint i, GError **err) {
+	if (i >= 1) {
+		set_error(err, CLO_ERROR_ARGS, "Kernel index %u out of range", i);
+		return nullptr;
+	}
+	return kSbitonicKernels[0];
+}
+size_t sbitonic_localmem(CloSort *, cl_uint, size_t, size_t, GError **) {
+	return 0;
+}
+
+cl_uint abitonic_num_kernels(CloSort *, GError **) { return 3; }
+const char *abitonic_kernel_name(CloSort *, cl_uint i, GError **err) {
+	if (i >= 3) {
+		set_error(err, CLO_ERROR_ARGS, "Kernel index %u out of range", i);
+		return nullptr;
+	}
+	return kAbitonicKernels[i];
+}
+size_t abitonic_localmem(CloSort *s, cl_uint i, size_t, size_t,
+	GError **) {
+	size_t eb = clo_sort_get_element_size(s);
+	size_t tile = eb >= 8 ? 8192 : 16384;
+	return i == 1 ? 0 : tile * eb + tile / 32 * eb;
+}
+
+// ============================================================ gselect
+const char *gselect_init(CloSort *s, const char *options, GError **err) {
+	(void)options;
+	s->data = nullptr;
+	if (s->key_type != s->elem_type) {
+		set_error(err, CLO_ERROR_ARGS,
+			"gselect: a key type different from the element type needs a "
+			"get_key snippet, which the compiled-in kernels do not take");
+		return nullptr;
+	}
+	return "sm_103a:gselect(rank by counting)";
+}
+
+void gselect_finalize(CloSort *s) { (void)s; }
+
+CCLEvent *gselect_sort(CloSort *s, CCLQueue *q, CCLQueue *cq_comm,
+	CCLBuffer *in, CCLBuffer *out, size_t numel, size_t lws_max,
+	GError **err) {
+	(void)cq_comm;
+	(void)lws_max;
+	if (!check_numel(s, in, numel, err)) return nullptr;
+	ccl_event *ev = clo::event_begin(q, "gselect");
+	size_t bytes = numel * clo_type_sizeof(s->elem_type);
+	if (out != nullptr && out != in) {
+		if (!check_numel(s, out, numel, err)) return nullptr;
+		if (clo::gselect_sort(in->ptr, out->ptr, numel, s->elem_type, nullptr,
+				nullptr, 0, s->ctx, q->stream, err) != cudaSuccess)
+			return nullptr;
+	} else {
+		// No output buffer: sort into a temporary and copy back, as the
+		// reference does (clo_sort_gselect.c:82-124).
+		void *tmp = clo::tmp_alloc(s->ctx, bytes, q->stream, err);
+		if (!tmp) return nullptr;
+		if (clo::gselect_sort(in->ptr, tmp, numel, s->elem_type, nullptr,
+				nullptr, 0, s->ctx, q->stream, err) != cudaSuccess) {
+			clo::tmp_free(tmp, q->stream);
+			return nullptr;
+		}
+		bool ok = cuda_ok(cudaMemcpyAsync(in->ptr, tmp, bytes,
+			cudaMemcpyDeviceToDevice, q->stream), err, "gselect copy back");
+		clo::tmp_free(tmp, q->stream);
+		if (!ok) return nullptr;
+	}
+	clo::event_end(ev);
+	return ev;
+}
+
+cl_uint gselect_num_kernels(CloSort *, GError **) { return 1; }
+const char *gselect_kernel_name(CloSort *, cl_uint i, GError **err) {
+	if (i >= 1) {
+		set_error(err, CLO_ERROR_ARGS, "Kernel index %u out of range", i);
+		return nullptr;
+	}
+	return "gselect";
+}
+size_t gselect_localmem(CloSort *s, cl_uint, size_t, size_t, GError **) {
+	return 2048 * clo_sort_get_element_size(s);
+}
+
+}  // namespace
+
+extern "C" {
+
+const CloSortImplDef clo_sort_sbitonic_def = {"sbitonic", CL_TRUE,
+	sbitonic_init, bitonic_finalize, sbitonic_sort, sbitonic_num_kernels,
+	sbitonic_kernel_name, sbitonic_localmem};
+
+const CloSortImplDef clo_sort_abitonic_def = {"abitonic", CL_TRUE,
+	abitonic_init, bitonic_finalize, abitonic_sort, abitonic_num_kernels,
+	abitonic_kernel_name, abitonic_localmem};
+
+const CloSortImplDef clo_sort_gselect_def = {"gselect", CL_FALSE,
+	gselect_init, gselect_finalize, gselect_sort, gselect_num_kernels,
+	gselect_kernel_name, gselect_localmem};
+
+const CloSortImplDef clo_sort_satradix_def = {"satradix", CL_TRUE,
+	satradix_init, satradix_finalize, satradix_sort, satradix_num_kernels,
+	satradix_kernel_name, satradix_localmem};
+
+CloSort *clo_sort_new(const char *type, const char *options, CCLContext *ctx,
+	CloType *elem_type, CloType *key_type, const char *compare,
+	const char *get_key, const char *compiler_opts, GError **err) {
+	if (err != nullptr && *err != nullptr) return nullptr;
+	const CloSortImplDef *impls[] = {&clo_sort_sbitonic_def,
+		&clo_sort_abitonic_def, &clo_sort_gselect_def, &clo_sort_satradix_def};
+	const CloSortImplDef *def = nullptr;
+	for (const CloSortImplDef *d : impls)
+		if (type && strcmp(type, d->name) == 0) def = d;
+	if (!def) {
+		set_error(err, CLO_ERROR_IMPL_NOT_FOUND,
+			"The requested sort implementation, '%s', was not found.",
+			type ? type : "(null)");
+		return nullptr;
+	}
+	if (!ctx || !elem_type || clo_type_sizeof(*elem_type) == 0 ||
+		(key_type && clo_type_sizeof(*key_type) == 0)) {
+		set_error(err, CLO_ERROR_ARGS, "Invalid context or element/key type");
+		return nullptr;
+	}
+	CloSort *s = new clo_sort();
+	s->impl_def = *def;
+	ccl_context_ref(ctx);
+	s->ctx = ctx;
+	s->prg = nullptr;
+	s->elem_type = *elem_type;
+	s->key_type = key_type ? *key_type : *elem_type;
+	s->data = nullptr;
+	GError *e2 = nullptr;
+	const char *src = s->impl_def.init(s, options, &e2);
+	if (!src) {
+		clo::propagate_error(err, e2);
+		clo_sort_destroy(s);
+		return nullptr;
+	}
+	// satradix ignores the compare macro (it always orders by the key's
+	// unsigned bits); the other implementations run the default compare.
+	bool is_radix = def == &clo_sort_satradix_def;
+	if ((!is_radix && !compare_is_default(compare)) ||
+		!get_key_is_default(get_key)) {
+		set_error(err, CLO_ERROR_ARGS,
+			"Custom compare/get_key snippets are not supported by the "
+			"compiled-in sm_103a kernels (compare='%s', get_key='%s')",
+			compare ? compare : "", get_key ? get_key : "");
+		clo_sort_destroy(s);
+		return nullptr;
+	}
+	s->prg = new ccl_program();
+	char macros[512];
+	snprintf(macros, sizeof macros,
+		"#define CLO_SORT_ELEM_TYPE %s\n#define CLO_SORT_KEY_TYPE %s\n"
+		"#define CLO_SORT_COMPARE(a, b) %s\n#define CLO_SORT_KEY_GET(x) %s\n",
+		clo_type_get_name(s->elem_type), clo_type_get_name(s->key_type),
+		compare ? compare : "((a) > (b))", get_key ? get_key : "(x)");
+	s->prg->src = std::string(macros) + src;
+	s->prg->opts = compiler_opts ? compiler_opts : "";
+	clo::wrapper_created();
+	return s;
+}
+
+void clo_sort_destroy(CloSort *sorter) {
+	if (!sorter) return;
+	if (sorter->impl_def.finalize) sorter->impl_def.finalize(sorter);
+	if (sorter->ctx) ccl_context_unref(sorter->ctx);
+	if (sorter->prg) {
+		delete sorter->prg;
+		clo::wrapper_destroyed();
+	}
+	delete sorter;
+}
+
+CCLEvent *clo_sort_with_device_data(CloSort *sorter, CCLQueue *cq_exec,
+	CCLQueue *cq_comm, CCLBuffer *data_in, CCLBuffer *data_out,
+	size_t numel, size_t lws_max, GError **err) {
+	if (!sorter || !cq_exec || (err && *err)) {
+		fprintf(stderr, "cl_ops: clo_sort_with_device_data: bad arguments\n");
+		return nullptr;
+	}
+	cudaSetDevice(sorter->ctx->ordinal);
+	return sorter->impl_def.sort_with_device_data(sorter, cq_exec, cq_comm,
+		data_in, data_out, numel, lws_max, err);
+}
+
+cl_bool clo_sort_with_host_data(CloSort *sorter, CCLQueue *cq_exec,
+	CCLQueue *cq_comm, void *data_in, void *data_out, size_t numel,
+	size_t lws_max, GError **err) {
+	if (!sorter || (err && *err)) {
+		fprintf(stderr, "cl_ops: clo_sort_with_host_data: bad arguments\n");
+		return CL_FALSE;
+	}
+	CCLContext *ctx = sorter->ctx;
+	cudaSetDevice(ctx->ordinal);
+	GError *e2 = nullptr;
+	CCLQueue *own = nullptr;
+	if (cq_exec == nullptr) {
+		own = ccl_queue_new(ctx, &ctx->device, 0, &e2);
+		if (!own) {
+			clo::propagate_error(err, e2);
+			return CL_FALSE;
+		}
+		cq_exec = own;
+	}
+	if (cq_comm == nullptr) cq_comm = cq_exec;
+	size_t bytes = numel * clo_type_sizeof(sorter->elem_type);
+	cl_bool status = CL_FALSE;
+	CCLBuffer *din = nullptr, *dout = nullptr;
+	CCLEvent *evt = nullptr;
+	CCLEventWaitList ewl = nullptr;
+	void *pin = clo::tmp_alloc(ctx, bytes, cq_comm->stream, &e2);
+	void *pout = nullptr;
+	if (!pin) goto done;
+	din = ccl_buffer_new_wrap(ctx, pin, bytes, &e2);
+	if (!sorter->impl_def.in_place) {
+		pout = clo::tmp_alloc(ctx, bytes, cq_comm->stream, &e2);
+		if (!pout) goto done;
+		dout = ccl_buffer_new_wrap(ctx, pout, bytes, &e2);
+	}
+	evt = ccl_buffer_enqueue_write(din, cq_comm, CL_FALSE, 0, bytes, data_in,
+		nullptr, &e2);
+	if (!evt) goto done;
+	if (cq_comm != cq_exec)
+		ccl_ewl(&ewl, evt, (CCLEvent *)nullptr);
+	if (!clo::wait_ewl(cq_exec, &ewl, &e2)) goto done;
+	evt = sorter->impl_def.sort_with_device_data(sorter, cq_exec, cq_comm, din,
+		dout, numel, lws_max, &e2);
+	if (!evt) goto done;
+	if (cq_comm != cq_exec) ccl_ewl(&ewl, evt, (CCLEvent *)nullptr);
+	evt = ccl_buffer_enqueue_read(dout ? dout : din, cq_comm, CL_FALSE, 0,
+		bytes, data_out, &ewl, &e2);
+	if (!evt) goto done;
+	ccl_ewl(&ewl, evt, (CCLEvent *)nullptr);
+	if (!ccl_event_wait(&ewl, &e2)) goto done;
+	status = CL_TRUE;
+done:
+	ccl_event_wait_list_clear(&ewl);
+	if (din) ccl_buffer_destroy(din);
+	if (dout) ccl_buffer_destroy(dout);
+	clo::tmp_free(pin, cq_comm->stream);
+	clo::tmp_free(pout, cq_comm->stream);
+	if (!status) cudaStreamSynchronize(cq_comm->stream);
+	if (own) ccl_queue_destroy(own);
+	clo::propagate_error(err, e2);
+	return status;
+}
+
+CCLContext *clo_sort_get_context(CloSort *s) { return s ? s->ctx : nullptr; }
+CCLProgram *clo_sort_get_program(CloSort *s) { return s ? s->prg : nullptr; }
+CloType clo_sort_get_element_type(CloSort *s) {
+	return s ? s->elem_type : (CloType)-1;
+}
+size_t clo_sort_get_element_size(CloSort *s) {
+	return s ? clo_type_sizeof(s->elem_type) : 0;
+}
+CloType clo_sort_get_key_type(CloSort *s) {
+	return s ? s->key_type : (CloType)-1;
+}
+size_t clo_sort_get_key_size(CloSort *s) {
+	return s ? clo_type_sizeof(s->key_type) : 0;
+}
+void *clo_sort_get_data(CloSort *s) { return s ? s->data : nullptr; }
+void clo_sort_set_data(CloSort *s, void *data) {
+	if (s) s->data = data;
+}
+cl_uint clo_sort_get_num_kernels(CloSort *s, GError **err) {
+	return s ? s->impl_def.get_num_kernels(s, err) : 0;
+}
+const char *clo_sort_get_kernel_name(CloSort *s, cl_uint i, GError **err) {
+	return s ? s->impl_def.get_kernel_name(s, i, err) : nullptr;
+}
+size_t clo_sort_get_localmem_usage(CloSort *s, cl_uint i, size_t lws_max,
+	size_t numel, GError **err) {
+	return s ? s->impl_def.get_localmem_usage(s, i, lws_max, numel, err) : 0;
+}
+
+// ------------------------------------------------------- key-value sort
+CCLEvent *clo_sort_kv_with_device_data(CloSort *sorter, CCLQueue *q,
+	CCLBuffer *keys, CCLBuffer *values, CloType value_type, size_t numel,
+	GError **err) {
+	if (!sorter || !q || (err && *err)) {
+		fprintf(stderr, "cl_ops: clo_sort_kv_with_device_data: bad arguments\n");
+		return nullptr;
+	}
+	cudaSetDevice(sorter->ctx->ordinal);
+	size_t vb = clo_type_sizeof(value_type);
+	const char *name = sorter->impl_def.name;
+	bool radix = strcmp(name, "satradix") == 0;
+	bool gsel = strcmp(name, "gselect") == 0;
+	if (!radix && !gsel) {
+		set_error(err, CLO_ERROR_ARGS,
+			"Key-value sorting needs a stable sorter (satradix or gselect), "
+			"not '%s'", name);
+		return nullptr;
+	}
+	if (vb != 4 && vb != 8) {
+		set_error(err, CLO_ERROR_ARGS, "Value type must be 4 or 8 bytes wide");
+		return nullptr;
+	}
+	if (!check_numel(sorter, keys, numel, err)) return nullptr;
+	if (!values || values->size < numel * vb) {
+		set_error(err, CLO_ERROR_ARGS, "Value buffer too small");
+		return nullptr;
+	}
+	ccl_event *ev = clo::event_begin(q, radix ? "satradix_kv" : "gselect_kv");
+	size_t kb = clo_type_sizeof(sorter->elem_type);
+	if (radix) {
+		bool skip = !clo::stream_capturing(q->stream);
+		if (clo::radix_sort(keys->ptr, values->ptr, numel, (int)kb, (int)vb,
+				satradix_sort_bits(sorter), sorter->ctx, q->stream, skip,
+				err) != cudaSuccess)
+			return nullptr;
+	} else {
+		void *tk = clo::tmp_alloc(sorter->ctx, numel * kb, q->stream, err);
+		if (!tk) return nullptr;
+		void *tv = clo::tmp_alloc(sorter->ctx, numel * vb, q->stream, err);
+		if (!tv) {
+			clo::tmp_free(tk, q->stream);
+			return nullptr;
+		}
+		bool ok = clo::gselect_sort(keys->ptr, tk, numel, sorter->elem_type,
+			values->ptr, tv, (int)vb, sorter->ctx, q->stream, err) == cudaSuccess;
+		ok = ok && cuda_ok(cudaMemcpyAsync(keys->ptr, tk, numel * kb,
+			cudaMemcpyDeviceToDevice, q->stream), err, "kv copy back");
+		ok = ok && cuda_ok(cudaMemcpyAsync(values->ptr, tv, numel * vb,
+			cudaMemcpyDeviceToDevice, q->stream), err, "kv copy back");
+		clo::tmp_free(tk, q->stream);
+		clo::tmp_free(tv, q->stream);
+		if (!ok) return nullptr;
+	}
+	clo::event_end(ev);
+	return ev;
+}
+
+cl_bool clo_sort_kv_with_host_data(CloSort *sorter, CCLQueue *q, void *keys,
+	void *values, CloType value_type, size_t numel, GError **err) {
+	if (!sorter || (err && *err)) return CL_FALSE;
+	CCLContext *ctx = sorter->ctx;
+	cudaSetDevice(ctx->ordinal);
+	GError *e2 = nullptr;
+	CCLQueue *own = nullptr;
+	if (!q) {
+		own = ccl_queue_new(ctx, &ctx->device, 0, &e2);
+		if (!own) {
+			clo::propagate_error(err, e2);
+			return CL_FALSE;
+		}
+		q = own;
+	}
+	size_t kbytes = numel * clo_type_sizeof(sorter->elem_type);
+	size_t vbytes = numel * clo_type_sizeof(value_type);
+	cl_bool status = CL_FALSE;
+	CCLBuffer *dk = nullptr, *dv = nullptr;
+	CCLEventWaitList ewl = nullptr;
+	CCLEvent *evt = nullptr;
+	void *pk = clo::tmp_alloc(ctx, kbytes, q->stream, &e2);
+	void *pv = pk ? clo::tmp_alloc(ctx, vbytes, q->stream, &e2) : nullptr;
+	if (!pk || !pv) goto done;
+	dk = ccl_buffer_new_wrap(ctx, pk, kbytes, &e2);
+	dv = ccl_buffer_new_wrap(ctx, pv, vbytes, &e2);
+	if (!ccl_buffer_enqueue_write(dk, q, CL_FALSE, 0, kbytes, keys, nullptr, &e2))
+		goto done;
+	if (!ccl_buffer_enqueue_write(dv, q, CL_FALSE, 0, vbytes, values, nullptr, &e2))
+		goto done;
+	if (!clo_sort_kv_with_device_data(sorter, q, dk, dv, value_type, numel, &e2))
+		goto done;
+	if (!ccl_buffer_enqueue_read(dk, q, CL_FALSE, 0, kbytes, keys, nullptr, &e2))
+		goto done;
+	evt = ccl_buffer_enqueue_read(dv, q, CL_FALSE, 0, vbytes, values, nullptr, &e2);
+	if (!evt) goto done;
+	ccl_ewl(&ewl, evt, (CCLEvent *)nullptr);
+	if (!ccl_event_wait(&ewl, &e2)) goto done;
+	status = CL_TRUE;
+done:
+	ccl_event_wait_list_clear(&ewl);
+	if (dk) ccl_buffer_destroy(dk);
+	if (dv) ccl_buffer_destroy(dv);
+	clo::tmp_free(pk, q->stream);
+	clo::tmp_free(pv, q->stream);
+	if (!status) cudaStreamSynchronize(q->stream);
+	if (own) ccl_queue_destroy(own);
+	clo::propagate_error(err, e2);
+	return status;
+}
+
+}  // extern "C"

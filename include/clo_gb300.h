@@ -1,0 +1,78 @@
+/*
+ * cl_ops on GB300 -- entry points that extend the reference API.
+ *
+ * None of these has a counterpart in the reference. Each exists because
+ * the reference cannot express the operation:
+ *  - key-value sorting: the reference sorts one CloType per element and
+ *    has no 12-byte type for a (uint64 key, uint32 value) pair;
+ *  - clo_rng_fill: the reference draws random numbers from client kernels
+ *    only (its benchmark kernel src/benchmarks/clo_rng_bench.cl:23-37 is
+ *    what this entry point packages, with the whole draw loop on device);
+ *  - pinned host buffers for full-speed host<->device copies.
+ */
+#ifndef CLO_GB300_H
+#define CLO_GB300_H
+
+#include "clo_common.h"
+#include "ccl_shim.h"
+#include "clo_sort_abstract.h"
+#include "clo_scan_abstract.h"
+#include "clo_rng.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Stable sort of `keys` (the sorter's element type, ascending by the
+ * key's unsigned bit pattern, as "satradix" sorts) carrying `values`
+ * (value_type, any 4- or 8-byte type) along. In place on both buffers.
+ * Only "satradix" and "gselect" (both stable) accept it; other sorters set
+ * CLO_ERROR_ARGS. Asynchronous; returns the last event. */
+CCLEvent *clo_sort_kv_with_device_data(CloSort *sorter, CCLQueue *cq_exec,
+	CCLBuffer *keys, CCLBuffer *values, CloType value_type, size_t numel,
+	GError **err);
+
+/* Blocking host-memory form of clo_sort_kv_with_device_data. */
+cl_bool clo_sort_kv_with_host_data(CloSort *sorter, CCLQueue *cq_exec,
+	void *keys, void *values, CloType value_type, size_t numel,
+	GError **err);
+
+/* Draws `draws` numbers from every state of `rng` into `out`, draw-major:
+ * out[r * n_states + i] = next(state i) >> (32 - bits) when maxint == 0,
+ * else next(state i) % maxint (the two modes of clo_rng_bench.cl). The
+ * states advance, so consecutive calls continue the streams. `out` must
+ * hold draws * n_states uint32 values. bits in [1, 32]. */
+CCLEvent *clo_rng_fill(CloRng *rng, CCLQueue *cq, CCLBuffer *out,
+	size_t draws, cl_uint bits, cl_uint maxint, GError **err);
+
+/* Page-locked host memory for full-bandwidth copies (cudaMallocHost). */
+void *clo_host_alloc(size_t size, GError **err);
+void clo_host_free(void *ptr);
+
+/* Number of kernel launches this library issued so far in this process
+ * (all devices). */
+cl_ulong clo_gb300_launch_count(void);
+
+/* Per-kernel device time: when enabled, every kernel launch of this
+ * library is bracketed by CUDA events on its stream, and
+ * clo_gb300_timing_get returns (after waiting for them) the summed time,
+ * the summed algorithmic HBM bytes and the launch count of the named
+ * kernel ("satradix_onesweep", "satradix_upsweep", "scan_lookback",
+ * "abitonic_tile_sort", "abitonic_global_steps", "abitonic_tile_finish",
+ * "rng_fill"); it returns 0 when the kernel has not run. */
+void clo_gb300_timing_enable(int on);
+void clo_gb300_timing_reset(void);
+int clo_gb300_timing_get(const char *kernel, double *total_ms,
+	double *total_bytes, cl_ulong *launches);
+
+/* Test hook for the bounded lookback waits: tile `tile` of subsequent
+ * scans withholds its status, so the next tile's wait runs out, the
+ * kernel ends and the next synchronising call reports CLO_ERROR_LIBRARY.
+ * -1 restores normal operation. */
+void clo_gb300_debug_scan_withhold(long long tile);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CLO_GB300_H */

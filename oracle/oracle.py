@@ -1,0 +1,108 @@
+"""TEST INFRASTRUCTURE -- ctypes binding of the C oracle (clo_oracle.c).
+
+Used only by tests/, __graft_entry__.smoke() and bench.py's CPU baseline
+leg, as the checker. numpy arrays in, numpy arrays out.
+"""
+import ctypes as C
+import pathlib
+import sys
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+import build_oracle  # noqa: E402
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_oracle.build()
+        _lib = C.CDLL(str(path))
+        P, SZ = C.c_void_p, C.c_size_t
+        _lib.oracle_radix_sort.argtypes = [P, P, SZ, C.c_int, C.c_int, C.c_int]
+        _lib.oracle_bitonic_sort.argtypes = [P, SZ, C.c_int]
+        _lib.oracle_gselect_sort.argtypes = [P, P, SZ, C.c_int, P, P, C.c_int]
+        _lib.oracle_scan.argtypes = [P, P, SZ, C.c_int, C.c_int]
+        _lib.oracle_rng_init_gid.argtypes = [P, SZ, C.c_int, C.c_uint64, C.c_int]
+        _lib.oracle_rng_fill.argtypes = [P, SZ, C.c_int, P, SZ, C.c_uint, C.c_uint]
+        _lib.oracle_mt19937.argtypes = [C.c_uint32, P, SZ]
+        _lib.oracle_splitmix64.argtypes = [C.c_uint64, P, SZ]
+        _lib.oracle_radix_sort_u32_threaded.argtypes = [P, SZ, C.c_int, C.c_int]
+    return _lib
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def radix_sort(keys, vals=None, sort_bits=None):
+    k = np.ascontiguousarray(keys).copy()
+    v = None if vals is None else np.ascontiguousarray(vals).copy()
+    kb = k.dtype.itemsize
+    vb = 0 if v is None else v.dtype.itemsize
+    lib().oracle_radix_sort(_p(k), _p(v), k.size, kb, vb,
+                            8 * kb if sort_bits is None else sort_bits)
+    return k if v is None else (k, v)
+
+
+def radix_sort_u32_threaded(keys, threads, bits=4):
+    """In place on `keys` (a uint32 array); returns it."""
+    k = np.ascontiguousarray(keys, dtype=np.uint32)
+    lib().oracle_radix_sort_u32_threaded(_p(k), k.size, threads, bits)
+    return k
+
+
+def bitonic_sort(a, clo_type):
+    d = np.ascontiguousarray(a).copy()
+    lib().oracle_bitonic_sort(_p(d), d.size, clo_type)
+    return d
+
+
+def gselect_sort(a, clo_type, vals=None):
+    a = np.ascontiguousarray(a)
+    out = np.empty_like(a)
+    vout = None if vals is None else np.empty_like(vals)
+    lib().oracle_gselect_sort(_p(a), _p(out), a.size, clo_type,
+                              _p(vals), _p(vout), 0 if vals is None else vals.dtype.itemsize)
+    return out if vals is None else (out, vout)
+
+
+def scan(a, in_type, out_dtype):
+    a = np.ascontiguousarray(a)
+    out = np.empty(a.size, dtype=out_dtype)
+    lib().oracle_scan(_p(a), _p(out), a.size, in_type, out.dtype.itemsize)
+    return out
+
+
+GEN = {"lcg": 0, "xorshift64": 1, "xorshift128": 2, "mwc64x": 3, "parkmiller": 4,
+       "tauslcg": 5}
+SEED_SIZE = {"lcg": 8, "xorshift64": 8, "xorshift128": 16, "mwc64x": 8,
+             "parkmiller": 4, "tauslcg": 16}
+
+
+def rng_init_gid(name, count, main_seed, hash_kind=0):
+    st = np.zeros(count * SEED_SIZE[name], dtype=np.uint8)
+    lib().oracle_rng_init_gid(_p(st), count, GEN[name], main_seed, hash_kind)
+    return st
+
+
+def rng_fill(name, states, count, draws, bits=32, maxint=0):
+    st = np.ascontiguousarray(states).copy()
+    out = np.empty(draws * count, dtype=np.uint32)
+    lib().oracle_rng_fill(_p(st), count, GEN[name], _p(out), draws, bits, maxint)
+    return out, st
+
+
+def mt19937(seed, nwords):
+    out = np.empty(nwords, dtype=np.uint32)
+    lib().oracle_mt19937(seed & 0xFFFFFFFF, _p(out), nwords)
+    return out
+
+
+def splitmix64(seed, n):
+    out = np.empty(n, dtype=np.uint64)
+    lib().oracle_splitmix64(seed, _p(out), n)
+    return out

@@ -1,0 +1,177 @@
+"""GPU parity of the four sorters against the CPU oracle, through the
+C-ABI (clo_sort_new / clo_sort_with_device_data / clo_sort_with_host_data),
+bit-exact. Sizes cover empty, tiny, ragged (non-multiples of the tile and
+of powers of two), one-tile boundaries and multi-tile arrays."""
+import numpy as np
+import pytest
+
+import oracle
+from inputs import keys_of_type, keys_u32, keys_u64, adversarial_u32, low20_u64
+
+pytestmark = pytest.mark.gpu
+
+INT = [(0, np.int8), (1, np.uint8), (2, np.int16), (3, np.uint16), (4, np.int32),
+       (5, np.uint32), (6, np.int64), (7, np.uint64)]
+ALL = INT + [(8, np.float16), (9, np.float32), (10, np.float64)]
+
+
+def _sort_dev(clops, ctx, q, algo, code, a, options=None, key_type=None):
+    s = clops.Sorter(ctx, algo, code, key_type=key_type, options=options)
+    b = clops.Buffer.from_array(ctx, q, a)
+    clops.wait(s.sort_device(q, b, a.size))
+    out = b.read(q, a.dtype, a.size)
+    b.destroy()
+    s.destroy()
+    return out
+
+
+# ------------------------------------------------------------- satradix
+@pytest.mark.parametrize("code,dt", INT)
+@pytest.mark.parametrize("n", [0, 1, 2, 3, 31, 33, 1000, 4095, 4096, 4097, 8191, 8192,
+                               8193, 65537, 300001])
+def test_satradix_matches_oracle(clops, ctx, queue, code, dt, n):
+    a = keys_of_type(100 + n + code, n, dt)
+    got = _sort_dev(clops, ctx, queue, "satradix", code, a)
+    np.testing.assert_array_equal(got, oracle.radix_sort(a))
+
+
+@pytest.mark.parametrize("code,dt", [(5, np.uint32), (7, np.uint64), (4, np.int32)])
+def test_satradix_low_entropy_and_radix_options(clops, ctx, queue, code, dt):
+    n = 200003
+    a = keys_of_type(5, n, dt)
+    a = (a.view(f"u{a.dtype.itemsize}") & np.array(0x00F000F0, dtype=f"u{a.dtype.itemsize}")
+         if a.dtype.itemsize >= 4 else a).view(dt)
+    ref = oracle.radix_sort(a)
+    for opt in (None, "radix=16", "radix=256", "radix=2,scan=blelloch"):
+        np.testing.assert_array_equal(_sort_dev(clops, ctx, queue, "satradix", code, a, opt), ref)
+
+
+def test_satradix_key_type_narrower_than_element(clops, ctx, queue):
+    # ulong elements with a uint key: the reference's passes shift the key
+    # with OpenCL-masked shifts, so only the low 32 bits order the output.
+    n = 70001
+    a = keys_u64(9, n)
+    got = _sort_dev(clops, ctx, queue, "satradix", 7, a, key_type=5)
+    np.testing.assert_array_equal(got, oracle.radix_sort(a, sort_bits=32))
+
+
+@pytest.mark.parametrize("kind", ["sorted", "reverse", "equal", "distinct16", "zipf"])
+def test_satradix_adversarial(clops, ctx, queue, kind):
+    a = adversarial_u32(kind, 1 << 20)
+    got = _sort_dev(clops, ctx, queue, "satradix", 5, a)
+    np.testing.assert_array_equal(got, np.sort(a))
+
+
+def test_satradix_u64_low20(clops, ctx, queue):
+    a = low20_u64(1 << 20)
+    np.testing.assert_array_equal(_sort_dev(clops, ctx, queue, "satradix", 7, a), np.sort(a))
+
+
+@pytest.mark.parametrize("kcode,kdt,vcode,vdt", [
+    (5, np.uint32, 5, np.uint32), (7, np.uint64, 5, np.uint32),
+    (5, np.uint32, 7, np.uint64), (7, np.uint64, 7, np.uint64), (4, np.int32, 9, np.float32)])
+@pytest.mark.parametrize("n", [1, 1000, 8193, 250007])
+def test_satradix_kv_stable(clops, ctx, queue, kcode, kdt, vcode, vdt, n):
+    k = keys_of_type(31 + n, n, kdt)
+    k = (k.view(f"u{k.dtype.itemsize}") & np.array(0x0303, dtype=f"u{k.dtype.itemsize}")).view(kdt)
+    v = np.arange(n, dtype=np.uint64).astype(vdt)
+    s = clops.Sorter(ctx, "satradix", kcode)
+    kb = clops.Buffer.from_array(ctx, queue, k)
+    vb = clops.Buffer.from_array(ctx, queue, v)
+    clops.wait(s.sort_kv_device(queue, kb, vb, vcode, n))
+    gk, gv = kb.read(queue, kdt, n), vb.read(queue, vdt, n)
+    rk, rv = oracle.radix_sort(k, v)
+    np.testing.assert_array_equal(gk, rk)
+    np.testing.assert_array_equal(gv.view(f"u{v.dtype.itemsize}"), rv.view(f"u{v.dtype.itemsize}"))
+    for b in (kb, vb):
+        b.destroy()
+    s.destroy()
+
+
+def test_satradix_host_data_and_out_buffer(clops, ctx, queue):
+    a = keys_u32(77, 123457)
+    s = clops.Sorter(ctx, "satradix", 5)
+    out = np.empty_like(a)
+    s.sort_host(queue, a.copy(), out)
+    np.testing.assert_array_equal(out, np.sort(a))
+    # data_out != NULL sorts into data_out and leaves data_in untouched.
+    bi = clops.Buffer.from_array(ctx, queue, a)
+    bo = clops.Buffer(ctx, a.nbytes)
+    clops.wait(s.sort_device(queue, bi, a.size, buf_out=bo))
+    np.testing.assert_array_equal(bo.read(queue, np.uint32, a.size), np.sort(a))
+    np.testing.assert_array_equal(bi.read(queue, np.uint32, a.size), a)
+    bi.destroy()
+    bo.destroy()
+    s.destroy()
+
+
+# ------------------------------------------------------------- bitonic
+@pytest.mark.parametrize("algo", ["sbitonic", "abitonic"])
+@pytest.mark.parametrize("code,dt", ALL)
+@pytest.mark.parametrize("n", [1, 2, 3, 16, 100, 1024, 16384, 32768, 131075])
+def test_bitonic_matches_network_replay(clops, ctx, queue, algo, code, dt, n):
+    if algo == "sbitonic" and n > 40000:
+        pytest.skip("one launch per step; covered at smaller sizes")
+    a = keys_of_type(200 + n + code, n, dt)
+    got = _sort_dev(clops, ctx, queue, algo, code, a)
+    ref = oracle.bitonic_sort(a, code)
+    np.testing.assert_array_equal(got.view(f"u{a.dtype.itemsize}"), ref.view(f"u{a.dtype.itemsize}"))
+
+
+@pytest.mark.parametrize("code,dt", [(8, np.float16), (9, np.float32), (10, np.float64)])
+def test_bitonic_non_total_order_is_bit_exact(clops, ctx, queue, code, dt):
+    pat = np.array([0.0, -0.0, np.nan, 1.0, -1.0, np.nan, -0.0, 0.0, np.inf, -np.inf], dtype=dt)
+    a = np.tile(pat, 6554)[:65536].copy()
+    rnd = keys_of_type(3, 65536, dt)
+    a[::3] = rnd[::3]
+    ref = oracle.bitonic_sort(a, code)
+    for algo in ("abitonic",):
+        got = _sort_dev(clops, ctx, queue, algo, code, a)
+        np.testing.assert_array_equal(got.view(f"u{a.dtype.itemsize}"), ref.view(f"u{a.dtype.itemsize}"))
+
+
+@pytest.mark.parametrize("opts", ["maxps=1", "maxps=2", "maxps=3,minps=2", "maxsfs=6", "maxsfs=11,maxps=4"])
+def test_abitonic_options_do_not_change_result(clops, ctx, queue, opts):
+    a = keys_u32(8, 1 << 17)
+    got = _sort_dev(clops, ctx, queue, "abitonic", 5, a, options=opts)
+    np.testing.assert_array_equal(got, oracle.bitonic_sort(a, 5))
+
+
+# ------------------------------------------------------------- gselect
+@pytest.mark.parametrize("code,dt", ALL)
+@pytest.mark.parametrize("n", [1, 2, 7, 1000, 5003])
+def test_gselect_matches_oracle(clops, ctx, queue, code, dt, n):
+    a = keys_of_type(300 + n, n, dt)
+    if np.issubdtype(dt, np.integer):
+        a = (a % 13).astype(dt)
+    got = _sort_dev(clops, ctx, queue, "gselect", code, a)
+    np.testing.assert_array_equal(got, oracle.gselect_sort(a, code))
+
+
+def test_gselect_kv_stable(clops, ctx, queue):
+    n = 4097
+    k = (keys_u32(4, n) % 17).astype(np.uint32)
+    v = np.arange(n, dtype=np.uint32)
+    s = clops.Sorter(ctx, "gselect", 5)
+    kb = clops.Buffer.from_array(ctx, queue, k)
+    vb = clops.Buffer.from_array(ctx, queue, v)
+    clops.wait(s.sort_kv_device(queue, kb, vb, 5, n))
+    rk, rv = oracle.gselect_sort(k, 5, v)
+    np.testing.assert_array_equal(kb.read(queue, np.uint32, n), rk)
+    np.testing.assert_array_equal(vb.read(queue, np.uint32, n), rv)
+    kb.destroy()
+    vb.destroy()
+    s.destroy()
+
+
+def test_gselect_out_of_place(clops, ctx, queue):
+    a = keys_u32(12, 3001)
+    s = clops.Sorter(ctx, "gselect", 5)
+    bi = clops.Buffer.from_array(ctx, queue, a)
+    bo = clops.Buffer(ctx, a.nbytes)
+    clops.wait(s.sort_device(queue, bi, a.size, buf_out=bo))
+    np.testing.assert_array_equal(bo.read(queue, np.uint32, a.size), np.sort(a))
+    np.testing.assert_array_equal(bi.read(queue, np.uint32, a.size), a)
+    bi.destroy()
+    bo.destroy()
+    s.destroy()
