@@ -296,8 +296,9 @@ def run_ours(args):
     dist.close()
 
 
-def run_suite(clops, ctx, q, args):
-    """The other large-size primitives, 2 warm-up + 3 timed calls each."""
+def run_suite(clops, ctx, q, args, only=None):
+    """The other large-size primitives, 2 warm-up + 3 timed calls each
+    (`only` selects one of them)."""
     from inputs import splitmix64, keys_u64
     res = {}
     peak, _ = measured_peaks()
@@ -308,78 +309,82 @@ def run_suite(clops, ctx, q, args):
         q.finish()
         return timed_region(clops, q, lambda i: fn(), reps) / reps
 
-    # abitonic 2^26 uint32
-    n = 1 << 26
-    a = keys_u32_chunked(44, n)
-    b = clops.Buffer.from_array(ctx, q, a)
-    s = clops.Sorter(ctx, "abitonic", clops.CLO_UINT)
-    pristine = clops.Buffer.from_array(ctx, q, a)
+    def copy(src, dst, nbytes):
+        clops.call(clops.lib.ccl_buffer_enqueue_copy, src.h, dst.h, q.h, 0, 0, nbytes, None)
 
-    def bit():
-        clops.call(clops.lib.ccl_buffer_enqueue_copy, pristine.h, b.h, q.h, 0, 0, a.nbytes, None)
-    bit()
-    q.finish()
-    ms_copy = timed(bit)
-    ms = timed(lambda: (bit(), s.sort_device(q, b, n))) - ms_copy
-    res["abitonic_2pow26_u32"] = {"Gkeys/s": round(n / (ms * 1e-3) / 1e9, 3), "ms": round(ms, 3),
-                                  "canonical_bytes_GB": 17.7,
-                                  "frac_of_peak_canonical": round(17.7e9 / (ms * 1e-3) / 1e9 / peak, 4)}
-    s.destroy()
-    b.destroy()
-    pristine.destroy()
+    def abitonic():
+        n = 1 << 26
+        a = keys_u32_chunked(44, n)
+        b = clops.Buffer.from_array(ctx, q, a)
+        pristine = clops.Buffer.from_array(ctx, q, a)
+        s = clops.Sorter(ctx, "abitonic", clops.CLO_UINT)
+        ms_copy = timed(lambda: copy(pristine, b, a.nbytes))
+        ms = timed(lambda: (copy(pristine, b, a.nbytes), s.sort_device(q, b, n))) - ms_copy
+        res["abitonic_2pow26_u32"] = {
+            "Gkeys/s": round(n / (ms * 1e-3) / 1e9, 3), "ms": round(ms, 3),
+            "canonical_bytes_GB": 17.7,
+            "frac_of_peak_canonical": round(17.7e9 / (ms * 1e-3) / 1e9 / peak, 4)}
+        for x in (s, b, pristine):
+            x.destroy()
 
-    # satradix KV 2^27 (uint64 key, uint32 value = index)
-    n = 1 << 27
-    k = keys_u64(43, n)
-    v = np.arange(n, dtype=np.uint32)
-    kp, vp = clops.Buffer.from_array(ctx, q, k), clops.Buffer.from_array(ctx, q, v)
-    kb, vb = clops.Buffer(ctx, k.nbytes), clops.Buffer(ctx, v.nbytes)
-    s = clops.Sorter(ctx, "satradix", clops.CLO_ULONG)
+    def kv():
+        n = 1 << 27
+        k = keys_u64(43, n)
+        v = np.arange(n, dtype=np.uint32)
+        kp, vp = clops.Buffer.from_array(ctx, q, k), clops.Buffer.from_array(ctx, q, v)
+        kb, vb = clops.Buffer(ctx, k.nbytes), clops.Buffer(ctx, v.nbytes)
+        s = clops.Sorter(ctx, "satradix", clops.CLO_ULONG)
 
-    def restore():
-        clops.call(clops.lib.ccl_buffer_enqueue_copy, kp.h, kb.h, q.h, 0, 0, k.nbytes, None)
-        clops.call(clops.lib.ccl_buffer_enqueue_copy, vp.h, vb.h, q.h, 0, 0, v.nbytes, None)
-    ms_copy = timed(restore)
-    ms = timed(lambda: (restore(), s.sort_kv_device(q, kb, vb, clops.CLO_UINT, n))) - ms_copy
-    res["satradix_kv_2pow27_u64_u32"] = {"Gpairs/s": round(n / (ms * 1e-3) / 1e9, 3), "ms": round(ms, 3),
-                                         "model_bytes_per_pair": 200,
-                                         "frac_of_peak": round(200.0 * n / (ms * 1e-3) / 1e9 / peak, 4)}
-    for x in (kp, vp, kb, vb, s):
-        x.destroy()
-    del k, v
+        def restore():
+            copy(kp, kb, k.nbytes)
+            copy(vp, vb, v.nbytes)
+        ms_copy = timed(restore)
+        ms = timed(lambda: (restore(), s.sort_kv_device(q, kb, vb, clops.CLO_UINT, n))) - ms_copy
+        res["satradix_kv_2pow27_u64_u32"] = {
+            "Gpairs/s": round(n / (ms * 1e-3) / 1e9, 3), "ms": round(ms, 3),
+            "model_bytes_per_pair": 200,
+            "frac_of_peak": round(200.0 * n / (ms * 1e-3) / 1e9 / peak, 4)}
+        for x in (kp, vp, kb, vb, s):
+            x.destroy()
 
-    # blelloch scan 2^30 uint32 in [0, 255] -> uint64
-    n = 1 << 30
-    a = np.empty(n, dtype=np.uint32)
-    for o in range(0, n, 1 << 24):
-        a[o:o + (1 << 24)] = (splitmix64(45, 1 << 24, offset=o) >> np.uint64(56)).astype(np.uint32)
-    bi = clops.Buffer.from_array(ctx, q, a)
-    bo = clops.Buffer(ctx, n * 8)
-    sc = clops.Scanner(ctx, clops.CLO_UINT, clops.CLO_ULONG)
-    ms = timed(lambda: sc.scan_device(q, bi, bo, n))
-    res["blelloch_2pow30_u32_u64"] = {"GB/s": round(12.0 * n / (ms * 1e-3) / 1e9, 1), "ms": round(ms, 3),
-                                      "frac_of_peak": round(12.0 * n / (ms * 1e-3) / 1e9 / peak, 4)}
-    for x in (bi, bo, sc):
-        x.destroy()
-    del a
+    def scan():
+        n = 1 << (30 if only is None else min(args.log2n, 30))
+        a = np.empty(n, dtype=np.uint32)
+        for o in range(0, n, 1 << 24):
+            m = min(1 << 24, n - o)
+            a[o:o + m] = (splitmix64(45, m, offset=o) >> np.uint64(56)).astype(np.uint32)
+        bi = clops.Buffer.from_array(ctx, q, a)
+        bo = clops.Buffer(ctx, n * 8)
+        sc = clops.Scanner(ctx, clops.CLO_UINT, clops.CLO_ULONG)
+        ms = timed(lambda: sc.scan_device(q, bi, bo, n))
+        res[f"blelloch_2pow{n.bit_length() - 1}_u32_u64"] = {
+            "GB/s": round(12.0 * n / (ms * 1e-3) / 1e9, 1), "ms": round(ms, 3),
+            "frac_of_peak": round(12.0 * n / (ms * 1e-3) / 1e9 / peak, 4)}
+        for x in (bi, bo, sc):
+            x.destroy()
 
-    # RNGs: 2^24 states from a host seed array, 64 draws
-    count, draws = 1 << 24, 64
-    out = clops.Buffer(ctx, count * draws * 4)
-    for name in ["lcg", "xorshift64", "xorshift128", "mwc64x", "parkmiller"]:
-        size = clops.RNG_SEED_SIZE[name]
-        seeds = splitmix64(46, count * size // 8 + 1).view(np.uint8)[:count * size].copy()
-        if name == "parkmiller":  # nonzero 31-bit states
-            w = seeds.view(np.uint32)
-            w[:] = (w % 2147483646) + 1
-        rng = clops.Rng(ctx, q, name, clops.CLO_RNG_SEED_EXT_HOST, count, seeds=seeds)
-        ms = timed(lambda: rng.fill(q, out, draws))
-        byts = count * draws * 4 + 2 * count * size
-        res[f"rng_{name}"] = {"Gdraws/s": round(count * draws / (ms * 1e-3) / 1e9, 2),
-                              "GB/s": round(byts / (ms * 1e-3) / 1e9, 1), "ms": round(ms, 4),
-                              "frac_of_peak": round(byts / (ms * 1e-3) / 1e9 / peak, 4)}
-        rng.destroy()
-    out.destroy()
+    def rngs():
+        count, draws = 1 << 24, 64
+        out = clops.Buffer(ctx, count * draws * 4)
+        for name in ["lcg", "xorshift64", "xorshift128", "mwc64x", "parkmiller"]:
+            size = clops.RNG_SEED_SIZE[name]
+            seeds = splitmix64(46, count * size // 8 + 1).view(np.uint8)[:count * size].copy()
+            if name == "parkmiller":  # nonzero 31-bit states
+                w = seeds.view(np.uint32)
+                w[:] = (w % 2147483646) + 1
+            rng = clops.Rng(ctx, q, name, clops.CLO_RNG_SEED_EXT_HOST, count, seeds=seeds)
+            ms = timed(lambda: rng.fill(q, out, draws))
+            byts = count * draws * 4 + 2 * count * size
+            res[f"rng_{name}"] = {"Gdraws/s": round(count * draws / (ms * 1e-3) / 1e9, 2),
+                                  "GB/s": round(byts / (ms * 1e-3) / 1e9, 1), "ms": round(ms, 4),
+                                  "frac_of_peak": round(byts / (ms * 1e-3) / 1e9 / peak, 4)}
+            rng.destroy()
+        out.destroy()
+
+    parts = {"abitonic": abitonic, "kv": kv, "scan": scan, "rng": rngs}
+    for name, fn in parts.items():
+        if only is None or only == name:
+            fn()
     q.gc()
     return res
 
@@ -453,11 +458,20 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--log2n", type=int, default=28)
     ap.add_argument("--no-suite", dest="suite", action="store_false")
+    ap.add_argument("--only", choices=["abitonic", "kv", "scan", "rng"],
+                    help="run one suite primitive alone (profiling cases)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.only:
+        import clops
+        ctx = clops.Context(dist_env()[2])
+        q = clops.Queue(ctx, profiling=True)
+        print(json.dumps(run_suite(clops, ctx, q, args, only=args.only)), flush=True)
+        q.destroy()
+        ctx.destroy()
     else:
         run_ours(args)
 

@@ -58,8 +58,10 @@ __device__ __forceinline__ uint32_t digit_of(K k, int shift) {
 }
 
 // ----------------------------------------------------------- upsweep
-// Histograms of all `passes` digit positions in one read. Warps whose
-// lanes share a digit (sorted or constant input) add once per warp.
+// Histograms of all `passes` digit positions in one read: one shared-memory
+// atomic per key and digit position, except when all 32 x PER keys of a
+// warp step share the digit (sorted or constant input), which the warp
+// detects with one AND/OR reduction and adds once.
 template <typename K>
 __global__ void __launch_bounds__(256)
 radix_upsweep(const K *__restrict__ keys, size_t n, int passes,
@@ -71,41 +73,41 @@ radix_upsweep(const K *__restrict__ keys, size_t n, int passes,
 	const size_t warp_global = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
 	const size_t warps_total = ((size_t)gridDim.x * blockDim.x) >> 5;
 	constexpr int PER = 16 / sizeof(K);  // keys per 16-byte load
-	const size_t chunks = (n + PER - 1) / PER;
 	const bool aligned = ((uintptr_t)keys % 16) == 0;
-	for (size_t base = warp_global * 32; base < chunks; base += warps_total * 32) {
-		const size_t c = base + lane;
-		K kv[PER];
-		bool valid[PER];
-		if (aligned && (c + 1) * PER <= n) {
-			uint4 v = dev::ld_stream_v4(reinterpret_cast<const uint4 *>(keys) + c);
-			const K *e = reinterpret_cast<const K *>(&v);
+	// Full 16-byte chunks, processed 32 per warp step with the fast path.
+	const size_t full_chunks = aligned ? n / PER : 0;
+	const size_t full_steps = full_chunks / 32;
+	const uint4 *kv4 = reinterpret_cast<const uint4 *>(keys);
+	for (size_t step = warp_global; step < full_steps; step += warps_total) {
+		uint4 v = dev::ld_stream_v4(kv4 + step * 32 + lane);
+		const K *e = reinterpret_cast<const K *>(&v);
+		for (int p = 0; p < passes; ++p) {
+			uint32_t dd[PER];
+			uint32_t a = 0xffffffffu, o = 0u;
 #pragma unroll
 			for (int q = 0; q < PER; ++q) {
-				kv[q] = e[q];
-				valid[q] = true;
+				dd[q] = digit_of(e[q], p * kRadixBits);
+				a &= dd[q];
+				o |= dd[q];
 			}
-		} else {
+			uint32_t wa = __reduce_and_sync(0xffffffffu, a);
+			uint32_t wo = __reduce_or_sync(0xffffffffu, o);
+			if (wa == wo) {
+				if (lane == 0) atomicAdd(&h[p][wa], 32u * PER);
+			} else {
 #pragma unroll
-			for (int q = 0; q < PER; ++q) {
-				size_t i = c * PER + q;
-				valid[q] = i < n;
-				kv[q] = valid[q] ? keys[i] : (K)0;
+				for (int q = 0; q < PER; ++q) atomicAdd(&h[p][dd[q]], 1u);
 			}
 		}
-#pragma unroll
-		for (int q = 0; q < PER; ++q) {
-			for (int p = 0; p < passes; ++p) {
-				uint32_t d = digit_of(kv[q], p * kRadixBits);
-				uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
-				bool v0 = __shfl_sync(0xffffffffu, valid[q], 0);
-				if (__all_sync(0xffffffffu, valid[q] && d == d0) && v0) {
-					if (lane == 0) atomicAdd(&h[p][d], 32u);
-				} else if (valid[q]) {
-					atomicAdd(&h[p][d], 1u);
-				}
-			}
-		}
+	}
+	// Remaining keys (and unaligned inputs): one key per thread.
+	const size_t done = full_steps * 32 * PER;
+	const size_t tid_global = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+	const size_t threads_total = (size_t)gridDim.x * blockDim.x;
+	for (size_t i = done + tid_global; i < n; i += threads_total) {
+		K key = keys[i];
+		for (int p = 0; p < passes; ++p)
+			atomicAdd(&h[p][digit_of(key, p * kRadixBits)], 1u);
 	}
 	__syncthreads();
 	for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) {
@@ -125,10 +127,21 @@ struct PassArgs {
 	int shift;
 };
 
-template <typename K>
+// Lanes of the warp holding the same 8-bit digit, from one ballot per bit
+// (ALU votes; warp match would run on the much slower ADU pipe).
 __device__ __forceinline__ uint32_t peer_mask(uint32_t d) {
-	return __match_any_sync(0xffffffffu, d);
+	uint32_t m = 0xffffffffu;
+#pragma unroll
+	for (int b = 0; b < kRadixBits; ++b) {
+		const uint32_t bit = (d >> b) & 1u;
+		const uint32_t bal = __ballot_sync(0xffffffffu, bit);
+		m &= bit ? bal : ~bal;
+	}
+	return m;
 }
+
+// Lookback window: predecessor statuses read per round trip per digit.
+constexpr int kLookWindow = 32;
 
 template <typename K, typename V, bool HAS_V>
 __global__ void __launch_bounds__(kThreads, 2)
@@ -136,6 +149,8 @@ radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
 	const V *__restrict__ vin, V *__restrict__ vout, PassArgs a) {
 	constexpr int KPT = KeyCfg<K>::kKpt;
 	constexpr int TILE = KeyCfg<K>::kTile;
+	// Narrower window when the value pass keeps tile positions live.
+	constexpr int kWin = HAS_V ? kLookWindow / 2 : kLookWindow;
 	extern __shared__ __align__(16) unsigned char smem[];
 	uint32_t *s_hist = reinterpret_cast<uint32_t *>(smem);        // [kWarps][256]
 	uint32_t *s_tile_off = s_hist + kWarps * kRadix;               // [256]
@@ -167,7 +182,7 @@ radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
 #pragma unroll
 	for (int j = 0; j < KPT; ++j) {
 		uint32_t d = digit_of(k[j], shift);
-		uint32_t peers = peer_mask<K>(d);
+		uint32_t peers = peer_mask(d);
 		uint32_t leader = __ffs(peers) - 1;
 		uint32_t cnt = __popc(peers);
 		uint32_t old = 0;
@@ -216,6 +231,7 @@ radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
 		s_glob[d] = inc - hv;
 	}
 	__syncthreads();
+	uint32_t digit_base = 0;
 	if (tid < kRadix) {
 		uint32_t woff = 0, goff = 0;
 #pragma unroll
@@ -226,42 +242,64 @@ radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
 			}
 		}
 		s_tile_off[tid] += woff;
-		uint32_t digit_base = s_glob[tid] + goff;
-		// Lookback over predecessor tiles for digit tid.
-		uint32_t excl = 0;
-		if (tile > 0) {
-			long long j = (long long)tile - 1;
-			uint32_t iter = 0;
-			while (j >= 0) {
-				uint32_t sv = dev::ld_relaxed_u32(a.status + (size_t)j * kRadix + tid);
-				if ((sv & ~kStValue) == 0) {
-					if (++iter >= dev::kSpinLimit) {
-						dev::report_timeout(a.dev_status, DEV_ERR_LOOKBACK_TIMEOUT,
-							(int)tile);
-						break;
-					}
-					dev::backoff(iter);
-					continue;
-				}
-				excl += sv & kStValue;
-				if (sv & kStPrefix) break;
-				--j;
-			}
-			dev::st_relaxed_u32(a.status + (size_t)tile * kRadix + tid,
-				kStPrefix | (excl + tile_cnt));
-		}
-		s_glob[tid] = digit_base + excl - s_tile_off[tid];
+		digit_base = s_glob[tid] + goff;
 	}
 	__syncthreads();
 
-	// d. stage keys in tile order, then write each digit run coalesced.
+	// d. stage keys in tile order (before the lookback, which only decides
+	//    where each digit run goes globally).
 	K *sk = reinterpret_cast<K *>(s_stage);
 #pragma unroll
 	for (int j = 0; j < KPT; ++j) {
 		uint32_t d = digit_of(k[j], shift);
 		uint32_t pos = s_tile_off[d] + s_hist[warp * kRadix + d] + rank[j];
 		rank[j] = pos;  // keep the tile position for the value pass
-		sk[pos] = k[j];
+		if (pos < (uint32_t)TILE) sk[pos] = k[j];
+	}
+
+	// e. lookback over predecessor tiles for digit tid: kLookWindow status
+	//    words per round trip, summed in order up to the nearest prefix.
+	if (tid < kRadix) {
+		uint32_t excl = 0;
+		if (tile > 0) {
+			long long base = (long long)tile - 1;
+			uint32_t iter = 0;
+			while (base >= 0) {
+				uint32_t sv[kWin];
+#pragma unroll
+				for (int i = 0; i < kWin; ++i) {
+					long long j = base - i;
+					sv[i] = j >= 0 ? dev::ld_relaxed_u32(a.status + (size_t)j * kRadix + tid)
+								   : kStPrefix;
+				}
+				int consumed = kWin;
+				bool done = false;
+#pragma unroll
+				for (int i = 0; i < kWin; ++i) {
+					if (!done && consumed == kWin) {
+						if ((sv[i] & ~kStValue) == 0) {
+							consumed = i;  // not yet published: wait here
+						} else {
+							excl += sv[i] & kStValue;
+							if (sv[i] & kStPrefix) done = true;
+						}
+					}
+				}
+				if (done) break;
+				base -= consumed;
+				if (consumed < kWin) {
+					if (++iter >= dev::kSpinLimit) {
+						dev::report_timeout(a.dev_status, DEV_ERR_LOOKBACK_TIMEOUT,
+							(int)tile);
+						break;
+					}
+					dev::backoff(iter);
+				}
+			}
+			dev::st_relaxed_u32(a.status + (size_t)tile * kRadix + tid,
+				kStPrefix | (excl + tile_cnt));
+		}
+		s_glob[tid] = digit_base + excl - s_tile_off[tid];
 	}
 	__syncthreads();
 	uint32_t outpos[HAS_V ? KPT : 1];
@@ -283,7 +321,8 @@ radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
 		__syncthreads();
 		V *sv = reinterpret_cast<V *>(s_stage);
 #pragma unroll
-		for (int j = 0; j < KPT; ++j) sv[rank[j]] = v[j];
+		for (int j = 0; j < KPT; ++j)
+			if (rank[j] < (uint32_t)TILE) sv[rank[j]] = v[j];
 		__syncthreads();
 #pragma unroll
 		for (int i = 0; i < KPT; ++i) {

@@ -12,11 +12,13 @@
 // and registers through a padded shared-memory transpose, so every global
 // access is a coalesced 16-byte vector access. Tiles take ids from an
 // atomic counter (so a tile only ever waits on tiles already running),
-// publish their aggregate, then warp 0 looks back over a 32-tile window
-// per step until it meets an inclusive prefix. Every wait is bounded.
+// publish their aggregate, then warp 0 looks back over a 64-tile window
+// per round trip until it meets an inclusive prefix. Status words carry
+// their own ready bits, so neither side needs a memory fence. Every wait
+// is bounded.
 //
 // HBM roofline: sizeof(in) + sizeof(out) bytes per element (12 B for
-// uint -> ulong), plus 20 B of tile status per 4096 elements.
+// uint -> ulong), plus 32 B of tile status per 4096 elements.
 #include <type_traits>
 
 #include "clo_internal.h"
@@ -33,15 +35,59 @@ constexpr int kWarpElems = 32 * kItems;
 constexpr int kTile = kWarps * kWarpElems;
 constexpr int kPadded = kWarpElems + kWarpElems / 32;
 
-constexpr uint32_t kFlagAgg = 1, kFlagPrefix = 2;
-
 __device__ __forceinline__ int pidx(int i) { return i + (i >> 5); }
 
+// Tile status without fences: every value is published once into its own
+// slot of 64-bit words, each word carrying a ready bit (bit 0) and 32
+// payload bits (bits 32..63). A word is either still zero or final, so a
+// reader that sees every word of a slot ready has the whole value. Per
+// tile: [aggregate slot][inclusive-prefix slot].
 template <typename Acc>
+struct Slots {
+	static constexpr int kWords = sizeof(Acc) / 4;
+	static constexpr int kPerTile = 2 * kWords;
+};
+
+template <typename Acc>
+__device__ __forceinline__ void publish(uint64_t *w, Acc v) {
+#pragma unroll
+	for (int i = 0; i < Slots<Acc>::kWords; ++i)
+		dev::st_relaxed_u64(w + i, ((uint64_t)(uint32_t)((uint64_t)v >> (32 * i)) << 32) | 1ull);
+}
+
+// 0 = nothing published, 1 = aggregate, 2 = inclusive prefix.
+template <typename Acc>
+__device__ __forceinline__ uint32_t read_status(const uint64_t *tile_words, Acc &v) {
+	constexpr int W = Slots<Acc>::kWords;
+	uint64_t a[W], p[W];
+#pragma unroll
+	for (int i = 0; i < W; ++i) {
+		a[i] = dev::ld_relaxed_u64(tile_words + i);
+		p[i] = dev::ld_relaxed_u64(tile_words + W + i);
+	}
+	bool pr = true, ar = true;
+	uint64_t pv = 0, av = 0;
+#pragma unroll
+	for (int i = 0; i < W; ++i) {
+		pr = pr && (p[i] & 1ull);
+		ar = ar && (a[i] & 1ull);
+		pv |= (p[i] >> 32) << (32 * i);
+		av |= (a[i] >> 32) << (32 * i);
+	}
+	if (pr) {
+		v = (Acc)pv;
+		return 2;
+	}
+	if (ar) {
+		v = (Acc)av;
+		return 1;
+	}
+	return 0;
+}
+
 struct TileStatus {
-	uint32_t *flags;  // num_tiles + 1 (the last word is the tile counter)
-	Acc *agg;
-	Acc *pre;
+	uint64_t *words;     // tiles * Slots<Acc>::kPerTile
+	uint32_t *counter;   // dynamic tile ids
 };
 
 template <typename Acc>
@@ -57,10 +103,9 @@ __device__ __forceinline__ Acc warp_sum(Acc v) {
 }
 
 template <typename InT, typename OutT>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 5)
 scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, size_t n,
-	TileStatus<typename std::conditional<(sizeof(OutT) <= 4), uint32_t,
-		uint64_t>::type> ts,
+	TileStatus ts,
 	int *dev_status, bool vec_ok, long long debug_skip_tile) {
 	using Acc = typename std::conditional<(sizeof(OutT) <= 4), uint32_t,
 		uint64_t>::type;
@@ -72,7 +117,8 @@ scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, size_t n,
 
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const uint32_t num_tiles = (uint32_t)((n + kTile - 1) / kTile);
-	if (tid == 0) s_tile = atomicAdd(ts.flags + num_tiles, 1u);
+	(void)num_tiles;
+	if (tid == 0) s_tile = atomicAdd(ts.counter, 1u);
 	__syncthreads();
 	const uint32_t tile = s_tile;
 	const size_t seg = (size_t)tile * kTile + (size_t)warp * kWarpElems;
@@ -128,56 +174,55 @@ scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, size_t n,
 		}
 		const Acc aggregate = __shfl_sync(0xffffffffu, winc, kWarps - 1);
 		if (lane < kWarps) s_warp_tot[lane] = winc - wt;  // warp exclusive
-		const bool publish = (long long)tile != debug_skip_tile;
+		const bool do_publish = (long long)tile != debug_skip_tile;
+		constexpr int PT = Slots<Acc>::kPerTile;
 		Acc excl = 0;
 		if (tile == 0) {
-			if (lane == 0 && publish) {
-				ts.pre[0] = aggregate;
-				dev::st_release_u32(ts.flags + 0, kFlagPrefix);
-			}
+			if (lane == 0 && do_publish) publish<Acc>(ts.words + Slots<Acc>::kWords, aggregate);
 		} else {
-			if (lane == 0 && publish) {
-				ts.agg[tile] = aggregate;
-				dev::st_release_u32(ts.flags + tile, kFlagAgg);
-			}
+			if (lane == 0 && do_publish) publish<Acc>(ts.words + (size_t)tile * PT, aggregate);
+			// Window of 64 predecessors per round trip: lane l covers tiles
+			// pred - l and pred - 32 - l.
 			long long pred = (long long)tile - 1;
 			for (;;) {
-				const long long t = pred - lane;
-				uint32_t f = t >= 0 ? dev::ld_relaxed_u32(ts.flags + t) : kFlagPrefix;
-				bool gave_up = false;
+				const long long t0 = pred - lane, t1 = pred - 32 - lane;
+				Acc v0 = 0, v1 = 0;
+				uint32_t s0 = t0 >= 0 ? read_status<Acc>(ts.words + (size_t)t0 * PT, v0) : 2u;
+				uint32_t s1 = t1 >= 0 ? read_status<Acc>(ts.words + (size_t)t1 * PT, v1) : 2u;
 				uint32_t iter = 0;
-				while (__any_sync(0xffffffffu, f == 0)) {
-					if (f == 0) {
-						if (iter >= dev::kSpinLimit) {
-							// Give up: record the failure and treat the
-							// predecessor as a zero prefix so the kernel ends.
-							dev::report_timeout(dev_status, DEV_ERR_LOOKBACK_TIMEOUT,
-								(int)tile);
-							f = kFlagPrefix;
-							gave_up = true;
-						} else {
-							dev::backoff(iter);
-							f = dev::ld_relaxed_u32(ts.flags + t);
-						}
+				while (__any_sync(0xffffffffu, s0 == 0 || s1 == 0)) {
+					if (iter >= dev::kSpinLimit) {
+						// Give up: record the failure and treat the missing
+						// predecessors as zero prefixes so the kernel ends.
+						if (s0 == 0 || s1 == 0)
+							dev::report_timeout(dev_status, DEV_ERR_LOOKBACK_TIMEOUT, (int)tile);
+						if (s0 == 0) { s0 = 2; v0 = 0; }
+						if (s1 == 0) { s1 = 2; v1 = 0; }
+						continue;
 					}
+					dev::backoff(iter);
+					if (s0 == 0) s0 = read_status<Acc>(ts.words + (size_t)t0 * PT, v0);
+					if (s1 == 0) s1 = read_status<Acc>(ts.words + (size_t)t1 * PT, v1);
 					++iter;
 				}
-				__threadfence();
-				Acc v = 0;
-				if (t >= 0 && !gave_up) v = f == kFlagPrefix ? ts.pre[t] : ts.agg[t];
-				const uint32_t pmask = __ballot_sync(0xffffffffu, f == kFlagPrefix);
-				if (pmask) {
-					const int first = __ffs(pmask) - 1;
-					excl += warp_sum<Acc>(lane <= first ? v : (Acc)0);
+				uint32_t pm = __ballot_sync(0xffffffffu, s0 == 2);
+				if (pm) {
+					const int first = __ffs(pm) - 1;
+					excl += warp_sum<Acc>(lane <= first ? v0 : (Acc)0);
 					break;
 				}
-				excl += warp_sum<Acc>(v);
-				pred -= 32;
+				excl += warp_sum<Acc>(v0);
+				pm = __ballot_sync(0xffffffffu, s1 == 2);
+				if (pm) {
+					const int first = __ffs(pm) - 1;
+					excl += warp_sum<Acc>(lane <= first ? v1 : (Acc)0);
+					break;
+				}
+				excl += warp_sum<Acc>(v1);
+				pred -= 64;
 			}
-			if (lane == 0 && publish) {
-				ts.pre[tile] = excl + aggregate;
-				dev::st_release_u32(ts.flags + tile, kFlagPrefix);
-			}
+			if (lane == 0 && do_publish)
+				publish<Acc>(ts.words + (size_t)tile * PT + Slots<Acc>::kWords, excl + aggregate);
 		}
 		if (lane == 0) s_excl = excl;
 	}
@@ -217,15 +262,14 @@ cudaError_t launch_scan(const void *in, void *out, size_t n, CCLContext *ctx,
 		set_error(err, CLO_ERROR_ARGS, "Scan of %zu elements is too large", n);
 		return cudaErrorInvalidValue;
 	}
-	size_t flag_bytes = ((tiles + 1) * sizeof(uint32_t) + 15) / 16 * 16;
-	size_t bytes = flag_bytes + 2 * tiles * sizeof(Acc);
+	const size_t status_bytes = tiles * Slots<Acc>::kPerTile * sizeof(uint64_t);
+	const size_t bytes = status_bytes + 16;
 	char *tmp = (char *)tmp_alloc(ctx, bytes, s, err);
 	if (!tmp) return cudaErrorMemoryAllocation;
-	TileStatus<Acc> ts;
-	ts.flags = (uint32_t *)tmp;
-	ts.agg = (Acc *)(tmp + flag_bytes);
-	ts.pre = ts.agg + tiles;
-	cudaError_t e = cudaMemsetAsync(tmp, 0, (tiles + 1) * sizeof(uint32_t), s);
+	TileStatus ts;
+	ts.words = (uint64_t *)tmp;
+	ts.counter = (uint32_t *)(tmp + status_bytes);
+	cudaError_t e = cudaMemsetAsync(tmp, 0, bytes, s);
 	bool vec_ok = ((uintptr_t)in % 16 == 0) && ((uintptr_t)out % 16 == 0);
 	if (e == cudaSuccess) {
 		KernelTimer t("scan_lookback", s, (double)n * (sizeof(InT) + sizeof(OutT)));

@@ -74,7 +74,13 @@ CLO_RNG_HD uint32_t clo_rng_step_mwc64x(uint2 *s) {
  * by one. */
 CLO_RNG_HD uint32_t clo_rng_step_parkmiller(int32_t *s) {
 	int64_t p = (int64_t)(*s) * 16807;
-	int32_t v = (int32_t)(p % 2147483647);
+	// |p| < 2^46; |p| mod (2^31 - 1) by folding (2^31 = 1 modulo 2^31 - 1):
+	// a*2^31 + b = a + b, then at most one subtraction. The sign follows
+	// the dividend, as C's truncating % does.
+	uint64_t u = (uint64_t)(p < 0 ? -p : p);
+	uint64_t q = (u & 0x7FFFFFFFull) + (u >> 31);
+	if (q >= 0x7FFFFFFFull) q -= 0x7FFFFFFFull;
+	int32_t v = p < 0 ? -(int32_t)q : (int32_t)q;
 	*s = v;
 	return ((uint32_t)v) << 1;
 }
