@@ -19,6 +19,7 @@
 //
 // HBM roofline: sizeof(in) + sizeof(out) bytes per element (12 B for
 // uint -> ulong), plus 32 B of tile status per 4096 elements.
+#include <mutex>
 #include <type_traits>
 
 #include "clo_internal.h"
@@ -332,4 +333,137 @@ cudaError_t scan_exclusive(const void *in, void *out, size_t n,
 // operation.
 extern "C" void clo_gb300_debug_scan_withhold(long long tile) {
 	clo::g_debug_skip_tile = tile;
+}
+
+// ---------------------------------------------------------------------
+// Scan that allocates nothing (clo_scan_blelloch_noalloc).
+//
+// Same kernel as above; its tile statuses and tile counter live in the
+// file-scope device array below instead of a pool temporary. The array is
+// part of the library's device image: every GPU that loads the library
+// holds it (2 MiB + 16 B) until the process exits. Host code cannot use
+// the array's name as a device address (on the host it names a stand-in),
+// so the device address is looked up once per device with
+// cudaGetSymbolAddress and cached.
+// ---------------------------------------------------------------------
+
+// Largest no-allocation scan: 2^16 tiles of 4096 elements = 2^28 elements.
+#define CLO_NOALLOC_MAX_TILES (1u << 16)
+// Four status words per tile (64-bit sums) and one word for the counter.
+#define CLO_NOALLOC_WORDS (CLO_NOALLOC_MAX_TILES * 4u + 2u)
+
+static __device__ __align__(256) uint64_t g_scan_noalloc_scratch[CLO_NOALLOC_WORDS];
+
+namespace clo {
+namespace {
+
+constexpr size_t kNoAllocMaxElems = (size_t)CLO_NOALLOC_MAX_TILES * kTile;
+
+std::mutex g_noalloc_mu;
+uint64_t *g_noalloc_addr[64] = {};
+
+// Device address of the scratch array on device `ordinal`, looked up on
+// the first call for that device with the device current.
+uint64_t *noalloc_scratch(int ordinal, GError **err) {
+	if (ordinal < 0 || ordinal >= 64) {
+		set_error(err, CLO_ERROR_ARGS, "Device ordinal %d out of range", ordinal);
+		return nullptr;
+	}
+	std::lock_guard<std::mutex> lk(g_noalloc_mu);
+	if (g_noalloc_addr[ordinal] == nullptr) {
+		cudaError_t e = cudaSetDevice(ordinal);
+		void *p = nullptr;
+		if (e == cudaSuccess) e = cudaGetSymbolAddress(&p, g_scan_noalloc_scratch);
+		if (e != cudaSuccess || p == nullptr) {
+			cudaGetLastError();
+			set_error(err, CLO_ERROR_LIBRARY,
+				"cudaGetSymbolAddress of the no-allocation scan scratch failed on "
+				"device %d: %s", ordinal, cudaGetErrorString(e));
+			return nullptr;
+		}
+		g_noalloc_addr[ordinal] = (uint64_t *)p;
+	}
+	return g_noalloc_addr[ordinal];
+}
+
+template <typename InT, typename OutT>
+cudaError_t launch_scan_noalloc(const void *in, void *out, size_t n,
+	uint64_t *scratch, int *dev_status, cudaStream_t s) {
+	using Acc = typename std::conditional<(sizeof(OutT) <= 4), uint32_t,
+		uint64_t>::type;
+	const size_t tiles = (n + kTile - 1) / kTile;
+	TileStatus ts;
+	ts.words = scratch;
+	ts.counter = (uint32_t *)(scratch + (size_t)CLO_NOALLOC_MAX_TILES * 4);
+	// The array keeps the previous call's statuses: clear the words this
+	// call reads before writing (its tiles' slots and the tile counter).
+	cudaError_t e = cudaMemsetAsync(ts.words, 0,
+		tiles * Slots<Acc>::kPerTile * sizeof(uint64_t), s);
+	if (e == cudaSuccess) e = cudaMemsetAsync(ts.counter, 0, sizeof(uint64_t), s);
+	if (e != cudaSuccess) return e;
+	bool vec_ok = ((uintptr_t)in % 16 == 0) && ((uintptr_t)out % 16 == 0);
+	scan_lookback<InT, OutT><<<(unsigned)tiles, kThreads, 0, s>>>(
+		(const InT *)in, (OutT *)out, n, ts, dev_status, vec_ok, -1);
+	count_launches(1);
+	return cudaGetLastError();
+}
+
+template <typename InT>
+cudaError_t noalloc_out(const void *in, void *out, size_t n, int out_bytes,
+	uint64_t *scratch, int *st, cudaStream_t s) {
+	switch (out_bytes) {
+	case 1: return launch_scan_noalloc<InT, uint8_t>(in, out, n, scratch, st, s);
+	case 2: return launch_scan_noalloc<InT, uint16_t>(in, out, n, scratch, st, s);
+	case 4: return launch_scan_noalloc<InT, uint32_t>(in, out, n, scratch, st, s);
+	default: return launch_scan_noalloc<InT, uint64_t>(in, out, n, scratch, st, s);
+	}
+}
+
+}  // namespace
+}  // namespace clo
+
+extern "C" cl_bool clo_scan_blelloch_noalloc(CCLQueue *cq, CloType elem_type,
+	CloType sum_type, const void *d_in, void *d_out, size_t numel,
+	GError **err) {
+	using namespace clo;
+	if (err && *err) return CL_FALSE;
+	if (!cq) {
+		set_error(err, CLO_ERROR_ARGS, "NULL queue");
+		return CL_FALSE;
+	}
+	if (!type_is_integer(elem_type) || !type_is_integer(sum_type)) {
+		set_error(err, CLO_ERROR_ARGS,
+			"No-allocation scan: integer element and sum types only");
+		return CL_FALSE;
+	}
+	if (numel > kNoAllocMaxElems) {
+		set_error(err, CLO_ERROR_ARGS,
+			"No-allocation scan of %zu elements exceeds its limit of %zu elements "
+			"(the size of its static device scratch); use clo_scan_with_device_data",
+			numel, kNoAllocMaxElems);
+		return CL_FALSE;
+	}
+	if (numel == 0) return CL_TRUE;
+	if (!d_in || !d_out) {
+		set_error(err, CLO_ERROR_ARGS, "NULL input or output pointer");
+		return CL_FALSE;
+	}
+	uint64_t *scratch = noalloc_scratch(cq->ctx->ordinal, err);
+	if (!scratch) return CL_FALSE;
+	cudaSetDevice(cq->ctx->ordinal);
+	const int ob = (int)clo_type_sizeof(sum_type);
+	int *st = cq->ctx->d_status;
+	cudaStream_t s = cq->stream;
+	cudaError_t e;
+	switch (elem_type) {
+	case CLO_CHAR: e = noalloc_out<int8_t>(d_in, d_out, numel, ob, scratch, st, s); break;
+	case CLO_UCHAR: e = noalloc_out<uint8_t>(d_in, d_out, numel, ob, scratch, st, s); break;
+	case CLO_SHORT: e = noalloc_out<int16_t>(d_in, d_out, numel, ob, scratch, st, s); break;
+	case CLO_USHORT: e = noalloc_out<uint16_t>(d_in, d_out, numel, ob, scratch, st, s); break;
+	case CLO_INT: e = noalloc_out<int32_t>(d_in, d_out, numel, ob, scratch, st, s); break;
+	case CLO_UINT: e = noalloc_out<uint32_t>(d_in, d_out, numel, ob, scratch, st, s); break;
+	case CLO_LONG: e = noalloc_out<int64_t>(d_in, d_out, numel, ob, scratch, st, s); break;
+	default: e = noalloc_out<uint64_t>(d_in, d_out, numel, ob, scratch, st, s); break;
+	}
+	return cuda_ok(e, err, "clo_scan_blelloch_noalloc") ? CL_TRUE : CL_FALSE;
 }

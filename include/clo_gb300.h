@@ -65,6 +65,32 @@ void clo_gb300_timing_reset(void);
 int clo_gb300_timing_get(const char *kernel, double *total_ms,
 	double *total_bytes, cl_ulong *launches);
 
+/* Exclusive scan ("blelloch" semantics, integer types as clo_scan_new)
+ * that allocates no memory. It has no counterpart in the reference.
+ *
+ * It is for callers that cannot call cudaMalloc or any other allocator
+ * when they scan: code that runs while another thread captures a CUDA
+ * graph in global mode (where allocation calls are errors), processes
+ * whose device memory is all reserved up front by another allocator or a
+ * fixed budget (so a new allocation fails), and loops that cannot afford
+ * an allocation that may synchronise the device. The caller passes the
+ * device input and output pointers; the scan's own scratch (its tile
+ * statuses) is a file-scope device array of this library, sized for at
+ * most 2^28 elements (2 MiB, held on every GPU that loads the library
+ * until the process exits). Larger numel is rejected with CLO_ERROR_ARGS.
+ *
+ * The first call on a device looks the array's device address up
+ * (cudaGetSymbolAddress, with that device current); make that first call
+ * before any stream capture. Every call clears the part of the array it
+ * uses, on cq's stream, before the scan; all calls share the one array,
+ * so calls whose work overlaps on the GPU (different streams, no ordering
+ * between them) race and give wrong results. Asynchronous on cq: no event
+ * is created; a bounded-wait failure is reported by the next
+ * ccl_queue_finish on cq. */
+cl_bool clo_scan_blelloch_noalloc(CCLQueue *cq, CloType elem_type,
+	CloType sum_type, const void *d_in, void *d_out, size_t numel,
+	GError **err);
+
 /* Test hook for the bounded lookback waits: tile `tile` of subsequent
  * scans withholds its status, so the next tile's wait runs out, the
  * kernel ends and the next synchronising call reports CLO_ERROR_LIBRARY.
