@@ -62,12 +62,12 @@ __device__ __forceinline__ uint32_t digit_of(K k, int shift) {
 // atomic per key and digit position, except when all 32 x PER keys of a
 // warp step share the digit (sorted or constant input), which the warp
 // detects with one AND/OR reduction and adds once.
-template <typename K>
+template <typename K, int PASSES>
 __global__ void __launch_bounds__(256)
-radix_upsweep(const K *__restrict__ keys, size_t n, int passes,
-	uint32_t *__restrict__ hist) {
-	__shared__ uint32_t h[8][kRadix];
-	for (int i = threadIdx.x; i < 8 * kRadix; i += blockDim.x) (&h[0][0])[i] = 0;
+radix_upsweep(const K *__restrict__ keys, size_t n, uint32_t *__restrict__ hist) {
+	constexpr int passes = PASSES;
+	__shared__ uint32_t h[PASSES][kRadix];
+	for (int i = threadIdx.x; i < PASSES * kRadix; i += blockDim.x) (&h[0][0])[i] = 0;
 	__syncthreads();
 	const int lane = threadIdx.x & 31;
 	const size_t warp_global = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
@@ -81,6 +81,7 @@ radix_upsweep(const K *__restrict__ keys, size_t n, int passes,
 	for (size_t step = warp_global; step < full_steps; step += warps_total) {
 		uint4 v = dev::ld_stream_v4(kv4 + step * 32 + lane);
 		const K *e = reinterpret_cast<const K *>(&v);
+#pragma unroll
 		for (int p = 0; p < passes; ++p) {
 			uint32_t dd[PER];
 			uint32_t a = 0xffffffffu, o = 0u;
@@ -143,6 +144,52 @@ __device__ __forceinline__ uint32_t peer_mask(uint32_t d) {
 // Lookback window: predecessor statuses read per round trip per digit.
 constexpr int kLookWindow = 32;
 
+// Reads the statuses of tiles base, base-1, ..., base-W+1 for one digit
+// (independent loads, one round trip), adds them in order to `excl` up to
+// and including the first inclusive prefix. Returns true when a prefix was
+// reached; otherwise moves `base` to the first unpublished predecessor
+// (or past the window).
+template <int W>
+__device__ __forceinline__ bool lookback_window(const uint32_t *status, int digit,
+	long long &base, uint32_t &excl) {
+	uint32_t sv[W];
+#pragma unroll
+	for (int i = 0; i < W; ++i) {
+		long long j = base - i;
+		sv[i] = j >= 0 ? dev::ld_relaxed_u32(status + (size_t)j * kRadix + digit)
+					   : kStPrefix;
+	}
+	int consumed = W;
+	bool done = false;
+#pragma unroll
+	for (int i = 0; i < W; ++i) {
+		if (!done && consumed == W) {
+			if ((sv[i] & ~kStValue) == 0) {
+				consumed = i;
+			} else {
+				excl += sv[i] & kStValue;
+				if (sv[i] & kStPrefix) done = true;
+			}
+		}
+	}
+	if (!done) base -= consumed;
+	return done;
+}
+
+// old = atomicAdd(p, v) on shared memory for the lanes where `pred` holds,
+// as a predicated instruction (no branch around it).
+__device__ __forceinline__ uint32_t atomic_add_shared_if(bool pred, uint32_t *p,
+	uint32_t v) {
+	uint32_t old = 0;
+	const uint32_t addr = (uint32_t)__cvta_generic_to_shared(p);
+	asm volatile(
+		"{\n\t.reg .pred q;\n\t"
+		"setp.ne.u32 q, %1, 0;\n\t"
+		"@q atom.shared.add.u32 %0, [%2], %3;\n\t}"
+		: "+r"(old) : "r"((uint32_t)pred), "r"(addr), "r"(v) : "memory");
+	return old;
+}
+
 template <typename K, typename V, bool HAS_V>
 __global__ void __launch_bounds__(kThreads, 2)
 radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
@@ -183,12 +230,12 @@ radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
 	for (int j = 0; j < KPT; ++j) {
 		uint32_t d = digit_of(k[j], shift);
 		uint32_t peers = peer_mask(d);
+		uint32_t below = __popc(peers & dev::lanemask_lt());
 		uint32_t leader = __ffs(peers) - 1;
-		uint32_t cnt = __popc(peers);
-		uint32_t old = 0;
-		if (lane == (int)leader) old = atomicAdd(my_hist + d, cnt);
-		old = __shfl_sync(peers, old, leader);
-		rank[j] = old + __popc(peers & dev::lanemask_lt());
+		uint32_t old = atomic_add_shared_if(below == 0, my_hist + d, __popc(peers));
+		// Every lane reads its own group's leader (full-mask shuffle).
+		old = __shfl_sync(0xffffffffu, old, leader);
+		rank[j] = old + below;
 	}
 	__syncthreads();
 
@@ -264,37 +311,24 @@ radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
 		if (tile > 0) {
 			long long base = (long long)tile - 1;
 			uint32_t iter = 0;
-			while (base >= 0) {
-				uint32_t sv[kWin];
-#pragma unroll
-				for (int i = 0; i < kWin; ++i) {
-					long long j = base - i;
-					sv[i] = j >= 0 ? dev::ld_relaxed_u32(a.status + (size_t)j * kRadix + tid)
-								   : kStPrefix;
-				}
-				int consumed = kWin;
-				bool done = false;
-#pragma unroll
-				for (int i = 0; i < kWin; ++i) {
-					if (!done && consumed == kWin) {
-						if ((sv[i] & ~kStValue) == 0) {
-							consumed = i;  // not yet published: wait here
-						} else {
-							excl += sv[i] & kStValue;
-							if (sv[i] & kStPrefix) done = true;
-						}
-					}
-				}
-				if (done) break;
-				base -= consumed;
-				if (consumed < kWin) {
-					if (++iter >= dev::kSpinLimit) {
-						dev::report_timeout(a.dev_status, DEV_ERR_LOOKBACK_TIMEOUT,
-							(int)tile);
-						break;
-					}
+			bool done = false;
+			// A short window first (the nearest predecessors usually hold a
+			// prefix), then wide windows while only aggregates are found.
+			done = lookback_window<4>(a.status, tid, base, excl);
+			while (!done && base >= 0) {
+				// An unpublished predecessor stops a window: poll that one
+				// word until it is published (bounded), then go on.
+				uint32_t sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + tid);
+				while ((sv & ~kStValue) == 0) {
+					if (++iter >= dev::kSpinLimit) break;
 					dev::backoff(iter);
+					sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + tid);
 				}
+				if ((sv & ~kStValue) == 0) {
+					dev::report_timeout(a.dev_status, DEV_ERR_LOOKBACK_TIMEOUT, (int)tile);
+					break;
+				}
+				done = lookback_window<kWin>(a.status, tid, base, excl);
 			}
 			dev::st_relaxed_u32(a.status + (size_t)tile * kRadix + tid,
 				kStPrefix | (excl + tile_cnt));
@@ -329,6 +363,21 @@ radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
 			int p = i * kThreads + tid;
 			if (outpos[i] < a.n) vout[outpos[i]] = sv[p];
 		}
+	}
+}
+
+template <typename K>
+void launch_upsweep(int passes, int grid, cudaStream_t s, const K *keys, size_t n,
+	uint32_t *hist) {
+	switch (passes) {
+	case 1: radix_upsweep<K, 1><<<grid, 256, 0, s>>>(keys, n, hist); break;
+	case 2: radix_upsweep<K, 2><<<grid, 256, 0, s>>>(keys, n, hist); break;
+	case 3: radix_upsweep<K, 3><<<grid, 256, 0, s>>>(keys, n, hist); break;
+	case 4: radix_upsweep<K, 4><<<grid, 256, 0, s>>>(keys, n, hist); break;
+	case 5: radix_upsweep<K, 5><<<grid, 256, 0, s>>>(keys, n, hist); break;
+	case 6: radix_upsweep<K, 6><<<grid, 256, 0, s>>>(keys, n, hist); break;
+	case 7: radix_upsweep<K, 7><<<grid, 256, 0, s>>>(keys, n, hist); break;
+	default: radix_upsweep<K, 8><<<grid, 256, 0, s>>>(keys, n, hist); break;
 	}
 }
 
@@ -375,7 +424,7 @@ cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
 		size_t need = (chunks + 255) / 256;
 		if ((size_t)grid > need) grid = (int)std::max<size_t>(need, 1);
 		KernelTimer t("satradix_upsweep", s, (double)n * sizeof(K));
-		radix_upsweep<K><<<grid, 256, 0, s>>>((const K *)keys, n, passes, hist);
+		launch_upsweep<K>(passes, grid, s, (const K *)keys, n, hist);
 		t.stop();
 		launches++;
 		e = cudaGetLastError();
