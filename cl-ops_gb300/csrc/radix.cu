@@ -199,15 +199,21 @@ radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
 	// Narrower window when the value pass keeps tile positions live.
 	constexpr int kWin = HAS_V ? kLookWindow / 2 : kLookWindow;
 	extern __shared__ __align__(16) unsigned char smem[];
-	uint32_t *s_hist = reinterpret_cast<uint32_t *>(smem);        // [kWarps][256]
-	uint32_t *s_tile_off = s_hist + kWarps * kRadix;               // [256]
-	uint32_t *s_glob = s_tile_off + kRadix;                        // [256]
-	uint32_t *s_misc = s_glob + kRadix;                            // [64]
+	uint32_t *s_hist = reinterpret_cast<uint32_t *>(smem);   // [kWarps][256]
+	uint32_t *s_match = s_hist + kWarps * kRadix;            // [kWarps][256]
+	uint32_t *s_tile_off = s_match + kWarps * kRadix;        // [256]
+	uint32_t *s_glob = s_tile_off + kRadix;                  // [256]
+	uint32_t *s_misc = s_glob + kRadix;                      // [64]
 	unsigned char *s_stage = reinterpret_cast<unsigned char *>(s_misc + 64);
 
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	uint32_t *my_hist = s_hist + warp * kRadix;
+	uint32_t *my_match = s_match + warp * kRadix;
 	if (tid == 0) s_misc[0] = atomicAdd(a.tile_counter, 1u);
-	for (int i = lane; i < kRadix; i += 32) s_hist[warp * kRadix + i] = 0;
+	for (int i = lane; i < kRadix; i += 32) {
+		my_hist[i] = 0;
+		my_match[i] = 0;
+	}
 	__syncthreads();
 	const uint32_t tile = s_misc[0];
 	const size_t tile_base = (size_t)tile * TILE;
@@ -223,23 +229,15 @@ radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
 		k[j] = idx < a.n ? kin[idx] : (K)~(K)0;
 	}
 
-	// b. warp multisplit ranks.
-	uint32_t rank[KPT];
-	uint32_t *my_hist = s_hist + warp * kRadix;
+	// b. early per-warp digit counts (order-free), so the tile can publish
+	//    its aggregate before it ranks.
 #pragma unroll
-	for (int j = 0; j < KPT; ++j) {
-		uint32_t d = digit_of(k[j], shift);
-		uint32_t peers = peer_mask(d);
-		uint32_t below = __popc(peers & dev::lanemask_lt());
-		uint32_t leader = __ffs(peers) - 1;
-		uint32_t old = atomic_add_shared_if(below == 0, my_hist + d, __popc(peers));
-		// Every lane reads its own group's leader (full-mask shuffle).
-		old = __shfl_sync(0xffffffffu, old, leader);
-		rank[j] = old + below;
-	}
+	for (int j = 0; j < KPT; ++j) atomicAdd(my_hist + digit_of(k[j], shift), 1u);
 	__syncthreads();
 
-	// c. per-digit tile counts, warp prefixes, publication and lookback.
+	// c. per-digit tile counts and warp prefixes; publish the aggregate;
+	//    exclusive scans over digits of the tile counts and of the global
+	//    histogram of this digit position.
 	uint32_t tile_cnt = 0;
 	if (tid < kRadix) {
 		uint32_t sum = 0;
@@ -254,7 +252,6 @@ radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
 		if (tile == 0) dev::st_relaxed_u32(st, kStPrefix | tile_cnt);
 		else dev::st_relaxed_u32(st, kStAgg | tile_cnt);
 		a.status_next[(size_t)tile * kRadix + tid] = 0;
-		// Exclusive scan of the tile counts over digits (warps 0..7).
 		uint32_t inc = tile_cnt;
 #pragma unroll
 		for (int d = 1; d < 32; d <<= 1) {
@@ -264,7 +261,6 @@ radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
 		if (lane == 31) s_misc[8 + warp] = inc;
 		s_tile_off[tid] = inc - tile_cnt;
 	}
-	// Global digit base: exclusive scan of this pass's histogram.
 	if (tid >= kRadix && tid < 2 * kRadix) {
 		int d = tid - kRadix;
 		uint32_t hv = a.hist[d];
@@ -288,36 +284,25 @@ radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
 				goff += s_misc[16 + w];
 			}
 		}
-		s_tile_off[tid] += woff;
+		const uint32_t to = s_tile_off[tid] + woff;
+		s_tile_off[tid] = to;
 		digit_base = s_glob[tid] + goff;
+		// Tile position where each warp's run of digit tid starts.
+#pragma unroll
+		for (int w = 0; w < kWarps; ++w) s_hist[w * kRadix + tid] += to;
 	}
 	__syncthreads();
 
-	// d. stage keys in tile order (before the lookback, which only decides
-	//    where each digit run goes globally).
-	K *sk = reinterpret_cast<K *>(s_stage);
-#pragma unroll
-	for (int j = 0; j < KPT; ++j) {
-		uint32_t d = digit_of(k[j], shift);
-		uint32_t pos = s_tile_off[d] + s_hist[warp * kRadix + d] + rank[j];
-		rank[j] = pos;  // keep the tile position for the value pass
-		if (pos < (uint32_t)TILE) sk[pos] = k[j];
-	}
-
-	// e. lookback over predecessor tiles for digit tid: kLookWindow status
-	//    words per round trip, summed in order up to the nearest prefix.
+	// d. lookback over predecessor tiles (warps 0..7, one thread per digit)
+	//    while warps 8..15 already rank: a short window, then wide windows;
+	//    an unpublished predecessor is polled alone (bounded).
 	if (tid < kRadix) {
 		uint32_t excl = 0;
 		if (tile > 0) {
 			long long base = (long long)tile - 1;
 			uint32_t iter = 0;
-			bool done = false;
-			// A short window first (the nearest predecessors usually hold a
-			// prefix), then wide windows while only aggregates are found.
-			done = lookback_window<4>(a.status, tid, base, excl);
+			bool done = lookback_window<4>(a.status, tid, base, excl);
 			while (!done && base >= 0) {
-				// An unpublished predecessor stops a window: poll that one
-				// word until it is published (bounded), then go on.
 				uint32_t sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + tid);
 				while ((sv & ~kStValue) == 0) {
 					if (++iter >= dev::kSpinLimit) break;
@@ -335,7 +320,35 @@ radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
 		}
 		s_glob[tid] = digit_base + excl - s_tile_off[tid];
 	}
+
+	// e. stable ranks within each warp, written straight to tile positions:
+	//    lanes holding the same digit in a round find each other through a
+	//    shared-memory OR (in lane order, rounds in index order); the lowest
+	//    of them advances the warp's run start and clears the mask.
+	K *sk = reinterpret_cast<K *>(s_stage);
+	uint32_t tpos[HAS_V ? KPT : 1];
+	const uint32_t lt = dev::lanemask_lt();
+#pragma unroll
+	for (int j = 0; j < KPT; ++j) {
+		const uint32_t d = digit_of(k[j], shift);
+		atomicOr(my_match + d, 1u << lane);
+		__syncwarp();
+		const uint32_t peers = my_match[d];
+		const uint32_t start = my_hist[d];
+		__syncwarp();
+		const uint32_t below = __popc(peers & lt);
+		if (below == 0) {
+			my_hist[d] = start + __popc(peers);
+			my_match[d] = 0;
+		}
+		__syncwarp();
+		const uint32_t pos = start + below;
+		if (pos < (uint32_t)TILE) sk[pos] = k[j];
+		if (HAS_V) tpos[j] = pos;
+	}
 	__syncthreads();
+
+	// f. write each digit run out coalesced.
 	uint32_t outpos[HAS_V ? KPT : 1];
 #pragma unroll
 	for (int i = 0; i < KPT; ++i) {
@@ -356,7 +369,7 @@ radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
 		V *sv = reinterpret_cast<V *>(s_stage);
 #pragma unroll
 		for (int j = 0; j < KPT; ++j)
-			if (rank[j] < (uint32_t)TILE) sv[rank[j]] = v[j];
+			if (tpos[j] < (uint32_t)TILE) sv[tpos[j]] = v[j];
 		__syncthreads();
 #pragma unroll
 		for (int i = 0; i < KPT; ++i) {
@@ -385,7 +398,7 @@ template <typename K, typename V, bool HAS_V>
 size_t onesweep_smem() {
 	constexpr int TILE = KeyCfg<K>::kTile;
 	size_t stage = (size_t)TILE * (sizeof(K) > sizeof(V) || !HAS_V ? sizeof(K) : sizeof(V));
-	return (kWarps * kRadix + 2 * kRadix + 64) * sizeof(uint32_t) + stage;
+	return (2 * kWarps * kRadix + 2 * kRadix + 64) * sizeof(uint32_t) + stage;
 }
 
 template <typename K, typename V, bool HAS_V>
