@@ -191,13 +191,13 @@ __device__ __forceinline__ uint32_t atomic_add_shared_if(bool pred, uint32_t *p,
 }
 
 template <typename K, typename V, bool HAS_V>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, (HAS_V || sizeof(K) > 4) ? 2 : 3)
 radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
 	const V *__restrict__ vin, V *__restrict__ vout, PassArgs a) {
 	constexpr int KPT = KeyCfg<K>::kKpt;
 	constexpr int TILE = KeyCfg<K>::kTile;
 	// Narrower window when the value pass keeps tile positions live.
-	constexpr int kWin = HAS_V ? kLookWindow / 2 : kLookWindow;
+	constexpr int kWin = kLookWindow / 2;
 	extern __shared__ __align__(16) unsigned char smem[];
 	uint32_t *s_hist = reinterpret_cast<uint32_t *>(smem);   // [kWarps][256]
 	uint32_t *s_match = s_hist + kWarps * kRadix;            // [kWarps][256]
@@ -379,6 +379,200 @@ radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
 	}
 }
 
+// ----------------------------------------------------- pipelined pass
+// Keys-only pass run by persistent CTAs with two tiles in flight each.
+// Per iteration a CTA counts, publishes and ranks its current tile c; in
+// the same interval its warps 0..7 look back for its previous tile p,
+// whose predecessors have had a whole iteration to publish, so the window
+// usually ends at the first round trip; then it loads the next tile's keys
+// into registers and writes p out while those loads are in flight.
+// Deadlock-free: a tile publishes its aggregate before its CTA waits on
+// anything, and a CTA holding an unpublished (just claimed) tile waits only
+// on tiles below its previous tile, so the lowest unpublished tile always
+// belongs to a CTA whose wait ends.
+template <typename K>
+__device__ __forceinline__ void load_tile_keys(K (&k)[KeyCfg<K>::kKpt],
+	const K *__restrict__ kin, size_t n, uint32_t tile, int warp, int lane) {
+	constexpr int KPT = KeyCfg<K>::kKpt;
+	const size_t wbase = (size_t)tile * KeyCfg<K>::kTile + (size_t)warp * (KPT * 32);
+#pragma unroll
+	for (int j = 0; j < KPT; ++j) {
+		size_t idx = wbase + (size_t)j * 32 + lane;
+		k[j] = idx < n ? kin[idx] : (K)~(K)0;
+	}
+}
+
+template <typename K>
+__global__ void __launch_bounds__(kThreads, 2)
+radix_onesweep_pp(const K *__restrict__ kin, K *__restrict__ kout, PassArgs a,
+	uint32_t num_tiles) {
+	constexpr int KPT = KeyCfg<K>::kKpt;
+	constexpr int TILE = KeyCfg<K>::kTile;
+	constexpr int kWin = kLookWindow / 2;
+	extern __shared__ __align__(16) unsigned char smem[];
+	uint32_t *s_hist = reinterpret_cast<uint32_t *>(smem);   // [kWarps][256]
+	uint32_t *s_match = s_hist + kWarps * kRadix;            // [kWarps][256]
+	uint32_t *s_tile_off = s_match + kWarps * kRadix;        // [2][256]
+	uint32_t *s_tile_cnt = s_tile_off + 2 * kRadix;          // [2][256]
+	uint32_t *s_glob = s_tile_cnt + 2 * kRadix;              // [256]
+	uint32_t *s_dbase = s_glob + kRadix;                     // [256]
+	uint32_t *s_misc = s_dbase + kRadix;                     // [64]
+	K *s_stage = reinterpret_cast<K *>(s_misc + 64);         // [2][TILE]
+
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	uint32_t *my_hist = s_hist + warp * kRadix;
+	uint32_t *my_match = s_match + warp * kRadix;
+	const int shift = a.shift;
+	const uint32_t lt = dev::lanemask_lt();
+
+	// Global digit base of this pass: exclusive scan of its histogram.
+	if (tid >= kRadix && tid < 2 * kRadix) {
+		const int d = tid - kRadix;
+		const uint32_t hv = a.hist[d];
+		uint32_t inc = hv;
+#pragma unroll
+		for (int s = 1; s < 32; s <<= 1) {
+			uint32_t t = __shfl_up_sync(0xffffffffu, inc, s);
+			if (lane >= s) inc += t;
+		}
+		if (lane == 31) s_misc[16 + (warp - 8)] = inc;
+		s_dbase[d] = inc - hv;
+	}
+	if (tid == 0) s_misc[0] = atomicAdd(a.tile_counter, 1u);
+	for (int i = lane; i < kRadix; i += 32) my_match[i] = 0;
+	__syncthreads();
+	if (tid >= kRadix && tid < 2 * kRadix) {
+		uint32_t goff = 0;
+#pragma unroll
+		for (int w = 8; w < 16; ++w)
+			if (w < warp) goff += s_misc[16 + (w - 8)];
+		s_dbase[tid - kRadix] += goff;
+	}
+	uint32_t c = s_misc[0];
+	K k[KPT];
+	if (c < num_tiles) load_tile_keys<K>(k, kin, a.n, c, warp, lane);
+	long long p = -1;
+	int it = 0;
+	for (;;) {
+		const bool have_c = c < num_tiles;
+		const int sc = it & 1, sp = sc ^ 1;
+		if (have_c) {
+			for (int i = lane; i < kRadix; i += 32) my_hist[i] = 0;
+			__syncwarp();
+#pragma unroll
+			for (int j = 0; j < KPT; ++j) atomicAdd(my_hist + digit_of(k[j], shift), 1u);
+		}
+		__syncthreads();  // counts complete; previous write-out done
+		if (have_c && tid < kRadix) {
+			uint32_t sum = 0;
+#pragma unroll
+			for (int w = 0; w < kWarps; ++w) {
+				uint32_t cw = s_hist[w * kRadix + tid];
+				s_hist[w * kRadix + tid] = sum;
+				sum += cw;
+			}
+			s_tile_cnt[sc * kRadix + tid] = sum;
+			uint32_t *st = a.status + (size_t)c * kRadix + tid;
+			if (c == 0) dev::st_relaxed_u32(st, kStPrefix | sum);
+			else dev::st_relaxed_u32(st, kStAgg | sum);
+			a.status_next[(size_t)c * kRadix + tid] = 0;
+			uint32_t inc = sum;
+#pragma unroll
+			for (int d = 1; d < 32; d <<= 1) {
+				uint32_t t = __shfl_up_sync(0xffffffffu, inc, d);
+				if (lane >= d) inc += t;
+			}
+			if (lane == 31) s_misc[8 + warp] = inc;
+			s_tile_off[sc * kRadix + tid] = inc - sum;
+		}
+		__syncthreads();
+		if (have_c && tid < kRadix) {
+			uint32_t woff = 0;
+#pragma unroll
+			for (int w = 0; w < 8; ++w)
+				if (w < warp) woff += s_misc[8 + w];
+			const uint32_t to = s_tile_off[sc * kRadix + tid] + woff;
+			s_tile_off[sc * kRadix + tid] = to;
+#pragma unroll
+			for (int w = 0; w < kWarps; ++w) s_hist[w * kRadix + tid] += to;
+		}
+		if (tid == 0) s_misc[1] = have_c ? atomicAdd(a.tile_counter, 1u) : num_tiles;
+		__syncthreads();
+
+		// Lookback for the previous tile (warps 0..7, one digit each).
+		if (p >= 0 && tid < kRadix) {
+			uint32_t excl = 0;
+			if (p > 0) {
+				long long base = p - 1;
+				uint32_t iter = 0;
+				bool done = lookback_window<4>(a.status, tid, base, excl);
+				while (!done && base >= 0) {
+					uint32_t sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + tid);
+					while ((sv & ~kStValue) == 0) {
+						if (++iter >= dev::kSpinLimit) break;
+						dev::backoff(iter);
+						sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + tid);
+					}
+					if ((sv & ~kStValue) == 0) {
+						dev::report_timeout(a.dev_status, DEV_ERR_LOOKBACK_TIMEOUT, (int)p);
+						break;
+					}
+					done = lookback_window<kWin>(a.status, tid, base, excl);
+				}
+				dev::st_relaxed_u32(a.status + (size_t)p * kRadix + tid,
+					kStPrefix | (excl + s_tile_cnt[sp * kRadix + tid]));
+			}
+			s_glob[tid] = s_dbase[tid] + excl - s_tile_off[sp * kRadix + tid];
+		}
+
+		// Stable warp ranks of the current tile, staged in its slot.
+		if (have_c) {
+			K *sk = s_stage + (size_t)sc * TILE;
+#pragma unroll
+			for (int j = 0; j < KPT; ++j) {
+				const uint32_t d = digit_of(k[j], shift);
+				atomicOr(my_match + d, 1u << lane);
+				__syncwarp();
+				const uint32_t peers = my_match[d];
+				const uint32_t start = my_hist[d];
+				__syncwarp();
+				const uint32_t below = __popc(peers & lt);
+				if (below == 0) {
+					my_hist[d] = start + __popc(peers);
+					my_match[d] = 0;
+				}
+				__syncwarp();
+				const uint32_t pos = start + below;
+				if (pos < (uint32_t)TILE) sk[pos] = k[j];
+			}
+		}
+		__syncthreads();  // ranks staged, lookback results and next id visible
+
+		const uint32_t next = s_misc[1];
+		if (next < num_tiles) load_tile_keys<K>(k, kin, a.n, next, warp, lane);
+		if (p >= 0) {
+			const K *sp_stage = s_stage + (size_t)sp * TILE;
+#pragma unroll
+			for (int i = 0; i < KPT; ++i) {
+				const int q = i * kThreads + tid;
+				const K key = sp_stage[q];
+				const size_t o = (size_t)s_glob[digit_of(key, shift)] + q;
+				if (o < a.n) kout[o] = key;
+			}
+		}
+		if (!have_c) break;
+		p = c;
+		c = next;
+		++it;
+	}
+}
+
+template <typename K>
+size_t onesweep_pp_smem() {
+	return (2 * kWarps * kRadix + 6 * kRadix + 64) * sizeof(uint32_t) +
+		2 * (size_t)KeyCfg<K>::kTile * sizeof(K);
+}
+
 template <typename K>
 void launch_upsweep(int passes, int grid, cudaStream_t s, const K *keys, size_t n,
 	uint32_t *hist) {
@@ -458,7 +652,33 @@ cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
 			for (int p = 0; p < passes; ++p) active.push_back(p);
 		}
 	}
-	if (e == cudaSuccess) {
+	if (e == cudaSuccess && !HAS_V) {
+		// Keys only: the pipelined persistent pass.
+		const size_t smem = onesweep_pp_smem<K>();
+		e = cudaFuncSetAttribute(radix_onesweep_pp<K>,
+			cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		const unsigned grid = (unsigned)std::min<size_t>(tiles, 2 * (size_t)ctx->sm_count);
+		K *src_k = (K *)keys, *dst_k = alt_k;
+		for (size_t q = 0; q < active.size() && e == cudaSuccess; ++q) {
+			PassArgs pa;
+			pa.hist = hist + (size_t)active[q] * kRadix;
+			pa.status = st[q & 1];
+			pa.status_next = st[(q + 1) & 1];
+			pa.tile_counter = cnt + active[q];
+			pa.dev_status = ctx->d_status;
+			pa.n = n;
+			pa.shift = active[q] * kRadixBits;
+			KernelTimer t("satradix_onesweep", s, 2.0 * (double)n * sizeof(K));
+			radix_onesweep_pp<K><<<grid, kThreads, smem, s>>>(src_k, dst_k, pa,
+				(uint32_t)tiles);
+			t.stop();
+			launches++;
+			e = cudaGetLastError();
+			std::swap(src_k, dst_k);
+		}
+		if (e == cudaSuccess && (active.size() & 1))
+			e = cudaMemcpyAsync(keys, alt_k, n * sizeof(K), cudaMemcpyDeviceToDevice, s);
+	} else if (e == cudaSuccess) {
 		size_t smem = onesweep_smem<K, V, HAS_V>();
 		auto kern = radix_onesweep<K, V, HAS_V>;
 		e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
