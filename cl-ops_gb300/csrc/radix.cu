@@ -144,6 +144,9 @@ __device__ __forceinline__ uint32_t peer_mask(uint32_t d) {
 // Lookback window: predecessor statuses read per round trip per digit.
 constexpr int kLookWindow = 32;
 
+// Threads per CTA of the chunked pass.
+constexpr int kChunkThreads = 256;
+
 // Reads the statuses of tiles base, base-1, ..., base-W+1 for one digit
 // (independent loads, one round trip), adds them in order to `excl` up to
 // and including the first inclusive prefix. Returns true when a prefix was
@@ -416,7 +419,9 @@ radix_onesweep_pp(const K *__restrict__ kin, K *__restrict__ kout, PassArgs a,
 	uint32_t *s_tile_cnt = s_tile_off + 2 * kRadix;          // [2][256]
 	uint32_t *s_glob = s_tile_cnt + 2 * kRadix;              // [256]
 	uint32_t *s_dbase = s_glob + kRadix;                     // [256]
-	uint32_t *s_misc = s_dbase + kRadix;                     // [64]
+	uint32_t *s_half = s_dbase + kRadix;                     // [2][256]
+	uint32_t *s_part = s_half + 2 * kRadix;                  // [256]
+	uint32_t *s_misc = s_part + kRadix;                      // [64]
 	K *s_stage = reinterpret_cast<K *>(s_misc + 64);         // [2][TILE]
 
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -463,40 +468,58 @@ radix_onesweep_pp(const K *__restrict__ kin, K *__restrict__ kout, PassArgs a,
 			for (int j = 0; j < KPT; ++j) atomicAdd(my_hist + digit_of(k[j], shift), 1u);
 		}
 		__syncthreads();  // counts complete; previous write-out done
-		if (have_c && tid < kRadix) {
-			uint32_t sum = 0;
+		// Warp prefixes per digit, by all 512 threads: thread (d, h) takes
+		// warps 8h..8h+7 of digit d with independent loads.
+		const int pd = tid & (kRadix - 1), ph = tid >> 8;
+		uint32_t cw[8];
+		if (have_c) {
 #pragma unroll
-			for (int w = 0; w < kWarps; ++w) {
-				uint32_t cw = s_hist[w * kRadix + tid];
-				s_hist[w * kRadix + tid] = sum;
-				sum += cw;
-			}
-			s_tile_cnt[sc * kRadix + tid] = sum;
-			uint32_t *st = a.status + (size_t)c * kRadix + tid;
-			if (c == 0) dev::st_relaxed_u32(st, kStPrefix | sum);
-			else dev::st_relaxed_u32(st, kStAgg | sum);
-			a.status_next[(size_t)c * kRadix + tid] = 0;
-			uint32_t inc = sum;
+			for (int i = 0; i < 8; ++i) cw[i] = s_hist[(8 * ph + i) * kRadix + pd];
+			uint32_t run = 0;
 #pragma unroll
-			for (int d = 1; d < 32; d <<= 1) {
-				uint32_t t = __shfl_up_sync(0xffffffffu, inc, d);
-				if (lane >= d) inc += t;
+			for (int i = 0; i < 8; ++i) {
+				uint32_t t = cw[i];
+				cw[i] = run;
+				run += t;
 			}
-			if (lane == 31) s_misc[8 + warp] = inc;
-			s_tile_off[sc * kRadix + tid] = inc - sum;
+			s_half[ph * kRadix + pd] = run;
 		}
 		__syncthreads();
-		if (have_c && tid < kRadix) {
-			uint32_t woff = 0;
+		if (have_c) {
+			const uint32_t lo = s_half[pd];
+			const uint32_t sum = lo + s_half[kRadix + pd];
+			if (ph == 1) {
 #pragma unroll
-			for (int w = 0; w < 8; ++w)
-				if (w < warp) woff += s_misc[8 + w];
-			const uint32_t to = s_tile_off[sc * kRadix + tid] + woff;
-			s_tile_off[sc * kRadix + tid] = to;
+				for (int i = 0; i < 8; ++i) cw[i] += lo;
+			} else {
+				s_tile_cnt[sc * kRadix + pd] = sum;
+				uint32_t *st = a.status + (size_t)c * kRadix + pd;
+				if (c == 0) dev::st_relaxed_u32(st, kStPrefix | sum);
+				else dev::st_relaxed_u32(st, kStAgg | sum);
+				a.status_next[(size_t)c * kRadix + pd] = 0;
+				uint32_t inc = sum;
 #pragma unroll
-			for (int w = 0; w < kWarps; ++w) s_hist[w * kRadix + tid] += to;
+				for (int d = 1; d < 32; d <<= 1) {
+					uint32_t t = __shfl_up_sync(0xffffffffu, inc, d);
+					if (lane >= d) inc += t;
+				}
+				if (lane == 31) s_misc[8 + warp] = inc;
+				s_part[pd] = inc - sum;
+			}
 		}
 		if (tid == 0) s_misc[1] = have_c ? atomicAdd(a.tile_counter, 1u) : num_tiles;
+		__syncthreads();
+		if (have_c) {
+			uint32_t woff = 0;
+			const int dw = pd >> 5;
+#pragma unroll
+			for (int w = 0; w < 8; ++w)
+				if (w < dw) woff += s_misc[8 + w];
+			const uint32_t to = s_part[pd] + woff;
+#pragma unroll
+			for (int i = 0; i < 8; ++i) s_hist[(8 * ph + i) * kRadix + pd] = to + cw[i];
+			if (ph == 0) s_tile_off[sc * kRadix + pd] = to;
+		}
 		__syncthreads();
 
 		// Lookback for the previous tile (warps 0..7, one digit each).
@@ -569,8 +592,277 @@ radix_onesweep_pp(const K *__restrict__ kin, K *__restrict__ kout, PassArgs a,
 
 template <typename K>
 size_t onesweep_pp_smem() {
-	return (2 * kWarps * kRadix + 6 * kRadix + 64) * sizeof(uint32_t) +
+	return (2 * kWarps * kRadix + 9 * kRadix + 64) * sizeof(uint32_t) +
 		2 * (size_t)KeyCfg<K>::kTile * sizeof(K);
+}
+
+// ------------------------------------------------------- chunked pass
+// One CTA per contiguous chunk of tiles (chunks claimed in order from an
+// atomic counter). The CTA first counts the digit over its whole chunk
+// with streaming 16-byte loads, publishes the chunk's counts and looks
+// back over the preceding chunks -- one decoupled lookback per CTA and
+// pass instead of one per tile, so no tile ever waits on another CTA --
+// then ranks and scatters its tiles in order, each digit's run continuing
+// where the previous tile's ended. The counting read costs key-size bytes
+// per key on top of the pass's read and write. THREADS is 256 or 512;
+// with 256 threads (4096-key tiles) four CTAs share an SM and hide each
+// other's per-tile latency.
+template <typename K, int THREADS>
+struct ChunkCfg {
+	static constexpr int kWarps = THREADS / 32;
+	static constexpr int kKpt = sizeof(K) <= 4 ? 16 : 8;
+	static constexpr int kTile = THREADS * kKpt;
+	static constexpr int kHalves = THREADS / kRadix;          // 1 or 2
+	static constexpr int kWarpsPerHalf = kWarps / kHalves;    // 8
+	static constexpr int kMinBlocks = THREADS == 256 ? 4 : 2;
+};
+
+template <typename K, int THREADS>
+__device__ __forceinline__ void chunk_load_keys(K (&k)[ChunkCfg<K, THREADS>::kKpt],
+	const K *__restrict__ kin, size_t n, uint32_t tile, int warp, int lane) {
+	constexpr int KPT = ChunkCfg<K, THREADS>::kKpt;
+	const size_t wbase = (size_t)tile * ChunkCfg<K, THREADS>::kTile +
+		(size_t)warp * (KPT * 32);
+#pragma unroll
+	for (int j = 0; j < KPT; ++j) {
+		size_t idx = wbase + (size_t)j * 32 + lane;
+		k[j] = idx < n ? kin[idx] : (K)~(K)0;
+	}
+}
+
+template <typename K, typename V, bool HAS_V, int THREADS>
+__global__ void __launch_bounds__(THREADS, ChunkCfg<K, THREADS>::kMinBlocks)
+radix_pass_chunked(const K *__restrict__ kin, K *__restrict__ kout,
+	const V *__restrict__ vin, V *__restrict__ vout, PassArgs a,
+	uint32_t num_tiles, uint32_t num_chunks) {
+	using Cfg = ChunkCfg<K, THREADS>;
+	constexpr int KPT = Cfg::kKpt;
+	constexpr int TILE = Cfg::kTile;
+	constexpr int WARPS = Cfg::kWarps;
+	constexpr int WPH = Cfg::kWarpsPerHalf;
+	constexpr int kWin = kLookWindow / 2;
+	extern __shared__ __align__(16) unsigned char smem[];
+	uint32_t *s_hist = reinterpret_cast<uint32_t *>(smem);   // [WARPS][256]
+	uint32_t *s_match = s_hist + WARPS * kRadix;             // [WARPS][256]
+	uint32_t *s_tile_off = s_match + WARPS * kRadix;         // [256]
+	uint32_t *s_tile_cnt = s_tile_off + kRadix;              // [256]
+	uint32_t *s_run = s_tile_cnt + kRadix;                   // [256]
+	uint32_t *s_half = s_run + kRadix;                       // [2][256]
+	uint32_t *s_part = s_half + 2 * kRadix;                  // [256]
+	uint32_t *s_misc = s_part + kRadix;                      // [64]
+	unsigned char *s_stage = reinterpret_cast<unsigned char *>(s_misc + 64);
+
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	uint32_t *my_hist = s_hist + warp * kRadix;
+	uint32_t *my_match = s_match + warp * kRadix;
+	const int shift = a.shift;
+	const uint32_t lt = dev::lanemask_lt();
+	const int pd = tid & (kRadix - 1), ph = tid >> 8;
+	const int dw = pd >> 5;  // warp (within a half) that owns digit pd
+
+	if (tid == 0) s_misc[0] = atomicAdd(a.tile_counter, 1u);
+	for (int i = lane; i < kRadix; i += 32) {
+		my_hist[i] = 0;
+		my_match[i] = 0;
+	}
+	// Global digit base of this pass: exclusive scan of its histogram.
+	if (ph == 0) {
+		const uint32_t hv = a.hist[pd];
+		uint32_t inc = hv;
+#pragma unroll
+		for (int s = 1; s < 32; s <<= 1) {
+			uint32_t t = __shfl_up_sync(0xffffffffu, inc, s);
+			if (lane >= s) inc += t;
+		}
+		if (lane == 31) s_misc[16 + dw] = inc;
+		s_part[pd] = inc - hv;
+	}
+	__syncthreads();
+	const uint32_t c = s_misc[0];
+	if (c >= num_chunks) return;
+	uint32_t run_init = 0;
+	if (ph == 0) {
+		uint32_t goff = 0;
+#pragma unroll
+		for (int w = 0; w < 8; ++w)
+			if (w < dw) goff += s_misc[16 + w];
+		run_init = s_part[pd] + goff;
+	}
+	const uint32_t t0 = (uint32_t)((uint64_t)c * num_tiles / num_chunks);
+	const uint32_t t1 = (uint32_t)((uint64_t)(c + 1) * num_tiles / num_chunks);
+	const size_t k_lo = (size_t)t0 * TILE;
+	const size_t k_hi = (size_t)t1 * TILE < a.n ? (size_t)t1 * TILE : a.n;
+
+	// Phase 1: digit counts of the whole chunk.
+	{
+		constexpr int PER = 16 / sizeof(K);
+		const bool vec = ((uintptr_t)(kin + k_lo) % 16) == 0;
+		const size_t nvec = vec ? (k_hi - k_lo) / PER : 0;
+		const uint4 *src = reinterpret_cast<const uint4 *>(kin + k_lo);
+#pragma unroll 4
+		for (size_t i = tid; i < nvec; i += THREADS) {
+			uint4 v = dev::ld_stream_v4(src + i);
+			const K *e = reinterpret_cast<const K *>(&v);
+#pragma unroll
+			for (int q = 0; q < PER; ++q) atomicAdd(my_hist + digit_of(e[q], shift), 1u);
+		}
+		for (size_t i = k_lo + nvec * PER + tid; i < k_hi; i += THREADS)
+			atomicAdd(my_hist + digit_of(kin[i], shift), 1u);
+	}
+	__syncthreads();
+	if (ph == 0) {
+		uint32_t cnt = 0;
+#pragma unroll
+		for (int w = 0; w < WARPS; ++w) cnt += s_hist[w * kRadix + pd];
+		uint32_t *st = a.status + (size_t)c * kRadix + pd;
+		if (c == 0) dev::st_relaxed_u32(st, kStPrefix | cnt);
+		else dev::st_relaxed_u32(st, kStAgg | cnt);
+		a.status_next[(size_t)c * kRadix + pd] = 0;
+		uint32_t excl = 0;
+		if (c > 0) {
+			long long base = (long long)c - 1;
+			uint32_t iter = 0;
+			bool done = lookback_window<4>(a.status, pd, base, excl);
+			while (!done && base >= 0) {
+				uint32_t sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + pd);
+				while ((sv & ~kStValue) == 0) {
+					if (++iter >= dev::kSpinLimit) break;
+					dev::backoff(iter);
+					sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + pd);
+				}
+				if ((sv & ~kStValue) == 0) {
+					dev::report_timeout(a.dev_status, DEV_ERR_LOOKBACK_TIMEOUT, (int)c);
+					break;
+				}
+				done = lookback_window<kWin>(a.status, pd, base, excl);
+			}
+			dev::st_relaxed_u32(st, kStPrefix | (excl + cnt));
+		}
+		s_run[pd] = run_init;
+		s_tile_cnt[pd] = excl;  // the first tile's run starts after excl
+	}
+	__syncthreads();
+
+	// Phase 2: tiles of the chunk in order.
+	K k[KPT];
+	if (t0 < t1) chunk_load_keys<K, THREADS>(k, kin, a.n, t0, warp, lane);
+	for (uint32_t t = t0; t < t1; ++t) {
+		for (int i = lane; i < kRadix; i += 32) my_hist[i] = 0;
+		__syncwarp();
+#pragma unroll
+		for (int j = 0; j < KPT; ++j) atomicAdd(my_hist + digit_of(k[j], shift), 1u);
+		__syncthreads();
+		// Warp prefixes per digit: thread (pd, ph) takes warps
+		// WPH*ph .. WPH*ph + WPH - 1 with independent loads.
+		uint32_t cw[WPH];
+#pragma unroll
+		for (int i = 0; i < WPH; ++i) cw[i] = s_hist[(WPH * ph + i) * kRadix + pd];
+		uint32_t run = 0;
+#pragma unroll
+		for (int i = 0; i < WPH; ++i) {
+			uint32_t tmp = cw[i];
+			cw[i] = run;
+			run += tmp;
+		}
+		uint32_t sum = run;
+		if (Cfg::kHalves == 2) {
+			s_half[ph * kRadix + pd] = run;
+			__syncthreads();
+			const uint32_t lo = s_half[pd];
+			sum = lo + s_half[kRadix + pd];
+			if (ph == 1) {
+#pragma unroll
+				for (int i = 0; i < WPH; ++i) cw[i] += lo;
+			}
+		}
+		if (ph == 0) {
+			// Advance the run by the previous tile's count (or the lookback).
+			s_run[pd] += s_tile_cnt[pd];
+			s_tile_cnt[pd] = sum;
+			uint32_t inc = sum;
+#pragma unroll
+			for (int d = 1; d < 32; d <<= 1) {
+				uint32_t tt = __shfl_up_sync(0xffffffffu, inc, d);
+				if (lane >= d) inc += tt;
+			}
+			if (lane == 31) s_misc[8 + dw] = inc;
+			s_part[pd] = inc - sum;
+		}
+		__syncthreads();
+		{
+			uint32_t woff = 0;
+#pragma unroll
+			for (int w = 0; w < 8; ++w)
+				if (w < dw) woff += s_misc[8 + w];
+			const uint32_t to = s_part[pd] + woff;
+#pragma unroll
+			for (int i = 0; i < WPH; ++i) s_hist[(WPH * ph + i) * kRadix + pd] = to + cw[i];
+			if (ph == 0) s_tile_off[pd] = to;
+		}
+		__syncthreads();
+		K *sk = reinterpret_cast<K *>(s_stage);
+		uint32_t tpos[HAS_V ? KPT : 1];
+#pragma unroll
+		for (int j = 0; j < KPT; ++j) {
+			const uint32_t d = digit_of(k[j], shift);
+			atomicOr(my_match + d, 1u << lane);
+			__syncwarp();
+			const uint32_t peers = my_match[d];
+			const uint32_t start = my_hist[d];
+			__syncwarp();
+			const uint32_t below = __popc(peers & lt);
+			if (below == 0) {
+				my_hist[d] = start + __popc(peers);
+				my_match[d] = 0;
+			}
+			__syncwarp();
+			const uint32_t pos = start + below;
+			if (pos < (uint32_t)TILE) sk[pos] = k[j];
+			if (HAS_V) tpos[j] = pos;
+		}
+		__syncthreads();
+		if (!HAS_V && t + 1 < t1) chunk_load_keys<K, THREADS>(k, kin, a.n, t + 1, warp, lane);
+		uint32_t outpos[HAS_V ? KPT : 1];
+#pragma unroll
+		for (int i = 0; i < KPT; ++i) {
+			const int q = i * THREADS + tid;
+			const K key = sk[q];
+			const uint32_t d = digit_of(key, shift);
+			const size_t o = (size_t)s_run[d] + q - s_tile_off[d];
+			if (o < a.n) kout[o] = key;
+			if (HAS_V) outpos[i] = (uint32_t)o;
+		}
+		if (HAS_V) {
+			V v[KPT];
+			const size_t wbase = (size_t)t * TILE + (size_t)warp * (KPT * 32);
+#pragma unroll
+			for (int j = 0; j < KPT; ++j) {
+				size_t idx = wbase + (size_t)j * 32 + lane;
+				v[j] = idx < a.n ? vin[idx] : (V)0;
+			}
+			__syncthreads();
+			V *sv = reinterpret_cast<V *>(s_stage);
+#pragma unroll
+			for (int j = 0; j < KPT; ++j)
+				if (tpos[j] < (uint32_t)TILE) sv[tpos[j]] = v[j];
+			__syncthreads();
+#pragma unroll
+			for (int i = 0; i < KPT; ++i) {
+				const int q = i * THREADS + tid;
+				if (outpos[i] < a.n) vout[outpos[i]] = sv[q];
+			}
+			if (t + 1 < t1) chunk_load_keys<K, THREADS>(k, kin, a.n, t + 1, warp, lane);
+			__syncthreads();
+		}
+	}
+}
+
+template <typename K, typename V, bool HAS_V, int THREADS>
+size_t chunked_smem() {
+	constexpr int TILE = ChunkCfg<K, THREADS>::kTile;
+	size_t stage = (size_t)TILE * (sizeof(K) > sizeof(V) || !HAS_V ? sizeof(K) : sizeof(V));
+	return (2 * ChunkCfg<K, THREADS>::kWarps * kRadix + 7 * kRadix + 64) * sizeof(uint32_t) +
+		stage;
 }
 
 template <typename K>
@@ -607,7 +899,14 @@ cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
 		return cudaErrorInvalidValue;
 	}
 	const size_t tiles = (n + TILE - 1) / TILE;
-	const size_t status_words = tiles * kRadix;
+	// The chunked pass: tiles of ChunkCfg size, one chunk per CTA.
+	constexpr int CT = kChunkThreads;
+	constexpr int CTILE = ChunkCfg<K, CT>::kTile;
+	const size_t ctiles = (n + CTILE - 1) / CTILE;
+	const uint32_t chunks = (uint32_t)std::min<size_t>(ctiles,
+		(size_t)ChunkCfg<K, CT>::kMinBlocks * ctx->sm_count);
+	// Status slots: one per chunk (chunked pass) or per tile (tile passes).
+	const size_t status_words = std::max<size_t>(tiles, chunks) * kRadix;
 	// Scratch: [hist passes*256][counters 8][status0][status1][alt keys][alt vals]
 	size_t off_hist = 0;
 	size_t off_cnt = off_hist + (size_t)passes * kRadix * 4;
@@ -652,35 +951,9 @@ cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
 			for (int p = 0; p < passes; ++p) active.push_back(p);
 		}
 	}
-	if (e == cudaSuccess && !HAS_V) {
-		// Keys only: the pipelined persistent pass.
-		const size_t smem = onesweep_pp_smem<K>();
-		e = cudaFuncSetAttribute(radix_onesweep_pp<K>,
-			cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-		const unsigned grid = (unsigned)std::min<size_t>(tiles, 2 * (size_t)ctx->sm_count);
-		K *src_k = (K *)keys, *dst_k = alt_k;
-		for (size_t q = 0; q < active.size() && e == cudaSuccess; ++q) {
-			PassArgs pa;
-			pa.hist = hist + (size_t)active[q] * kRadix;
-			pa.status = st[q & 1];
-			pa.status_next = st[(q + 1) & 1];
-			pa.tile_counter = cnt + active[q];
-			pa.dev_status = ctx->d_status;
-			pa.n = n;
-			pa.shift = active[q] * kRadixBits;
-			KernelTimer t("satradix_onesweep", s, 2.0 * (double)n * sizeof(K));
-			radix_onesweep_pp<K><<<grid, kThreads, smem, s>>>(src_k, dst_k, pa,
-				(uint32_t)tiles);
-			t.stop();
-			launches++;
-			e = cudaGetLastError();
-			std::swap(src_k, dst_k);
-		}
-		if (e == cudaSuccess && (active.size() & 1))
-			e = cudaMemcpyAsync(keys, alt_k, n * sizeof(K), cudaMemcpyDeviceToDevice, s);
-	} else if (e == cudaSuccess) {
-		size_t smem = onesweep_smem<K, V, HAS_V>();
-		auto kern = radix_onesweep<K, V, HAS_V>;
+	if (e == cudaSuccess) {
+		const size_t smem = chunked_smem<K, V, HAS_V, CT>();
+		auto kern = radix_pass_chunked<K, V, HAS_V, CT>;
 		e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
 			(int)smem);
 		K *src_k = (K *)keys, *dst_k = alt_k;
@@ -696,7 +969,8 @@ cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
 			pa.shift = active[q] * kRadixBits;
 			KernelTimer t("satradix_onesweep", s,
 				2.0 * (double)n * (sizeof(K) + (HAS_V ? sizeof(V) : 0)));
-			kern<<<(unsigned)tiles, kThreads, smem, s>>>(src_k, dst_k, src_v, dst_v, pa);
+			kern<<<chunks, CT, smem, s>>>(src_k, dst_k, src_v, dst_v, pa,
+				(uint32_t)ctiles, chunks);
 			t.stop();
 			launches++;
 			e = cudaGetLastError();
