@@ -797,7 +797,9 @@ radix_pass_chunked(const K *__restrict__ kin, K *__restrict__ kout,
 			const uint32_t to = s_part[pd] + woff;
 #pragma unroll
 			for (int i = 0; i < WPH; ++i) s_hist[(WPH * ph + i) * kRadix + pd] = to + cw[i];
-			if (ph == 0) s_tile_off[pd] = to;
+			// Output index of staged position q of digit d is q + G[d]
+			// (modulo 2^32), G[d] = global run start - tile offset.
+			if (ph == 0) s_tile_off[pd] = s_run[pd] - to;
 		}
 		__syncthreads();
 		K *sk = reinterpret_cast<K *>(s_stage);
@@ -827,8 +829,7 @@ radix_pass_chunked(const K *__restrict__ kin, K *__restrict__ kout,
 		for (int i = 0; i < KPT; ++i) {
 			const int q = i * THREADS + tid;
 			const K key = sk[q];
-			const uint32_t d = digit_of(key, shift);
-			const size_t o = (size_t)s_run[d] + q - s_tile_off[d];
+			const size_t o = (uint32_t)(s_tile_off[digit_of(key, shift)] + (uint32_t)q);
 			if (o < a.n) kout[o] = key;
 			if (HAS_V) outpos[i] = (uint32_t)o;
 		}
