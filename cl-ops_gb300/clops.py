@@ -28,6 +28,7 @@ CLO_ERROR_IMPL_NOT_FOUND, CLO_ERROR_UNKNOWN_TYPE, CLO_ERROR_LIBRARY = 5, 6, 7
 CLO_RNG_SEED_DEV_GID, CLO_RNG_SEED_HOST_MT, CLO_RNG_SEED_EXT_DEV, \
     CLO_RNG_SEED_EXT_HOST = range(4)
 CL_QUEUE_PROFILING_ENABLE = 1 << 1
+SEG_SORT_VARIANTS = 3  # CLO_SEG_SORT_VARIANTS
 CL_MEM_READ_WRITE = 1 << 0
 
 NP_OF_TYPE = {
@@ -160,6 +161,17 @@ _SIGS = {
     "clo_host_free": (None, [P]),
     "clo_gb300_launch_count": (U64, []),
     "clo_gb300_debug_scan_withhold": (None, [C.c_longlong]),
+    "clo_sort_segmented_with_device_data": (P, [P, P, P, P, SZ, PERR]),
+    "clo_sort_segmented_with_host_data": (U32, [P, P, P, SZ, P, SZ, PERR]),
+    "clo_sort_segmented_tune": (C.c_int, [P, P, P, P, SZ, C.POINTER(C.c_double), PERR]),
+    "clo_sort_segmented_get_variant": (C.c_int, [P]),
+    "clo_scan_segmented_with_device_data": (P, [P, P, P, P, P, SZ, PERR]),
+    "clo_scan_segmented_with_host_data": (U32, [P, P, P, P, SZ, P, SZ, PERR]),
+    "clo_queue_begin_capture": (U32, [P, PERR]),
+    "clo_queue_end_capture": (P, [P, PERR]),
+    "clo_graph_launch": (U32, [P, P, PERR]),
+    "clo_graph_get_num_nodes": (SZ, [P]),
+    "clo_graph_destroy": (None, [P]),
     "clo_gb300_timing_enable": (None, [C.c_int]),
     "clo_gb300_timing_reset": (None, []),
     "clo_gb300_timing_get": (C.c_int, [C.c_char_p, C.POINTER(C.c_double),
@@ -325,6 +337,27 @@ class Sorter:
         call(lib.clo_sort_kv_with_host_data, self.h, q.h if q else None,
              np_ptr(keys), np_ptr(vals), value_type, keys.size)
 
+    def sort_segmented_device(self, q, buf, off_buf, nseg):
+        return call(lib.clo_sort_segmented_with_device_data, self.h, q.h, buf.h,
+                    off_buf.h if off_buf else None, nseg)
+
+    def sort_segmented_host(self, q, a, offsets):
+        a = np.ascontiguousarray(a)
+        off = np.ascontiguousarray(offsets, dtype=np.uint64)
+        call(lib.clo_sort_segmented_with_host_data, self.h, q.h if q else None,
+             np_ptr(a), a.size, np_ptr(off), off.size - 1)
+        return a
+
+    def tune_segmented(self, q, buf, off_buf, nseg):
+        """(chosen variant, per-variant ms)."""
+        times = (C.c_double * SEG_SORT_VARIANTS)()
+        v = call(lib.clo_sort_segmented_tune, self.h, q.h, buf.h, off_buf.h, nseg, times)
+        return v, list(times)
+
+    @property
+    def seg_variant(self):
+        return lib.clo_sort_segmented_get_variant(self.h)
+
     def destroy(self):
         if self.h:
             lib.clo_sort_destroy(self.h)
@@ -346,9 +379,47 @@ class Scanner:
              np_ptr(a), np_ptr(out), a.size, lws_max)
         return out
 
+    def scan_segmented_device(self, q, buf_in, buf_out, off_buf, nseg):
+        return call(lib.clo_scan_segmented_with_device_data, self.h, q.h, buf_in.h,
+                    buf_out.h, off_buf.h if off_buf else None, nseg)
+
+    def scan_segmented_host(self, q, a, out, offsets):
+        off = np.ascontiguousarray(offsets, dtype=np.uint64)
+        call(lib.clo_scan_segmented_with_host_data, self.h, q.h if q else None,
+             np_ptr(a), np_ptr(out), a.size, np_ptr(off), off.size - 1)
+        return out
+
     def destroy(self):
         if self.h:
             lib.clo_scan_destroy(self.h)
+            self.h = None
+
+
+class Graph:
+    """Work enqueued on a queue between begin() and end(), replayed by
+    launch()."""
+
+    def __init__(self, q):
+        self.q = q
+        self.h = None
+
+    def begin(self):
+        call(lib.clo_queue_begin_capture, self.q.h)
+
+    def end(self):
+        self.h = call(lib.clo_queue_end_capture, self.q.h)
+        return self
+
+    def launch(self, q=None):
+        call(lib.clo_graph_launch, self.h, (q or self.q).h)
+
+    @property
+    def num_nodes(self):
+        return int(lib.clo_graph_get_num_nodes(self.h))
+
+    def destroy(self):
+        if self.h:
+            lib.clo_graph_destroy(self.h)
             self.h = None
 
 

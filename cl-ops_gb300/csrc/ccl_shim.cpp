@@ -163,6 +163,14 @@ bool check_device_status(CCLContext *ctx, GError **err) {
 	if (!cuda_ok(cudaMemcpy(st, ctx->d_status, 2 * sizeof(int),
 			cudaMemcpyDeviceToHost), err, "status readback"))
 		return false;
+	if (st[0] == DEV_ERR_BAD_SEGMENTS) {
+		cudaMemset(ctx->d_status, 0, 2 * sizeof(int));
+		set_error(err, CLO_ERROR_ARGS,
+			"Segment offsets are invalid (segment %d: offsets must not decrease "
+			"and must stay within the buffer, segments shorter than 2^30); "
+			"results of the operation are invalid", st[1]);
+		return false;
+	}
 	if (st[0] != DEV_OK) {
 		cudaMemset(ctx->d_status, 0, 2 * sizeof(int));
 		set_error(err, CLO_ERROR_LIBRARY,
@@ -561,6 +569,65 @@ void *clo_host_alloc(size_t size, GError **err) {
 
 void clo_host_free(void *ptr) {
 	if (ptr) cudaFreeHost(ptr);
+}
+
+// ------------------------------------------------------------ CUDA graphs
+cl_bool clo_queue_begin_capture(CCLQueue *cq, GError **err) {
+	if (!cq) {
+		set_error(err, CLO_ERROR_ARGS, "NULL queue");
+		return CL_FALSE;
+	}
+	cudaSetDevice(cq->ctx->ordinal);
+	return cuda_ok(cudaStreamBeginCapture(cq->stream, cudaStreamCaptureModeThreadLocal),
+		err, "cudaStreamBeginCapture") ? CL_TRUE : CL_FALSE;
+}
+
+CloGraph *clo_queue_end_capture(CCLQueue *cq, GError **err) {
+	if (!cq) {
+		set_error(err, CLO_ERROR_ARGS, "NULL queue");
+		return nullptr;
+	}
+	cudaSetDevice(cq->ctx->ordinal);
+	cudaGraph_t g = nullptr;
+	if (!cuda_ok(cudaStreamEndCapture(cq->stream, &g), err, "cudaStreamEndCapture"))
+		return nullptr;
+	cudaGraphExec_t x = nullptr;
+	if (!cuda_ok(cudaGraphInstantiate(&x, g, 0), err, "cudaGraphInstantiate")) {
+		cudaGraphDestroy(g);
+		return nullptr;
+	}
+	CloGraph *r = new CloGraph();
+	r->graph = g;
+	r->exec = x;
+	r->ctx = cq->ctx;
+	ccl_context_ref(cq->ctx);
+	size_t nodes = 0;
+	cudaGraphGetNodes(g, nullptr, &nodes);
+	r->nodes = nodes;
+	clo::wrapper_created();
+	return r;
+}
+
+cl_bool clo_graph_launch(CloGraph *g, CCLQueue *cq, GError **err) {
+	if (!g || !cq) {
+		set_error(err, CLO_ERROR_ARGS, "NULL graph or queue");
+		return CL_FALSE;
+	}
+	cudaSetDevice(cq->ctx->ordinal);
+	return cuda_ok(cudaGraphLaunch(g->exec, cq->stream), err, "cudaGraphLaunch")
+		? CL_TRUE : CL_FALSE;
+}
+
+size_t clo_graph_get_num_nodes(CloGraph *g) { return g ? g->nodes : 0; }
+
+void clo_graph_destroy(CloGraph *g) {
+	if (!g) return;
+	cudaSetDevice(g->ctx->ordinal);
+	cudaGraphExecDestroy(g->exec);
+	cudaGraphDestroy(g->graph);
+	ccl_context_unref(g->ctx);
+	delete g;
+	clo::wrapper_destroyed();
 }
 
 }  // extern "C"

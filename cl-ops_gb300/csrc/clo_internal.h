@@ -67,12 +67,20 @@ struct ccl_ewl_impl {
 	std::vector<ccl_event *> evts;
 };
 
+struct clo_graph {
+	cudaGraph_t graph;
+	cudaGraphExec_t exec;
+	CCLContext *ctx;
+	size_t nodes;
+};
+
 namespace clo {
 
 // Device-side error codes reported through ccl_context::d_status.
 enum DevError : int {
 	DEV_OK = 0,
 	DEV_ERR_LOOKBACK_TIMEOUT = 1,  // decoupled-lookback wait hit its cap
+	DEV_ERR_BAD_SEGMENTS = 2,      // segment offsets decrease or pass the buffer
 };
 
 // Error helpers (GError semantics: *err must be NULL on entry; err may be
@@ -137,6 +145,25 @@ cudaError_t bitonic_sort(void *data, size_t n, CloType type,
 cudaError_t gselect_sort(const void *in, void *out, size_t n, CloType type,
 	const void *vals_in, void *vals_out, int val_bytes, CCLContext *ctx,
 	cudaStream_t s, GError **err);
+
+// Segmented sort ("satradix" order within each segment [off[i], off[i+1])
+// of keys; off is a device array of S + 1 non-decreasing offsets within
+// n_cap elements), in a fixed launch sequence with no host readback.
+// variant selects the CTA class layout (0 .. seg_sort_num_variants()-1).
+int seg_sort_num_variants();
+cudaError_t seg_sort(void *keys, uint64_t n_cap, const uint64_t *off, size_t S,
+	int key_bytes, int sort_bits, int variant, CCLContext *ctx, cudaStream_t s,
+	GError **err);
+
+// Segmented exclusive scan: within each segment, out as the scan of that
+// segment alone; elements outside [off[0], off[S]) are not written.
+cudaError_t seg_scan(const void *in, void *out, uint64_t n_cap, const uint64_t *off,
+	size_t S, CloType in_type, int out_bytes, CCLContext *ctx, cudaStream_t s,
+	GError **err);
+
+// Host check of segment offsets (non-decreasing, within numel, segments
+// shorter than 2^30): CLO_ERROR_ARGS otherwise.
+bool check_offsets(const uint64_t *off, size_t S, size_t numel, GError **err);
 
 // Generator ids (index into clo_rng_infos).
 enum RngGen : int {

@@ -139,6 +139,25 @@ long live_wrappers() { return g_live_wrappers.load(); }
 static std::atomic<unsigned long long> g_launches{0};
 void count_launches(unsigned n) { g_launches.fetch_add(n); }
 
+bool check_offsets(const uint64_t *off, size_t S, size_t numel, GError **err) {
+	if (S > 0 && off == nullptr) {
+		set_error(err, CLO_ERROR_ARGS, "NULL segment offsets");
+		return false;
+	}
+	for (size_t i = 0; i < S; ++i) {
+		if (off[i] > off[i + 1] || off[i + 1] > numel ||
+			off[i + 1] - off[i] >= (1ull << 30)) {
+			set_error(err, CLO_ERROR_ARGS,
+				"Segment %zu [%llu, %llu) is invalid: offsets must not decrease, "
+				"must stay within %zu elements, and segments must be shorter "
+				"than 2^30", i, (unsigned long long)off[i],
+				(unsigned long long)off[i + 1], numel);
+			return false;
+		}
+	}
+	return true;
+}
+
 bool type_is_integer(CloType t) { return t >= CLO_CHAR && t <= CLO_ULONG; }
 bool type_is_signed(CloType t) {
 	return t == CLO_CHAR || t == CLO_SHORT || t == CLO_INT || t == CLO_LONG;

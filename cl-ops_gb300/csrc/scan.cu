@@ -24,6 +24,7 @@
 
 #include "clo_internal.h"
 #include "dev_common.cuh"
+#include "scan_status.cuh"
 #include "timing.h"
 
 namespace clo {
@@ -38,69 +39,15 @@ constexpr int kPadded = kWarpElems + kWarpElems / 32;
 
 __device__ __forceinline__ int pidx(int i) { return i + (i >> 5); }
 
-// Tile status without fences: every value is published once into its own
-// slot of 64-bit words, each word carrying a ready bit (bit 0) and 32
-// payload bits (bits 32..63). A word is either still zero or final, so a
-// reader that sees every word of a slot ready has the whole value. Per
-// tile: [aggregate slot][inclusive-prefix slot].
-template <typename Acc>
-struct Slots {
-	static constexpr int kWords = sizeof(Acc) / 4;
-	static constexpr int kPerTile = 2 * kWords;
-};
-
-template <typename Acc>
-__device__ __forceinline__ void publish(uint64_t *w, Acc v) {
-#pragma unroll
-	for (int i = 0; i < Slots<Acc>::kWords; ++i)
-		dev::st_relaxed_u64(w + i, ((uint64_t)(uint32_t)((uint64_t)v >> (32 * i)) << 32) | 1ull);
-}
-
-// 0 = nothing published, 1 = aggregate, 2 = inclusive prefix.
-template <typename Acc>
-__device__ __forceinline__ uint32_t read_status(const uint64_t *tile_words, Acc &v) {
-	constexpr int W = Slots<Acc>::kWords;
-	uint64_t a[W], p[W];
-#pragma unroll
-	for (int i = 0; i < W; ++i) {
-		a[i] = dev::ld_relaxed_u64(tile_words + i);
-		p[i] = dev::ld_relaxed_u64(tile_words + W + i);
-	}
-	bool pr = true, ar = true;
-	uint64_t pv = 0, av = 0;
-#pragma unroll
-	for (int i = 0; i < W; ++i) {
-		pr = pr && (p[i] & 1ull);
-		ar = ar && (a[i] & 1ull);
-		pv |= (p[i] >> 32) << (32 * i);
-		av |= (a[i] >> 32) << (32 * i);
-	}
-	if (pr) {
-		v = (Acc)pv;
-		return 2;
-	}
-	if (ar) {
-		v = (Acc)av;
-		return 1;
-	}
-	return 0;
-}
-
-struct TileStatus {
-	uint64_t *words;     // tiles * Slots<Acc>::kPerTile
-	uint32_t *counter;   // dynamic tile ids
-};
+using lb::Slots;
+using lb::TileStatus;
+using lb::publish;
+using lb::read_status;
+using lb::warp_sum;
 
 template <typename Acc>
 __device__ __forceinline__ Acc shfl_up(Acc v, int d) {
 	return __shfl_up_sync(0xffffffffu, v, d);
-}
-
-template <typename Acc>
-__device__ __forceinline__ Acc warp_sum(Acc v) {
-#pragma unroll
-	for (int d = 16; d >= 1; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
-	return v;
 }
 
 template <typename InT, typename OutT>
@@ -182,46 +129,7 @@ scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, size_t n,
 			if (lane == 0 && do_publish) publish<Acc>(ts.words + Slots<Acc>::kWords, aggregate);
 		} else {
 			if (lane == 0 && do_publish) publish<Acc>(ts.words + (size_t)tile * PT, aggregate);
-			// Window of 64 predecessors per round trip: lane l covers tiles
-			// pred - l and pred - 32 - l.
-			long long pred = (long long)tile - 1;
-			for (;;) {
-				const long long t0 = pred - lane, t1 = pred - 32 - lane;
-				Acc v0 = 0, v1 = 0;
-				uint32_t s0 = t0 >= 0 ? read_status<Acc>(ts.words + (size_t)t0 * PT, v0) : 2u;
-				uint32_t s1 = t1 >= 0 ? read_status<Acc>(ts.words + (size_t)t1 * PT, v1) : 2u;
-				uint32_t iter = 0;
-				while (__any_sync(0xffffffffu, s0 == 0 || s1 == 0)) {
-					if (iter >= dev::kSpinLimit) {
-						// Give up: record the failure and treat the missing
-						// predecessors as zero prefixes so the kernel ends.
-						if (s0 == 0 || s1 == 0)
-							dev::report_timeout(dev_status, DEV_ERR_LOOKBACK_TIMEOUT, (int)tile);
-						if (s0 == 0) { s0 = 2; v0 = 0; }
-						if (s1 == 0) { s1 = 2; v1 = 0; }
-						continue;
-					}
-					dev::backoff(iter);
-					if (s0 == 0) s0 = read_status<Acc>(ts.words + (size_t)t0 * PT, v0);
-					if (s1 == 0) s1 = read_status<Acc>(ts.words + (size_t)t1 * PT, v1);
-					++iter;
-				}
-				uint32_t pm = __ballot_sync(0xffffffffu, s0 == 2);
-				if (pm) {
-					const int first = __ffs(pm) - 1;
-					excl += warp_sum<Acc>(lane <= first ? v0 : (Acc)0);
-					break;
-				}
-				excl += warp_sum<Acc>(v0);
-				pm = __ballot_sync(0xffffffffu, s1 == 2);
-				if (pm) {
-					const int first = __ffs(pm) - 1;
-					excl += warp_sum<Acc>(lane <= first ? v1 : (Acc)0);
-					break;
-				}
-				excl += warp_sum<Acc>(v1);
-				pred -= 64;
-			}
+			excl = lb::lookback_warp<Acc>(ts.words, tile, dev_status);
 			if (lane == 0 && do_publish)
 				publish<Acc>(ts.words + (size_t)tile * PT + Slots<Acc>::kWords, excl + aggregate);
 		}

@@ -247,3 +247,102 @@ size_t clo_scan_get_localmem_usage(CloScan *s, cl_uint i, size_t lws_max,
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------- segmented scan
+extern "C" {
+
+CCLEvent *clo_scan_segmented_with_device_data(CloScan *scanner, CCLQueue *q,
+	CCLBuffer *data_in, CCLBuffer *data_out, CCLBuffer *offsets,
+	size_t num_segments, GError **err) {
+	if (!scanner || !q || (err && *err)) {
+		fprintf(stderr, "cl_ops: clo_scan_segmented_with_device_data: bad arguments\n");
+		return nullptr;
+	}
+	if (strcmp(scanner->impl_def.name, "blelloch") != 0) {
+		set_error(err, CLO_ERROR_ARGS, "Segmented scan: unknown scanner '%s'",
+			scanner->impl_def.name);
+		return nullptr;
+	}
+	cudaSetDevice(scanner->ctx->ordinal);
+	const size_t ib = clo_type_sizeof(scanner->elem_type);
+	const size_t ob = clo_type_sizeof(scanner->sum_type);
+	if (!data_in || !data_out ||
+		(num_segments > 0 && (!offsets || offsets->size < (num_segments + 1) * 8))) {
+		set_error(err, CLO_ERROR_ARGS,
+			"Segmented scan needs input and output buffers and %zu offsets",
+			num_segments + 1);
+		return nullptr;
+	}
+	const size_t n_in = data_in->size / ib, n_out = data_out->size / ob;
+	ccl_event *ev = clo::event_begin(q, "clo_scan_blelloch_segmented");
+	if (clo::seg_scan(data_in->ptr, data_out->ptr, n_in < n_out ? n_in : n_out,
+			num_segments ? (const uint64_t *)offsets->ptr : nullptr, num_segments,
+			scanner->elem_type, (int)ob, scanner->ctx, q->stream, err) != cudaSuccess)
+		return nullptr;
+	clo::event_end(ev);
+	return ev;
+}
+
+cl_bool clo_scan_segmented_with_host_data(CloScan *scanner, CCLQueue *q,
+	const void *data_in, void *data_out, size_t numel, const cl_ulong *offsets,
+	size_t num_segments, GError **err) {
+	if (!scanner || (err && *err)) return CL_FALSE;
+	CCLContext *ctx = scanner->ctx;
+	cudaSetDevice(ctx->ordinal);
+	if (!clo::check_offsets((const uint64_t *)offsets, num_segments, numel, err))
+		return CL_FALSE;
+	GError *e2 = nullptr;
+	CCLQueue *own = nullptr;
+	if (!q) {
+		own = ccl_queue_new(ctx, &ctx->device, 0, &e2);
+		if (!own) {
+			clo::propagate_error(err, e2);
+			return CL_FALSE;
+		}
+		q = own;
+	}
+	const size_t ib = numel * clo_type_sizeof(scanner->elem_type);
+	const size_t ob = numel * clo_type_sizeof(scanner->sum_type);
+	const size_t obytes = (num_segments + 1) * 8;
+	cl_bool status = CL_FALSE;
+	CCLBuffer *din = nullptr, *dout = nullptr, *doff = nullptr;
+	CCLEventWaitList ewl = nullptr;
+	CCLEvent *evt = nullptr;
+	void *pin = clo::tmp_alloc(ctx, ib, q->stream, &e2);
+	void *pout = pin ? clo::tmp_alloc(ctx, ob, q->stream, &e2) : nullptr;
+	void *po = pout ? clo::tmp_alloc(ctx, obytes, q->stream, &e2) : nullptr;
+	if (!pin || !pout || !po) goto done;
+	din = ccl_buffer_new_wrap(ctx, pin, ib, &e2);
+	dout = ccl_buffer_new_wrap(ctx, pout, ob, &e2);
+	doff = ccl_buffer_new_wrap(ctx, po, obytes, &e2);
+	if (!ccl_buffer_enqueue_write(din, q, CL_FALSE, 0, ib, data_in, nullptr, &e2))
+		goto done;
+	// Elements outside the segments keep what data_out held.
+	if (!ccl_buffer_enqueue_write(dout, q, CL_FALSE, 0, ob, data_out, nullptr, &e2))
+		goto done;
+	if (num_segments > 0 &&
+		!ccl_buffer_enqueue_write(doff, q, CL_FALSE, 0, obytes, offsets, nullptr, &e2))
+		goto done;
+	if (!clo_scan_segmented_with_device_data(scanner, q, din, dout, doff, num_segments,
+			&e2))
+		goto done;
+	evt = ccl_buffer_enqueue_read(dout, q, CL_FALSE, 0, ob, data_out, nullptr, &e2);
+	if (!evt) goto done;
+	ccl_ewl(&ewl, evt, (CCLEvent *)nullptr);
+	if (!ccl_event_wait(&ewl, &e2)) goto done;
+	status = CL_TRUE;
+done:
+	ccl_event_wait_list_clear(&ewl);
+	if (din) ccl_buffer_destroy(din);
+	if (dout) ccl_buffer_destroy(dout);
+	if (doff) ccl_buffer_destroy(doff);
+	clo::tmp_free(pin, q->stream);
+	clo::tmp_free(pout, q->stream);
+	clo::tmp_free(po, q->stream);
+	if (!status) cudaStreamSynchronize(q->stream);
+	if (own) ccl_queue_destroy(own);
+	clo::propagate_error(err, e2);
+	return status;
+}
+
+}  // extern "C"

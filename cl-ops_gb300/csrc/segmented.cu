@@ -1,0 +1,1107 @@
+// Segmented sort and segmented scan: many independent segments of one
+// buffer, each handled exactly as a separate clo_sort / clo_scan call on it
+// would handle it, in a fixed sequence of launches whatever the number and
+// the sizes of the segments (no host readback, so the sequence can be
+// captured into a CUDA graph).
+//
+// Segments are given by a device array of S + 1 non-decreasing 64-bit
+// offsets; segment i is [off[i], off[i+1]).
+//
+// Sort ("satradix" order: stable, ascending by the low sort_bits bits of
+// the unsigned element pattern), by segment length:
+//   len <= 32           one warp per segment: a 32-lane bitonic network on
+//                       (key, index) pairs, which makes it stable;
+//   len <= tile A       one CTA per segment (class A tile, e.g. 128 x 8),
+//   len <= tile B       one CTA per segment (class B tile, e.g. 512 x 16):
+//                       an LSD radix sort in shared memory, 8-bit digits,
+//                       stable warp-multisplit ranking, digits that are
+//                       constant over the segment skipped;
+//   longer              the onesweep pass of the full sort, with tiles that
+//                       never straddle segments, per-segment digit
+//                       histograms and a decoupled lookback that stops at
+//                       the segment's first tile.
+// A classification kernel builds one list per class (and the tile counts
+// of the long segments, scanned into tile starts) on the device.
+//
+// Scan ("blelloch" semantics per segment): one decoupled-lookback launch
+// over the whole buffer with a bitmap of segment heads; sums restart at
+// every head, a tile holding a head publishes its inclusive prefix at once.
+#include <algorithm>
+#include <mutex>
+#include <type_traits>
+
+#include "clo_internal.h"
+#include "dev_common.cuh"
+#include "scan_status.cuh"
+#include "timing.h"
+
+namespace clo {
+namespace {
+
+constexpr int kRadix = 256;
+constexpr int kRadixBits = 8;
+constexpr uint32_t kMaxSegLen = (1u << 30) - 1u;
+
+// Large-segment pass: 512 threads, 16 (8 for 64-bit keys) keys per thread.
+constexpr int kLThreads = 512;
+constexpr int kLWarps = kLThreads / 32;
+template <typename K>
+struct LCfg {
+	static constexpr int kKpt = sizeof(K) <= 4 ? 16 : 8;
+	static constexpr int kTile = kLThreads * kKpt;
+};
+
+// Tile status word of the large-segment pass: 2-bit flag | 30-bit count.
+constexpr uint32_t kStAgg = 1u << 30;
+constexpr uint32_t kStPrefix = 2u << 30;
+constexpr uint32_t kStValue = (1u << 30) - 1u;
+
+template <typename K>
+__device__ __forceinline__ uint32_t digit_of(K k, int shift) {
+	return (uint32_t)(k >> shift) & (kRadix - 1);
+}
+
+__device__ __forceinline__ void report_bad_segment(int *st, uint32_t s) {
+	if (atomicCAS(st, 0, DEV_ERR_BAD_SEGMENTS) == 0) atomicExch(st + 1, (int)s);
+}
+
+// Length of segment s, or 0 (and an error report) when its offsets are
+// invalid: decreasing, past the buffer, or 2^30 elements or more.
+__device__ __forceinline__ uint64_t checked_len(const uint64_t *off, uint32_t s,
+	uint64_t n_cap, int *st) {
+	const uint64_t a = off[s], b = off[s + 1];
+	if (a > b || b > n_cap || b - a > kMaxSegLen) {
+		report_bad_segment(st, s);
+		return 0;
+	}
+	return b - a;
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl_xor_any(T v, int m) {
+	if (sizeof(T) == 8)
+		return (T)__shfl_xor_sync(0xffffffffu, (unsigned long long)v, m);
+	return (T)__shfl_xor_sync(0xffffffffu, (uint32_t)v, m);
+}
+
+// ------------------------------------------------------ classification
+// Class lists: [0] warp, [1] CTA A, [2] CTA B, [3] large; counts[0..3].
+// tinfo[s] = (tiles of s << 32) | 1 for a large segment, else 0;
+// tinfo[S] = 0 (its exclusive scan gives the tile starts and the large
+// ranks, and in entry S the totals).
+struct ClassArgs {
+	const uint64_t *off;
+	uint32_t S;
+	uint64_t n_cap;
+	uint32_t max_warp, max_a, max_b, large_tile;
+	uint32_t *lists;
+	uint32_t *counts;
+	uint64_t *tinfo;
+	int *dev_status;
+};
+
+__global__ void __launch_bounds__(256) seg_classify(ClassArgs a) {
+	const uint32_t lane = threadIdx.x & 31u;
+	const uint32_t lt = dev::lanemask_lt();
+	const uint64_t warp_id = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+	const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+	for (uint64_t w = warp_id; w * 32 <= (uint64_t)a.S; w += nwarps) {
+		const uint64_t s = w * 32 + lane;
+		int cls = -1;
+		uint64_t packed = 0;
+		if (s < a.S) {
+			const uint64_t len = checked_len(a.off, (uint32_t)s, a.n_cap, a.dev_status);
+			if (len >= 2) {
+				if (len <= a.max_warp) cls = 0;
+				else if (len <= a.max_a) cls = 1;
+				else if (len <= a.max_b) cls = 2;
+				else {
+					cls = 3;
+					packed = (((len + a.large_tile - 1) / a.large_tile) << 32) | 1ull;
+				}
+			}
+		}
+		if (s <= a.S) a.tinfo[s] = packed;
+#pragma unroll
+		for (int c = 0; c < 4; ++c) {
+			const uint32_t m = __ballot_sync(0xffffffffu, cls == c);
+			if (m) {
+				const int leader = __ffs(m) - 1;
+				uint32_t base = 0;
+				if ((int)lane == leader) base = atomicAdd(a.counts + c, (uint32_t)__popc(m));
+				base = __shfl_sync(0xffffffffu, base, leader);
+				if (cls == c) a.lists[(size_t)c * a.S + base + __popc(m & lt)] = (uint32_t)s;
+			}
+		}
+	}
+}
+
+// --------------------------------------------------------- warp class
+template <typename K>
+__global__ void __launch_bounds__(256) seg_sort_warp(K *keys, const uint64_t *off,
+	const uint32_t *list, const uint32_t *count, K mask) {
+	const uint32_t lane = threadIdx.x & 31u;
+	const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+	const uint32_t cnt = *count;
+	for (uint32_t i = gw; i < cnt; i += nw) {
+		const uint32_t s = list[i];
+		const uint64_t base = off[s];
+		const uint32_t len = (uint32_t)(off[s + 1] - base);
+		K v = lane < len ? keys[base + lane] : (K)~(K)0;
+		K key = v & mask;
+		uint32_t idx = lane;
+		// Ascending bitonic network over (key, original lane): ties keep
+		// their input order, so the result is the stable order.
+#pragma unroll
+		for (uint32_t size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+			for (uint32_t j = size >> 1; j > 0; j >>= 1) {
+				const K ov = shfl_xor_any(v, (int)j);
+				const uint32_t oi = __shfl_xor_sync(0xffffffffu, idx, (int)j);
+				const K okey = ov & mask;
+				const bool up = (lane & size) == 0;
+				const bool lower = (lane & j) == 0;
+				const bool other_less = okey < key || (okey == key && oi < idx);
+				if ((lower == up) == other_less) {
+					v = ov;
+					key = okey;
+					idx = oi;
+				}
+			}
+		}
+		if (lane < len) keys[base + lane] = v;
+	}
+}
+
+// ---------------------------------------------------------- CTA classes
+template <typename K, int THREADS, int KPT>
+struct CtaCfg {
+	static constexpr int kWarps = THREADS / 32;
+	static constexpr int kTile = THREADS * KPT;
+	static constexpr int kDigitsPerThread = THREADS >= kRadix ? 1 : kRadix / THREADS;
+	static constexpr int kDigitThreads = kRadix / kDigitsPerThread;
+	static size_t smem() {
+		return (2 * (size_t)kWarps * kRadix + 64) * sizeof(uint32_t) +
+			(size_t)kTile * sizeof(K);
+	}
+};
+
+// One CTA per segment of the list: keys stay in registers (warp-striped,
+// so index order is (warp, round, lane)); per 8-bit digit, per-warp counts,
+// a block scan of the digit totals, stable ranks through shared-memory OR
+// peer masks, and a pass through shared memory back to index order.
+// Elements past the segment end are all-ones keys: they rank last in every
+// digit, so they stay behind the segment and are never written.
+template <typename K, int THREADS, int KPT>
+__global__ void __launch_bounds__(THREADS) seg_sort_cta(K *keys, const uint64_t *off,
+	const uint32_t *list, const uint32_t *count, int passes) {
+	using Cfg = CtaCfg<K, THREADS, KPT>;
+	constexpr int W = Cfg::kWarps;
+	constexpr int TILE = Cfg::kTile;
+	constexpr int DPT = Cfg::kDigitsPerThread;
+	constexpr int DT = Cfg::kDigitThreads;
+	extern __shared__ __align__(16) unsigned char smem[];
+	uint32_t *s_hist = reinterpret_cast<uint32_t *>(smem);  // [W][256]
+	uint32_t *s_match = s_hist + W * kRadix;                // [W][256]
+	uint32_t *s_misc = s_match + W * kRadix;                // [64]
+	K *sk = reinterpret_cast<K *>(s_misc + 64);             // [TILE]
+
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	uint32_t *my_hist = s_hist + warp * kRadix;
+	uint32_t *my_match = s_match + warp * kRadix;
+	const uint32_t lt = dev::lanemask_lt();
+	for (int i = lane; i < kRadix; i += 32) my_match[i] = 0;
+	const uint32_t cnt = *count;
+	const uint32_t wb = (uint32_t)warp * (KPT * 32);
+
+	for (uint32_t li = blockIdx.x; li < cnt; li += gridDim.x) {
+		const uint32_t s = list[li];
+		const uint64_t base = off[s];
+		const uint32_t len = (uint32_t)(off[s + 1] - base);
+		K k[KPT];
+#pragma unroll
+		for (int j = 0; j < KPT; ++j) {
+			const uint32_t idx = wb + j * 32 + lane;
+			k[j] = idx < len ? keys[base + idx] : (K)~(K)0;
+		}
+		for (int p = 0; p < passes; ++p) {
+			const int shift = p * kRadixBits;
+			for (int i = lane; i < kRadix; i += 32) my_hist[i] = 0;
+			__syncwarp();
+#pragma unroll
+			for (int j = 0; j < KPT; ++j) atomicAdd(my_hist + digit_of(k[j], shift), 1u);
+			__syncthreads();
+			// Digit totals (DPT consecutive digits per thread), the scan of
+			// the threads' sums within each warp, and whether one digit holds
+			// every key (then this digit leaves the order unchanged).
+			uint32_t tot[DPT];
+			uint32_t tsum = 0, tinc = 0;
+			bool triv = false;
+			if (tid < DT) {
+#pragma unroll
+				for (int q = 0; q < DPT; ++q) {
+					const int d = tid * DPT + q;
+					uint32_t c = 0;
+#pragma unroll
+					for (int w = 0; w < W; ++w) c += s_hist[w * kRadix + d];
+					tot[q] = c;
+					tsum += c;
+					triv = triv || c == (d == kRadix - 1 ? (uint32_t)TILE : len);
+				}
+				tinc = tsum;
+#pragma unroll
+				for (int d = 1; d < 32; d <<= 1) {
+					const uint32_t t = __shfl_up_sync(0xffffffffu, tinc, d);
+					if (lane >= d) tinc += t;
+				}
+				if (lane == 31) s_misc[warp] = tinc;
+			}
+			if (__syncthreads_or(triv)) continue;
+			if (tid < DT) {
+				uint32_t run = tinc - tsum;
+				for (int w = 0; w < warp; ++w) run += s_misc[w];
+#pragma unroll
+				for (int q = 0; q < DPT; ++q) {
+					const int d = tid * DPT + q;
+					uint32_t r = run;
+#pragma unroll
+					for (int w = 0; w < W; ++w) {
+						const uint32_t c = s_hist[w * kRadix + d];
+						s_hist[w * kRadix + d] = r;
+						r += c;
+					}
+					run += tot[q];
+				}
+			}
+			__syncthreads();
+#pragma unroll
+			for (int j = 0; j < KPT; ++j) {
+				const uint32_t d = digit_of(k[j], shift);
+				atomicOr(my_match + d, 1u << lane);
+				__syncwarp();
+				const uint32_t peers = my_match[d];
+				const uint32_t start = my_hist[d];
+				__syncwarp();
+				const uint32_t below = __popc(peers & lt);
+				if (below == 0) {
+					my_hist[d] = start + __popc(peers);
+					my_match[d] = 0;
+				}
+				__syncwarp();
+				sk[start + below] = k[j];
+			}
+			__syncthreads();
+#pragma unroll
+			for (int j = 0; j < KPT; ++j) k[j] = sk[wb + j * 32 + lane];
+		}
+#pragma unroll
+		for (int j = 0; j < KPT; ++j) {
+			const uint32_t idx = wb + j * 32 + lane;
+			if (idx < len) keys[base + idx] = k[j];
+		}
+		__syncthreads();
+	}
+}
+
+// ------------------------------------------------------ large segments
+// Tile -> segment map, and clearing of what the passes accumulate into:
+// the segment's digit histograms and the first pass's tile statuses.
+template <int TILE>
+__global__ void __launch_bounds__(256) seg_tiles(const uint64_t *off,
+	const uint64_t *tstart, const uint32_t *list, const uint32_t *count,
+	uint32_t *tile_seg, uint32_t *seg_hist, int passes, uint32_t *status0) {
+	const uint32_t lane = threadIdx.x & 31u;
+	const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+	const uint32_t cnt = *count;
+	for (uint32_t i = gw; i < cnt; i += nw) {
+		const uint32_t s = list[i];
+		const uint64_t ts = tstart[s];
+		const uint32_t first = (uint32_t)(ts >> 32), lr = (uint32_t)ts;
+		const uint64_t len = off[s + 1] - off[s];
+		const uint32_t ntiles = (uint32_t)((len + TILE - 1) / TILE);
+		for (uint32_t t = lane; t < ntiles; t += 32) tile_seg[first + t] = s;
+		uint4 *h = reinterpret_cast<uint4 *>(seg_hist + (size_t)lr * passes * kRadix);
+		for (uint32_t q = lane; q < (uint32_t)passes * (kRadix / 4); q += 32)
+			h[q] = make_uint4(0, 0, 0, 0);
+		uint4 *st = reinterpret_cast<uint4 *>(status0 + (size_t)first * kRadix);
+		for (uint32_t q = lane; q < ntiles * (kRadix / 4); q += 32)
+			st[q] = make_uint4(0, 0, 0, 0);
+	}
+}
+
+// Histograms of every digit position of every large segment: one CTA per
+// tile at a time, shared-memory counts added to the segment's histograms.
+template <typename K, int PASSES>
+__global__ void __launch_bounds__(256) seg_upsweep(const K *keys, const uint64_t *off,
+	const uint64_t *tstart, const uint32_t *tile_seg, uint32_t S,
+	uint32_t *seg_hist) {
+	constexpr int TILE = LCfg<K>::kTile;
+	__shared__ uint32_t h[PASSES * kRadix];
+	__shared__ uint64_t s_a, s_e;
+	__shared__ uint32_t s_lr;
+	const uint32_t T = (uint32_t)(tstart[S] >> 32);
+	for (uint32_t t = blockIdx.x; t < T; t += gridDim.x) {
+		for (int i = threadIdx.x; i < PASSES * kRadix; i += blockDim.x) h[i] = 0;
+		if (threadIdx.x == 0) {
+			const uint32_t s = tile_seg[t];
+			const uint64_t ts = tstart[s];
+			const uint64_t a = off[s] + (uint64_t)(t - (uint32_t)(ts >> 32)) * TILE;
+			const uint64_t e = off[s + 1];
+			s_a = a;
+			s_e = a + TILE < e ? a + TILE : e;
+			s_lr = (uint32_t)ts;
+		}
+		__syncthreads();
+		const uint64_t a = s_a, e = s_e;
+		for (uint64_t i = a + threadIdx.x; i < e; i += blockDim.x) {
+			const K key = keys[i];
+#pragma unroll
+			for (int p = 0; p < PASSES; ++p)
+				atomicAdd(&h[p * kRadix + digit_of(key, p * kRadixBits)], 1u);
+		}
+		__syncthreads();
+		uint32_t *dst = seg_hist + (size_t)s_lr * PASSES * kRadix;
+		for (int i = threadIdx.x; i < PASSES * kRadix; i += blockDim.x)
+			if (h[i]) atomicAdd(dst + i, h[i]);
+		__syncthreads();
+	}
+}
+
+struct SegPassArgs {
+	const uint64_t *off;
+	const uint64_t *tstart;
+	const uint32_t *tile_seg;
+	const uint32_t *seg_hist;  // + pass * 256; stride passes * 256 per segment
+	uint32_t hist_stride;
+	uint32_t *status;
+	uint32_t *status_next;
+	uint32_t *counter;
+	int *dev_status;
+	uint32_t S;
+	int shift;
+};
+
+// Reads tiles base, base-1, ... (W of them, one round trip) for one digit
+// and adds them to `excl` up to the first inclusive prefix.
+template <int W>
+__device__ __forceinline__ bool seg_lookback_window(const uint32_t *status, int digit,
+	long long &base, uint32_t &excl) {
+	uint32_t sv[W];
+#pragma unroll
+	for (int i = 0; i < W; ++i) {
+		const long long j = base - i;
+		sv[i] = j >= 0 ? dev::ld_relaxed_u32(status + (size_t)j * kRadix + digit) : kStPrefix;
+	}
+	int consumed = W;
+	bool done = false;
+#pragma unroll
+	for (int i = 0; i < W; ++i) {
+		if (!done && consumed == W) {
+			if ((sv[i] & ~kStValue) == 0) {
+				consumed = i;
+			} else {
+				excl += sv[i] & kStValue;
+				if (sv[i] & kStPrefix) done = true;
+			}
+		}
+	}
+	if (!done) base -= consumed;
+	return done;
+}
+
+// One pass over all tiles of all large segments, by persistent CTAs that
+// take tiles in order from a counter. A segment's first tile publishes an
+// inclusive prefix at once, so lookbacks never cross segments.
+template <typename K>
+__global__ void __launch_bounds__(kLThreads, 2)
+seg_pass(const K *__restrict__ kin, K *__restrict__ kout, SegPassArgs a) {
+	constexpr int KPT = LCfg<K>::kKpt;
+	constexpr int TILE = LCfg<K>::kTile;
+	extern __shared__ __align__(16) unsigned char smem[];
+	uint32_t *s_hist = reinterpret_cast<uint32_t *>(smem);   // [16][256]
+	uint32_t *s_match = s_hist + kLWarps * kRadix;           // [16][256]
+	uint32_t *s_tile_off = s_match + kLWarps * kRadix;       // [256]
+	uint32_t *s_glob = s_tile_off + kRadix;                  // [256]
+	uint32_t *s_misc = s_glob + kRadix;                      // [64]
+	uint64_t *s_seg = reinterpret_cast<uint64_t *>(s_misc + 64);  // [2]
+	unsigned char *s_stage = reinterpret_cast<unsigned char *>(s_seg + 2);
+
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	uint32_t *my_hist = s_hist + warp * kRadix;
+	uint32_t *my_match = s_match + warp * kRadix;
+	const uint32_t lt = dev::lanemask_lt();
+	const int shift = a.shift;
+	for (int i = lane; i < kRadix; i += 32) my_match[i] = 0;
+	const uint32_t T = (uint32_t)(a.tstart[a.S] >> 32);
+
+	for (;;) {
+		if (tid == 0) {
+			const uint32_t t = atomicAdd(a.counter, 1u);
+			s_misc[0] = t;
+			if (t < T) {
+				const uint32_t s = a.tile_seg[t];
+				const uint64_t ts = a.tstart[s];
+				const uint32_t first = (uint32_t)(ts >> 32);
+				s_misc[1] = t - first;       // tile index within the segment
+				s_misc[2] = (uint32_t)ts;    // large-segment rank
+				s_seg[0] = a.off[s];
+				s_seg[1] = a.off[s + 1];
+			}
+		}
+		for (int i = lane; i < kRadix; i += 32) my_hist[i] = 0;
+		__syncthreads();
+		const uint32_t tile = s_misc[0];
+		if (tile >= T) break;
+		const uint32_t ti = s_misc[1];
+		const uint32_t lr = s_misc[2];
+		const uint64_t seg_a = s_seg[0], seg_e = s_seg[1];
+		const uint64_t tile_base = seg_a + (uint64_t)ti * TILE;
+		const uint64_t wbase = tile_base + (uint64_t)warp * (KPT * 32);
+
+		K k[KPT];
+#pragma unroll
+		for (int j = 0; j < KPT; ++j) {
+			const uint64_t idx = wbase + (uint64_t)j * 32 + lane;
+			k[j] = idx < seg_e ? kin[idx] : (K)~(K)0;
+		}
+#pragma unroll
+		for (int j = 0; j < KPT; ++j) atomicAdd(my_hist + digit_of(k[j], shift), 1u);
+		__syncthreads();
+
+		uint32_t tile_cnt = 0;
+		if (tid < kRadix) {
+			uint32_t sum = 0;
+#pragma unroll
+			for (int w = 0; w < kLWarps; ++w) {
+				const uint32_t c = s_hist[w * kRadix + tid];
+				s_hist[w * kRadix + tid] = sum;
+				sum += c;
+			}
+			tile_cnt = sum;
+			uint32_t *st = a.status + (size_t)tile * kRadix + tid;
+			dev::st_relaxed_u32(st, (ti == 0 ? kStPrefix : kStAgg) | tile_cnt);
+			a.status_next[(size_t)tile * kRadix + tid] = 0;
+			uint32_t inc = tile_cnt;
+#pragma unroll
+			for (int d = 1; d < 32; d <<= 1) {
+				const uint32_t t = __shfl_up_sync(0xffffffffu, inc, d);
+				if (lane >= d) inc += t;
+			}
+			if (lane == 31) s_misc[8 + warp] = inc;
+			s_tile_off[tid] = inc - tile_cnt;
+		} else if (tid < 2 * kRadix) {
+			const int d = tid - kRadix;
+			const uint32_t hv = a.seg_hist[(size_t)lr * a.hist_stride + d];
+			uint32_t inc = hv;
+#pragma unroll
+			for (int s = 1; s < 32; s <<= 1) {
+				const uint32_t t = __shfl_up_sync(0xffffffffu, inc, s);
+				if (lane >= s) inc += t;
+			}
+			if (lane == 31) s_misc[16 + (warp - 8)] = inc;
+			s_glob[d] = inc - hv;
+		}
+		__syncthreads();
+		uint32_t digit_base = 0;
+		if (tid < kRadix) {
+			uint32_t woff = 0, goff = 0;
+#pragma unroll
+			for (int w = 0; w < 8; ++w) {
+				if (w < warp) {
+					woff += s_misc[8 + w];
+					goff += s_misc[16 + w];
+				}
+			}
+			const uint32_t to = s_tile_off[tid] + woff;
+			s_tile_off[tid] = to;
+			digit_base = s_glob[tid] + goff;
+#pragma unroll
+			for (int w = 0; w < kLWarps; ++w) s_hist[w * kRadix + tid] += to;
+		}
+		__syncthreads();
+
+		if (tid < kRadix) {
+			uint32_t excl = 0;
+			if (ti > 0) {
+				long long base = (long long)tile - 1;
+				uint32_t iter = 0;
+				bool done = seg_lookback_window<4>(a.status, tid, base, excl);
+				while (!done && base >= 0) {
+					uint32_t sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + tid);
+					while ((sv & ~kStValue) == 0) {
+						if (++iter >= dev::kSpinLimit) break;
+						dev::backoff(iter);
+						sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + tid);
+					}
+					if ((sv & ~kStValue) == 0) {
+						dev::report_timeout(a.dev_status, DEV_ERR_LOOKBACK_TIMEOUT, (int)tile);
+						break;
+					}
+					done = seg_lookback_window<16>(a.status, tid, base, excl);
+				}
+				dev::st_relaxed_u32(a.status + (size_t)tile * kRadix + tid,
+					kStPrefix | (excl + tile_cnt));
+			}
+			s_glob[tid] = digit_base + excl - s_tile_off[tid];
+		}
+
+		K *sk = reinterpret_cast<K *>(s_stage);
+#pragma unroll
+		for (int j = 0; j < KPT; ++j) {
+			const uint32_t d = digit_of(k[j], shift);
+			atomicOr(my_match + d, 1u << lane);
+			__syncwarp();
+			const uint32_t peers = my_match[d];
+			const uint32_t start = my_hist[d];
+			__syncwarp();
+			const uint32_t below = __popc(peers & lt);
+			if (below == 0) {
+				my_hist[d] = start + __popc(peers);
+				my_match[d] = 0;
+			}
+			__syncwarp();
+			const uint32_t pos = start + below;
+			if (pos < (uint32_t)TILE) sk[pos] = k[j];
+		}
+		__syncthreads();
+#pragma unroll
+		for (int i = 0; i < KPT; ++i) {
+			const int q = i * kLThreads + tid;
+			const K key = sk[q];
+			const uint64_t o = seg_a + (uint32_t)(s_glob[digit_of(key, shift)] + (uint32_t)q);
+			if (o < seg_e) kout[o] = key;
+		}
+		__syncthreads();
+	}
+}
+
+template <typename K>
+size_t seg_pass_smem() {
+	return (2 * kLWarps * kRadix + 2 * kRadix + 64) * sizeof(uint32_t) + 2 * sizeof(uint64_t) +
+		(size_t)LCfg<K>::kTile * sizeof(K);
+}
+
+// Copies the large segments back from the alternate buffer (odd number of
+// passes).
+template <typename K>
+__global__ void __launch_bounds__(256) seg_copy_large(K *dst, const K *src,
+	const uint64_t *off, const uint64_t *tstart, const uint32_t *tile_seg, uint32_t S) {
+	constexpr int TILE = LCfg<K>::kTile;
+	const uint32_t T = (uint32_t)(tstart[S] >> 32);
+	for (uint32_t t = blockIdx.x; t < T; t += gridDim.x) {
+		const uint32_t s = tile_seg[t];
+		const uint64_t a = off[s] + (uint64_t)(t - (uint32_t)(tstart[s] >> 32)) * TILE;
+		const uint64_t e = off[s + 1];
+		const uint64_t end = a + TILE < e ? a + TILE : e;
+		for (uint64_t i = a + threadIdx.x; i < end; i += blockDim.x) dst[i] = src[i];
+	}
+}
+
+// Class layouts the autotuner chooses from: (threads, keys per thread) of
+// classes A and B for keys of up to 4 bytes; 8-byte keys halve the keys
+// per thread.
+struct Variant {
+	int a_threads, a_kpt, b_threads, b_kpt;
+};
+constexpr Variant kVariants[] = {
+	{128, 8, 512, 16},
+	{256, 8, 512, 16},
+	{128, 8, 256, 16},
+};
+constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+
+template <typename K, int THREADS, int KPT>
+cudaError_t launch_cta_class(K *keys, const uint64_t *off, const uint32_t *list,
+	const uint32_t *count, int passes, uint32_t max_blocks, CCLContext *ctx,
+	cudaStream_t s) {
+	using Cfg = CtaCfg<K, THREADS, KPT>;
+	const size_t smem = Cfg::smem();
+	auto kern = seg_sort_cta<K, THREADS, KPT>;
+	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		(int)smem);
+	if (e != cudaSuccess) return e;
+	int occ = 0;
+	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, THREADS, smem);
+	if (e != cudaSuccess) return e;
+	uint32_t grid = (uint32_t)std::max(1, occ) * (uint32_t)ctx->sm_count;
+	if (grid > max_blocks) grid = std::max<uint32_t>(max_blocks, 1);
+	KernelTimer t("seg_sort_cta", s, 0.0);
+	kern<<<grid, THREADS, smem, s>>>(keys, off, list, count, passes);
+	t.stop();
+	count_launches(1);
+	return cudaGetLastError();
+}
+
+template <typename K, int KPT_DIV>
+cudaError_t launch_variant_classes(int variant, K *keys, const uint64_t *off,
+	const uint32_t *lists, const uint32_t *counts, uint32_t S, int passes,
+	uint64_t n_cap, CCLContext *ctx, cudaStream_t s) {
+	// Blocks beyond the number of segments that can exist would only exit.
+	auto cap = [&](int tile_lo) {
+		return (uint32_t)std::min<uint64_t>(S, n_cap / (uint64_t)(tile_lo + 1) + 1);
+	};
+	cudaError_t e = cudaSuccess;
+	switch (variant) {
+	case 1:
+		e = launch_cta_class<K, 256, 8 / KPT_DIV>(keys, off, lists + (size_t)S, counts + 1,
+			passes, cap(32), ctx, s);
+		if (e == cudaSuccess)
+			e = launch_cta_class<K, 512, 16 / KPT_DIV>(keys, off, lists + 2 * (size_t)S,
+				counts + 2, passes, cap(256 * 8 / KPT_DIV), ctx, s);
+		break;
+	case 2:
+		e = launch_cta_class<K, 128, 8 / KPT_DIV>(keys, off, lists + (size_t)S, counts + 1,
+			passes, cap(32), ctx, s);
+		if (e == cudaSuccess)
+			e = launch_cta_class<K, 256, 16 / KPT_DIV>(keys, off, lists + 2 * (size_t)S,
+				counts + 2, passes, cap(128 * 8 / KPT_DIV), ctx, s);
+		break;
+	default:
+		e = launch_cta_class<K, 128, 8 / KPT_DIV>(keys, off, lists + (size_t)S, counts + 1,
+			passes, cap(32), ctx, s);
+		if (e == cudaSuccess)
+			e = launch_cta_class<K, 512, 16 / KPT_DIV>(keys, off, lists + 2 * (size_t)S,
+				counts + 2, passes, cap(128 * 8 / KPT_DIV), ctx, s);
+		break;
+	}
+	return e;
+}
+
+template <typename K>
+void launch_seg_upsweep(int passes, uint32_t grid, cudaStream_t s, const K *keys,
+	const uint64_t *off, const uint64_t *tstart, const uint32_t *tile_seg, uint32_t S,
+	uint32_t *seg_hist) {
+	switch (passes) {
+	case 1: seg_upsweep<K, 1><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist); break;
+	case 2: seg_upsweep<K, 2><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist); break;
+	case 3: seg_upsweep<K, 3><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist); break;
+	case 4: seg_upsweep<K, 4><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist); break;
+	case 5: seg_upsweep<K, 5><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist); break;
+	case 6: seg_upsweep<K, 6><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist); break;
+	case 7: seg_upsweep<K, 7><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist); break;
+	default: seg_upsweep<K, 8><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist); break;
+	}
+}
+
+template <typename K>
+cudaError_t seg_sort_typed(K *keys, uint64_t n_cap, const uint64_t *off, uint32_t S,
+	int sort_bits, int variant, CCLContext *ctx, cudaStream_t s, GError **err) {
+	constexpr int KPT_DIV = sizeof(K) > 4 ? 2 : 1;
+	constexpr int LTILE = LCfg<K>::kTile;
+	const int passes = sort_bits / kRadixBits;
+	if (S == 0 || passes == 0 || n_cap < 2) return cudaSuccess;
+	if (variant < 0 || variant >= kNumVariants) variant = 0;
+	const Variant &v = kVariants[variant];
+	const uint32_t max_a = (uint32_t)(v.a_threads * (v.a_kpt / KPT_DIV));
+	const uint32_t max_b = (uint32_t)(v.b_threads * (v.b_kpt / KPT_DIV));
+	// Bounds the host can derive without reading the offsets.
+	const uint64_t L_bound = std::min<uint64_t>(S, n_cap / (max_b + 1));
+	const uint64_t T_bound = n_cap / LTILE + L_bound + 1;
+	// Scratch: [counts 16][lists 4S][tinfo S+1][tstart S+1] then, with large
+	// segments possible, [tile_seg T][seg_hist L*passes*256][status 2*T*256]
+	// [alt keys n_cap].
+	size_t off_cnt = 0;
+	size_t off_lists = 64;
+	size_t off_tinfo = (off_lists + 4 * (size_t)S * 4 + 15) / 16 * 16;
+	size_t off_tstart = off_tinfo + ((size_t)S + 1) * 8;
+	size_t off_tseg = (off_tstart + ((size_t)S + 1) * 8 + 255) / 256 * 256;
+	size_t off_hist = (off_tseg + T_bound * 4 + 255) / 256 * 256;
+	size_t off_st0 = (off_hist + L_bound * passes * kRadix * 4 + 255) / 256 * 256;
+	size_t off_st1 = off_st0 + T_bound * kRadix * 4;
+	size_t off_alt = (off_st1 + T_bound * kRadix * 4 + 255) / 256 * 256;
+	size_t total = L_bound ? off_alt + n_cap * sizeof(K) : off_tseg;
+	char *tmp = (char *)tmp_alloc(ctx, total, s, err);
+	if (!tmp) return cudaErrorMemoryAllocation;
+	uint32_t *counts = (uint32_t *)(tmp + off_cnt);
+	uint32_t *lists = (uint32_t *)(tmp + off_lists);
+	uint64_t *tinfo = (uint64_t *)(tmp + off_tinfo);
+	uint64_t *tstart = (uint64_t *)(tmp + off_tstart);
+	uint32_t *tile_seg = (uint32_t *)(tmp + off_tseg);
+	uint32_t *seg_hist = (uint32_t *)(tmp + off_hist);
+	uint32_t *st[2] = {(uint32_t *)(tmp + off_st0), (uint32_t *)(tmp + off_st1)};
+	K *alt = (K *)(tmp + off_alt);
+	unsigned launches = 0;
+	cudaError_t e = cudaMemsetAsync(counts, 0, 64, s);
+	if (e == cudaSuccess) {
+		ClassArgs ca;
+		ca.off = off;
+		ca.S = S;
+		ca.n_cap = n_cap;
+		ca.max_warp = 32;
+		ca.max_a = max_a;
+		ca.max_b = max_b;
+		ca.large_tile = LTILE;
+		ca.lists = lists;
+		ca.counts = counts;
+		ca.tinfo = tinfo;
+		ca.dev_status = ctx->d_status;
+		const uint32_t grid = (uint32_t)std::min<uint64_t>(((uint64_t)S + 1 + 255) / 256,
+			(uint64_t)ctx->sm_count * 8);
+		seg_classify<<<grid, 256, 0, s>>>(ca);
+		launches++;
+		e = cudaGetLastError();
+	}
+	if (e == cudaSuccess)
+		e = scan_exclusive(tinfo, tstart, (size_t)S + 1, CLO_ULONG, 8, ctx, s, err);
+	const K mask = sort_bits >= (int)(8 * sizeof(K)) ? (K)~(K)0
+		: (K)(((K)1 << sort_bits) - 1);
+	if (e == cudaSuccess) {
+		const uint32_t grid = (uint32_t)std::min<uint64_t>(((uint64_t)S + 7) / 8,
+			(uint64_t)ctx->sm_count * 8);
+		KernelTimer t("seg_sort_warp", s, 0.0);
+		seg_sort_warp<K><<<grid, 256, 0, s>>>(keys, off, lists, counts, mask);
+		t.stop();
+		launches++;
+		e = cudaGetLastError();
+	}
+	if (e == cudaSuccess)
+		e = launch_variant_classes<K, KPT_DIV>(variant, keys, off, lists, counts, S,
+			passes, n_cap, ctx, s);
+	if (e == cudaSuccess && L_bound > 0) {
+		const uint32_t *list3 = lists + 3 * (size_t)S;
+		{
+			const uint32_t grid = (uint32_t)std::min<uint64_t>((L_bound + 7) / 8,
+				(uint64_t)ctx->sm_count * 8);
+			seg_tiles<LTILE><<<grid, 256, 0, s>>>(off, tstart, list3, counts + 3, tile_seg,
+				seg_hist, passes, st[0]);
+			launches++;
+			e = cudaGetLastError();
+		}
+		if (e == cudaSuccess) {
+			const uint32_t grid = (uint32_t)std::min<uint64_t>(T_bound,
+				(uint64_t)ctx->sm_count * 8);
+			KernelTimer t("seg_upsweep", s, 0.0);
+			launch_seg_upsweep<K>(passes, grid, s, keys, off, tstart, tile_seg, S, seg_hist);
+			t.stop();
+			launches++;
+			e = cudaGetLastError();
+		}
+		const size_t smem = seg_pass_smem<K>();
+		auto kern = seg_pass<K>;
+		if (e == cudaSuccess)
+			e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+				(int)smem);
+		int occ = 0;
+		if (e == cudaSuccess)
+			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kLThreads, smem);
+		const uint32_t pgrid = (uint32_t)std::min<uint64_t>(T_bound,
+			(uint64_t)std::max(occ, 1) * ctx->sm_count);
+		K *src = keys, *dst = alt;
+		for (int p = 0; p < passes && e == cudaSuccess; ++p) {
+			SegPassArgs pa;
+			pa.off = off;
+			pa.tstart = tstart;
+			pa.tile_seg = tile_seg;
+			pa.seg_hist = seg_hist + (size_t)p * kRadix;
+			pa.hist_stride = (uint32_t)(passes * kRadix);
+			pa.status = st[p & 1];
+			pa.status_next = st[(p + 1) & 1];
+			pa.counter = counts + 8 + p;
+			pa.dev_status = ctx->d_status;
+			pa.S = S;
+			pa.shift = p * kRadixBits;
+			KernelTimer t("seg_pass", s, 0.0);
+			kern<<<pgrid, kLThreads, smem, s>>>(src, dst, pa);
+			t.stop();
+			launches++;
+			e = cudaGetLastError();
+			std::swap(src, dst);
+		}
+		if (e == cudaSuccess && (passes & 1)) {
+			const uint32_t grid = (uint32_t)std::min<uint64_t>(T_bound,
+				(uint64_t)ctx->sm_count * 8);
+			seg_copy_large<K><<<grid, 256, 0, s>>>(keys, alt, off, tstart, tile_seg, S);
+			launches++;
+			e = cudaGetLastError();
+		}
+	}
+	count_launches(launches);
+	tmp_free(tmp, s);
+	if (e != cudaSuccess && (err == nullptr || *err == nullptr)) cuda_ok(e, err, "segmented sort");
+	return e;
+}
+
+// ------------------------------------------------------------ segmented scan
+constexpr int kSThreads = 256;
+constexpr int kSWarps = kSThreads / 32;
+constexpr int kSItems = 16;
+constexpr int kSWarpElems = 32 * kSItems;
+constexpr int kSTile = kSWarps * kSWarpElems;
+constexpr int kSPadded = kSWarpElems + kSWarpElems / 32;
+
+__device__ __forceinline__ int pidx(int i) { return i + (i >> 5); }
+
+// Head bitmap: bit i set when a segment starts at element i (and holds
+// elements).
+__global__ void __launch_bounds__(256) seg_heads(const uint64_t *off, uint32_t S,
+	uint64_t n_cap, uint32_t *bits, int *dev_status) {
+	const uint64_t end = off[S];
+	for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < S;
+		 s += (uint64_t)gridDim.x * blockDim.x) {
+		const uint64_t len = checked_len(off, (uint32_t)s, n_cap, dev_status);
+		const uint64_t a = off[s];
+		if (len > 0 && a < end) atomicOr(bits + (a >> 5), 1u << (a & 31));
+	}
+}
+
+// Segmented exclusive scan: out[i] = sum of in[j] for j from the start of
+// i's segment to i - 1, for i in [off[0], off[S]); nothing else is written.
+// The combine of (head seen, sum) pairs is the usual segmented one: a
+// later head discards what came before it.
+template <typename InT, typename OutT>
+__global__ void __launch_bounds__(kSThreads, 4)
+seg_scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, uint64_t n,
+	const uint32_t *__restrict__ heads, const uint64_t *off, uint32_t S,
+	lb::TileStatus ts, int *dev_status, bool vec_ok) {
+	using Acc = typename std::conditional<(sizeof(OutT) <= 4), uint32_t, uint64_t>::type;
+	constexpr int ESZ = sizeof(InT) > sizeof(OutT) ? sizeof(InT) : sizeof(OutT);
+	constexpr int PT = lb::Slots<Acc>::kPerTile;
+	constexpr int KW = lb::Slots<Acc>::kWords;
+	__shared__ __align__(16) unsigned char s_buf[kSWarps][kSPadded * ESZ];
+	__shared__ Acc s_wsum[kSWarps];
+	__shared__ uint32_t s_wflag[kSWarps];
+	__shared__ Acc s_excl;
+	__shared__ uint32_t s_tile;
+	__shared__ uint64_t s_lo, s_hi;
+
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	if (tid == 0) {
+		s_tile = atomicAdd(ts.counter, 1u);
+		s_lo = off[0];
+		s_hi = off[S];
+	}
+	__syncthreads();
+	const uint32_t tile = s_tile;
+	const uint64_t lo = s_lo, hi = s_hi;
+	const uint64_t seg = (uint64_t)tile * kSTile + (uint64_t)warp * kSWarpElems;
+	const bool full = seg + kSWarpElems <= n;
+
+	InT *sin = reinterpret_cast<InT *>(s_buf[warp]);
+	if (full && vec_ok) {
+		constexpr int EPC = 16 / sizeof(InT);
+		constexpr int CHUNKS = kSWarpElems / EPC;
+		const uint4 *src = reinterpret_cast<const uint4 *>(in + seg);
+#pragma unroll
+		for (int c = lane; c < CHUNKS; c += 32) {
+			uint4 v = dev::ld_stream_v4(src + c);
+			const InT *e = reinterpret_cast<const InT *>(&v);
+#pragma unroll
+			for (int k = 0; k < EPC; ++k) sin[pidx(c * EPC + k)] = e[k];
+		}
+	} else {
+		for (int i = lane; i < kSWarpElems; i += 32)
+			sin[pidx(i)] = (seg + i < n) ? in[seg + i] : (InT)0;
+	}
+	// This thread's 16 elements start at a multiple of 16: their head bits
+	// are one half of one bitmap word.
+	const uint64_t e0 = seg + (uint64_t)lane * kSItems;
+	const uint32_t hb = e0 < n ? (heads[e0 >> 5] >> (uint32_t)(e0 & 31)) & 0xffffu : 0u;
+	__syncwarp();
+
+	Acc x[kSItems];
+	Acc run = 0;
+#pragma unroll
+	for (int j = 0; j < kSItems; ++j) {
+		const Acc v = (Acc)(OutT)sin[pidx(lane * kSItems + j)];
+		if ((hb >> j) & 1u) run = 0;
+		x[j] = run;
+		run += v;
+	}
+	// Warp inclusive segmented scan of (has head, sum since last head).
+	Acc inc = run;
+	uint32_t finc = hb != 0;
+#pragma unroll
+	for (int d = 1; d < 32; d <<= 1) {
+		const Acc t = __shfl_up_sync(0xffffffffu, inc, d);
+		const uint32_t tf = __shfl_up_sync(0xffffffffu, finc, d);
+		if (lane >= d) {
+			if (!finc) inc += t;
+			finc |= tf;
+		}
+	}
+	Acc ex = __shfl_up_sync(0xffffffffu, inc, 1);
+	uint32_t fex = __shfl_up_sync(0xffffffffu, finc, 1);
+	if (lane == 0) {
+		ex = 0;
+		fex = 0;
+	}
+	if (lane == 31) {
+		s_wsum[warp] = inc;
+		s_wflag[warp] = finc;
+	}
+	__syncthreads();
+
+	if (warp == 0) {
+		const Acc wt = lane < kSWarps ? s_wsum[lane] : (Acc)0;
+		const uint32_t wf = lane < kSWarps ? s_wflag[lane] : 0u;
+		Acc winc = wt;
+		uint32_t wfinc = wf;
+#pragma unroll
+		for (int d = 1; d < kSWarps; d <<= 1) {
+			const Acc t = __shfl_up_sync(0xffffffffu, winc, d);
+			const uint32_t tf = __shfl_up_sync(0xffffffffu, wfinc, d);
+			if (lane >= d) {
+				if (!wfinc) winc += t;
+				wfinc |= tf;
+			}
+		}
+		const Acc agg = __shfl_sync(0xffffffffu, winc, kSWarps - 1);
+		const uint32_t agg_f = __shfl_sync(0xffffffffu, wfinc, kSWarps - 1);
+		Acc wex = __shfl_up_sync(0xffffffffu, winc, 1);
+		uint32_t wfex = __shfl_up_sync(0xffffffffu, wfinc, 1);
+		if (lane == 0) {
+			wex = 0;
+			wfex = 0;
+		}
+		// A tile holding a head knows its inclusive prefix at once.
+		uint64_t *tw = ts.words + (size_t)tile * PT;
+		if (lane == 0) {
+			if (agg_f || tile == 0) lb::publish<Acc>(tw + KW, agg);
+			else lb::publish<Acc>(tw, agg);
+		}
+		// The carry from earlier tiles matters only when the tile's first
+		// element is not a head.
+		const uint32_t first_head = __shfl_sync(0xffffffffu, hb, 0) & 1u;
+		Acc excl = 0;
+		if (tile > 0 && !first_head) excl = lb::lookback_warp<Acc>(ts.words, tile, dev_status);
+		if (lane == 0 && !agg_f && tile > 0) lb::publish<Acc>(tw + KW, excl + agg);
+		if (lane < kSWarps) {
+			s_wsum[lane] = wex;
+			s_wflag[lane] = wfex;
+		}
+		if (lane == 0) s_excl = excl;
+	}
+	__syncthreads();
+
+	const Acc wcarry = s_wsum[warp] + (s_wflag[warp] ? (Acc)0 : s_excl);
+	const Acc tcarry = ex + (fex ? (Acc)0 : wcarry);
+	const int fh = hb ? __ffs(hb) - 1 : kSItems;
+	OutT *sout = reinterpret_cast<OutT *>(s_buf[warp]);
+#pragma unroll
+	for (int j = 0; j < kSItems; ++j)
+		sout[pidx(lane * kSItems + j)] = (OutT)(x[j] + (j < fh ? tcarry : (Acc)0));
+	__syncwarp();
+	if (full && vec_ok && seg >= lo && seg + kSWarpElems <= hi) {
+		constexpr int EPC = 16 / sizeof(OutT);
+		constexpr int CHUNKS = kSWarpElems / EPC;
+		uint4 *dst = reinterpret_cast<uint4 *>(out + seg);
+#pragma unroll
+		for (int c = lane; c < CHUNKS; c += 32) {
+			uint4 v;
+			OutT *e = reinterpret_cast<OutT *>(&v);
+#pragma unroll
+			for (int k = 0; k < EPC; ++k) e[k] = sout[pidx(c * EPC + k)];
+			dev::st_stream_v4(dst + c, v);
+		}
+	} else {
+		for (int i = lane; i < kSWarpElems; i += 32) {
+			const uint64_t g = seg + i;
+			if (g < n && g >= lo && g < hi) out[g] = sout[pidx(i)];
+		}
+	}
+}
+
+template <typename InT, typename OutT>
+cudaError_t launch_seg_scan(const void *in, void *out, uint64_t n_cap,
+	const uint64_t *off, uint32_t S, CCLContext *ctx, cudaStream_t s, GError **err) {
+	using Acc = typename std::conditional<(sizeof(OutT) <= 4), uint32_t, uint64_t>::type;
+	const uint64_t tiles = (n_cap + kSTile - 1) / kSTile;
+	if (tiles >= (1ull << 31)) {
+		set_error(err, CLO_ERROR_ARGS, "Segmented scan buffer of %llu elements is too large",
+			(unsigned long long)n_cap);
+		return cudaErrorInvalidValue;
+	}
+	const size_t words = (size_t)((n_cap + 31) / 32) + 1;
+	const size_t bm_bytes = (words * 4 + 15) / 16 * 16;
+	const size_t st_bytes = (size_t)tiles * lb::Slots<Acc>::kPerTile * 8;
+	const size_t total = bm_bytes + st_bytes + 16;
+	char *tmp = (char *)tmp_alloc(ctx, total, s, err);
+	if (!tmp) return cudaErrorMemoryAllocation;
+	uint32_t *bits = (uint32_t *)tmp;
+	lb::TileStatus ts;
+	ts.words = (uint64_t *)(tmp + bm_bytes);
+	ts.counter = (uint32_t *)(tmp + bm_bytes + st_bytes);
+	cudaError_t e = cudaMemsetAsync(tmp, 0, total, s);
+	if (e == cudaSuccess) {
+		const uint32_t grid = (uint32_t)std::min<uint64_t>(((uint64_t)S + 255) / 256,
+			(uint64_t)ctx->sm_count * 8);
+		seg_heads<<<std::max<uint32_t>(grid, 1), 256, 0, s>>>(off, S, n_cap, bits,
+			ctx->d_status);
+		e = cudaGetLastError();
+	}
+	const bool vec_ok = ((uintptr_t)in % 16 == 0) && ((uintptr_t)out % 16 == 0);
+	if (e == cudaSuccess) {
+		KernelTimer t("seg_scan_lookback", s, (double)n_cap * (sizeof(InT) + sizeof(OutT)));
+		seg_scan_lookback<InT, OutT><<<(unsigned)tiles, kSThreads, 0, s>>>(
+			(const InT *)in, (OutT *)out, n_cap, bits, off, S, ts, ctx->d_status, vec_ok);
+		t.stop();
+		e = cudaGetLastError();
+	}
+	count_launches(2);
+	tmp_free(tmp, s);
+	if (e != cudaSuccess) cuda_ok(e, err, "segmented scan");
+	return e;
+}
+
+template <typename InT>
+cudaError_t seg_scan_out(const void *in, void *out, uint64_t n_cap, const uint64_t *off,
+	uint32_t S, int out_bytes, CCLContext *ctx, cudaStream_t s, GError **err) {
+	switch (out_bytes) {
+	case 1: return launch_seg_scan<InT, uint8_t>(in, out, n_cap, off, S, ctx, s, err);
+	case 2: return launch_seg_scan<InT, uint16_t>(in, out, n_cap, off, S, ctx, s, err);
+	case 4: return launch_seg_scan<InT, uint32_t>(in, out, n_cap, off, S, ctx, s, err);
+	case 8: return launch_seg_scan<InT, uint64_t>(in, out, n_cap, off, S, ctx, s, err);
+	}
+	set_error(err, CLO_ERROR_ARGS, "Unsupported sum width %d", out_bytes);
+	return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+int seg_sort_num_variants() { return kNumVariants; }
+
+cudaError_t seg_sort(void *keys, uint64_t n_cap, const uint64_t *off, size_t S,
+	int key_bytes, int sort_bits, int variant, CCLContext *ctx, cudaStream_t s,
+	GError **err) {
+	if (S >= (1ull << 31)) {
+		set_error(err, CLO_ERROR_ARGS, "Too many segments (%zu)", S);
+		return cudaErrorInvalidValue;
+	}
+	const uint32_t s32 = (uint32_t)S;
+	switch (key_bytes) {
+	case 1: return seg_sort_typed<uint8_t>((uint8_t *)keys, n_cap, off, s32, sort_bits, variant, ctx, s, err);
+	case 2: return seg_sort_typed<uint16_t>((uint16_t *)keys, n_cap, off, s32, sort_bits, variant, ctx, s, err);
+	case 4: return seg_sort_typed<uint32_t>((uint32_t *)keys, n_cap, off, s32, sort_bits, variant, ctx, s, err);
+	case 8: return seg_sort_typed<uint64_t>((uint64_t *)keys, n_cap, off, s32, sort_bits, variant, ctx, s, err);
+	}
+	set_error(err, CLO_ERROR_ARGS, "Unsupported key width %d", key_bytes);
+	return cudaErrorInvalidValue;
+}
+
+cudaError_t seg_scan(const void *in, void *out, uint64_t n_cap, const uint64_t *off,
+	size_t S, CloType in_type, int out_bytes, CCLContext *ctx, cudaStream_t s,
+	GError **err) {
+	if (S == 0 || n_cap == 0) return cudaSuccess;
+	if (S >= (1ull << 31)) {
+		set_error(err, CLO_ERROR_ARGS, "Too many segments (%zu)", S);
+		return cudaErrorInvalidValue;
+	}
+	const uint32_t s32 = (uint32_t)S;
+	switch (in_type) {
+	case CLO_CHAR: return seg_scan_out<int8_t>(in, out, n_cap, off, s32, out_bytes, ctx, s, err);
+	case CLO_UCHAR: return seg_scan_out<uint8_t>(in, out, n_cap, off, s32, out_bytes, ctx, s, err);
+	case CLO_SHORT: return seg_scan_out<int16_t>(in, out, n_cap, off, s32, out_bytes, ctx, s, err);
+	case CLO_USHORT: return seg_scan_out<uint16_t>(in, out, n_cap, off, s32, out_bytes, ctx, s, err);
+	case CLO_INT: return seg_scan_out<int32_t>(in, out, n_cap, off, s32, out_bytes, ctx, s, err);
+	case CLO_UINT: return seg_scan_out<uint32_t>(in, out, n_cap, off, s32, out_bytes, ctx, s, err);
+	case CLO_LONG: return seg_scan_out<int64_t>(in, out, n_cap, off, s32, out_bytes, ctx, s, err);
+	case CLO_ULONG: return seg_scan_out<uint64_t>(in, out, n_cap, off, s32, out_bytes, ctx, s, err);
+	default: break;
+	}
+	set_error(err, CLO_ERROR_ARGS, "Unsupported scan element type %d", (int)in_type);
+	return cudaErrorInvalidValue;
+}
+
+}  // namespace clo

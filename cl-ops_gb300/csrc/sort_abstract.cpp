@@ -99,6 +99,9 @@ struct SatradixData {
 	std::string scan_type;
 	std::string scan_opts;
 	CloScan *scanner;
+	// Class layout of segmented sorts (segvariant= option, or the
+	// autotuner's choice).
+	int seg_variant;
 };
 
 const char *kSatradixKernels[] = {"satradix_upsweep", "satradix_onesweep"};
@@ -126,6 +129,7 @@ const char *satradix_init(CloSort *s, const char *options, GError **err) {
 	SatradixData *d = new SatradixData();
 	d->radix = 16;
 	d->scanner = nullptr;
+	d->seg_variant = 0;
 	s->data = d;
 	bool ok = for_each_option(options, [&](const std::string &k,
 		const std::string &v, const std::string &tok, bool has_eq) {
@@ -138,6 +142,13 @@ const char *satradix_init(CloSort *s, const char *options, GError **err) {
 			d->radix = (unsigned)atoi(v.c_str());
 			if (clo_ones32(d->radix) != 1) {
 				set_error(err, CLO_ERROR_ARGS, "Radix must be a power of 2.");
+				return false;
+			}
+		} else if (k == "segvariant") {
+			d->seg_variant = atoi(v.c_str());
+			if (d->seg_variant < 0 || d->seg_variant >= clo::seg_sort_num_variants()) {
+				set_error(err, CLO_ERROR_ARGS, "segvariant must be in [0, %d).",
+					clo::seg_sort_num_variants());
 				return false;
 			}
 		} else if (k.size() >= 4 && strncasecmp(k.c_str(), "scan", 4) == 0) {
@@ -738,6 +749,169 @@ done:
 	if (own) ccl_queue_destroy(own);
 	clo::propagate_error(err, e2);
 	return status;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------- segmented sort
+namespace {
+
+bool seg_args_ok(CloSort *sorter, CCLQueue *q, const char *what, GError **err) {
+	if (!sorter || !q || (err && *err)) {
+		fprintf(stderr, "cl_ops: %s: bad arguments\n", what);
+		return false;
+	}
+	if (strcmp(sorter->impl_def.name, "satradix") != 0) {
+		set_error(err, CLO_ERROR_ARGS,
+			"Segmented sorting is implemented for the satradix sorter (stable, "
+			"unsigned key order), not '%s'", sorter->impl_def.name);
+		return false;
+	}
+	return true;
+}
+
+CCLEvent *seg_sort_device(CloSort *sorter, CCLQueue *q, CCLBuffer *data,
+	CCLBuffer *offsets, size_t nseg, int variant, GError **err) {
+	const size_t eb = clo_type_sizeof(sorter->elem_type);
+	if (!data || (nseg > 0 && (!offsets || offsets->size < (nseg + 1) * 8))) {
+		set_error(err, CLO_ERROR_ARGS,
+			"Segmented sort needs a data buffer and %zu offsets", nseg + 1);
+		return nullptr;
+	}
+	ccl_event *ev = clo::event_begin(q, "satradix_segmented");
+	if (nseg > 0 && clo::seg_sort(data->ptr, data->size / eb,
+			(const uint64_t *)offsets->ptr, nseg, (int)eb, satradix_sort_bits(sorter),
+			variant, sorter->ctx, q->stream, err) != cudaSuccess)
+		return nullptr;
+	clo::event_end(ev);
+	return ev;
+}
+
+}  // namespace
+
+extern "C" {
+
+CCLEvent *clo_sort_segmented_with_device_data(CloSort *sorter, CCLQueue *q,
+	CCLBuffer *data, CCLBuffer *offsets, size_t num_segments, GError **err) {
+	if (!seg_args_ok(sorter, q, "clo_sort_segmented_with_device_data", err))
+		return nullptr;
+	cudaSetDevice(sorter->ctx->ordinal);
+	SatradixData *d = (SatradixData *)sorter->data;
+	return seg_sort_device(sorter, q, data, offsets, num_segments, d->seg_variant, err);
+}
+
+cl_bool clo_sort_segmented_with_host_data(CloSort *sorter, CCLQueue *q, void *data,
+	size_t numel, const cl_ulong *offsets, size_t num_segments, GError **err) {
+	if (!sorter || (err && *err)) return CL_FALSE;
+	CCLContext *ctx = sorter->ctx;
+	cudaSetDevice(ctx->ordinal);
+	if (!clo::check_offsets((const uint64_t *)offsets, num_segments, numel, err))
+		return CL_FALSE;
+	GError *e2 = nullptr;
+	CCLQueue *own = nullptr;
+	if (!q) {
+		own = ccl_queue_new(ctx, &ctx->device, 0, &e2);
+		if (!own) {
+			clo::propagate_error(err, e2);
+			return CL_FALSE;
+		}
+		q = own;
+	}
+	const size_t bytes = numel * clo_type_sizeof(sorter->elem_type);
+	const size_t obytes = (num_segments + 1) * 8;
+	cl_bool status = CL_FALSE;
+	CCLBuffer *dd = nullptr, *doff = nullptr;
+	CCLEventWaitList ewl = nullptr;
+	CCLEvent *evt = nullptr;
+	void *pd = clo::tmp_alloc(ctx, bytes, q->stream, &e2);
+	void *po = pd ? clo::tmp_alloc(ctx, obytes, q->stream, &e2) : nullptr;
+	if (!pd || !po) goto done;
+	dd = ccl_buffer_new_wrap(ctx, pd, bytes, &e2);
+	doff = ccl_buffer_new_wrap(ctx, po, obytes, &e2);
+	if (!ccl_buffer_enqueue_write(dd, q, CL_FALSE, 0, bytes, data, nullptr, &e2))
+		goto done;
+	if (num_segments > 0 &&
+		!ccl_buffer_enqueue_write(doff, q, CL_FALSE, 0, obytes, offsets, nullptr, &e2))
+		goto done;
+	if (!clo_sort_segmented_with_device_data(sorter, q, dd, doff, num_segments, &e2))
+		goto done;
+	evt = ccl_buffer_enqueue_read(dd, q, CL_FALSE, 0, bytes, data, nullptr, &e2);
+	if (!evt) goto done;
+	ccl_ewl(&ewl, evt, (CCLEvent *)nullptr);
+	if (!ccl_event_wait(&ewl, &e2)) goto done;
+	status = CL_TRUE;
+done:
+	ccl_event_wait_list_clear(&ewl);
+	if (dd) ccl_buffer_destroy(dd);
+	if (doff) ccl_buffer_destroy(doff);
+	clo::tmp_free(pd, q->stream);
+	clo::tmp_free(po, q->stream);
+	if (!status) cudaStreamSynchronize(q->stream);
+	if (own) ccl_queue_destroy(own);
+	clo::propagate_error(err, e2);
+	return status;
+}
+
+cl_int clo_sort_segmented_tune(CloSort *sorter, CCLQueue *q, CCLBuffer *data,
+	CCLBuffer *offsets, size_t num_segments, double *times_ms, GError **err) {
+	if (!seg_args_ok(sorter, q, "clo_sort_segmented_tune", err)) return -1;
+	if (!data) {
+		set_error(err, CLO_ERROR_ARGS, "NULL data buffer");
+		return -1;
+	}
+	CCLContext *ctx = sorter->ctx;
+	cudaSetDevice(ctx->ordinal);
+	SatradixData *d = (SatradixData *)sorter->data;
+	const int nv = clo::seg_sort_num_variants();
+	// Each variant sorts a fresh copy of the caller's data; the best of two
+	// runs counts. The caller's data is left as it was.
+	void *work = clo::tmp_alloc(ctx, data->size, q->stream, err);
+	if (!work) return -1;
+	CCLBuffer *wb = ccl_buffer_new_wrap(ctx, work, data->size, err);
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	int best = -1;
+	double best_ms = 0.0;
+	GError *e2 = nullptr;
+	for (int v = 0; v < nv && !e2; ++v) {
+		double vbest = -1.0;
+		for (int rep = 0; rep < 2 && !e2; ++rep) {
+			if (!cuda_ok(cudaMemcpyAsync(work, data->ptr, data->size,
+					cudaMemcpyDeviceToDevice, q->stream), &e2, "tune copy"))
+				break;
+			cudaEventRecord(e0, q->stream);
+			if (!seg_sort_device(sorter, q, wb, offsets, num_segments, v, &e2)) break;
+			cudaEventRecord(e1, q->stream);
+			if (!cuda_ok(cudaEventSynchronize(e1), &e2, "tune wait")) break;
+			if (!clo::check_device_status(ctx, &e2)) break;
+			float ms = 0.f;
+			cudaEventElapsedTime(&ms, e0, e1);
+			if (vbest < 0 || ms < vbest) vbest = ms;
+		}
+		if (e2) break;
+		if (times_ms) times_ms[v] = vbest;
+		if (best < 0 || vbest < best_ms) {
+			best = v;
+			best_ms = vbest;
+		}
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	ccl_buffer_destroy(wb);
+	clo::tmp_free(work, q->stream);
+	cudaStreamSynchronize(q->stream);
+	if (e2) {
+		clo::propagate_error(err, e2);
+		return -1;
+	}
+	d->seg_variant = best;
+	return best;
+}
+
+cl_int clo_sort_segmented_get_variant(CloSort *sorter) {
+	if (!sorter || strcmp(sorter->impl_def.name, "satradix") != 0) return -1;
+	return ((SatradixData *)sorter->data)->seg_variant;
 }
 
 }  // extern "C"

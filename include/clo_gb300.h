@@ -91,6 +91,75 @@ cl_bool clo_scan_blelloch_noalloc(CCLQueue *cq, CloType elem_type,
 	CloType sum_type, const void *d_in, void *d_out, size_t numel,
 	GError **err);
 
+/* ---------------------------------------------------------------------
+ * Segmented operations: many independent segments of one buffer in one
+ * call. `offsets` holds num_segments + 1 cl_ulong values, non-decreasing;
+ * segment i is elements [offsets[i], offsets[i+1]). Every segment comes
+ * out exactly as a separate clo_sort_with_device_data /
+ * clo_scan_with_device_data call on that segment alone would leave it;
+ * elements outside [offsets[0], offsets[num_segments]) are not written.
+ * Segments must be shorter than 2^30 elements. The device-data forms
+ * issue a fixed sequence of launches that depends only on the buffer sizes
+ * and num_segments (no host readback of the offsets), so they can be
+ * captured into a CUDA graph (clo_queue_begin_capture); invalid offsets
+ * are detected on the device and reported (CLO_ERROR_ARGS) by the next
+ * synchronising call on the queue. The host-data forms check the offsets
+ * first and block.
+ * --------------------------------------------------------------------- */
+
+/* Sorts every segment of `data` (in place) in "satradix" order: stable,
+ * ascending by the unsigned bit pattern of the sorter's key. Only
+ * "satradix" sorters accept it; others set CLO_ERROR_ARGS. The buffer
+ * capacity (its size / element size) bounds the offsets. Segments go by
+ * length to a warp (<= 32 elements), a CTA (two classes of shared-memory
+ * radix sort) or the multi-CTA onesweep passes; the CTA class layout is
+ * the sorter's "segvariant=<n>" option or the autotuner's choice. */
+CCLEvent *clo_sort_segmented_with_device_data(CloSort *sorter, CCLQueue *cq_exec,
+	CCLBuffer *data, CCLBuffer *offsets, size_t num_segments, GError **err);
+cl_bool clo_sort_segmented_with_host_data(CloSort *sorter, CCLQueue *cq_exec,
+	void *data, size_t numel, const cl_ulong *offsets, size_t num_segments,
+	GError **err);
+
+/* Number of CTA class layouts of the segmented sort. */
+#define CLO_SEG_SORT_VARIANTS 3
+
+/* Autotuner: times every class layout on a copy of `data` with these
+ * offsets (best of two runs each), stores the fastest in the sorter for
+ * its later segmented sorts and returns its index (-1 on error). The
+ * caller's data is not modified. times_ms, when not NULL, receives
+ * CLO_SEG_SORT_VARIANTS times in milliseconds. Blocking. */
+cl_int clo_sort_segmented_tune(CloSort *sorter, CCLQueue *cq_exec,
+	CCLBuffer *data, CCLBuffer *offsets, size_t num_segments, double *times_ms,
+	GError **err);
+/* The class layout the sorter's segmented sorts use (-1: not satradix). */
+cl_int clo_sort_segmented_get_variant(CloSort *sorter);
+
+/* Per-segment exclusive scan of data_in into data_out (the scanner's
+ * element and sum types): within each segment, the scan of that segment
+ * alone. One launch over the buffer, whatever the number of segments. The
+ * capacity is the smaller of the two buffers' element counts. */
+CCLEvent *clo_scan_segmented_with_device_data(CloScan *scanner, CCLQueue *cq_exec,
+	CCLBuffer *data_in, CCLBuffer *data_out, CCLBuffer *offsets,
+	size_t num_segments, GError **err);
+cl_bool clo_scan_segmented_with_host_data(CloScan *scanner, CCLQueue *cq_exec,
+	const void *data_in, void *data_out, size_t numel, const cl_ulong *offsets,
+	size_t num_segments, GError **err);
+
+/* ---------------------------------------------------------------------
+ * CUDA graphs of queue work: everything enqueued on cq between
+ * clo_queue_begin_capture and clo_queue_end_capture (by this thread) is
+ * recorded instead of run, and replayed by clo_graph_launch. Device-data
+ * calls of this library are capturable (satradix then runs every pass: it
+ * skips no constant digit, which needs a host readback); host-data calls
+ * and anything that waits are not. Temporaries become graph memory nodes.
+ * --------------------------------------------------------------------- */
+typedef struct clo_graph CloGraph;
+cl_bool clo_queue_begin_capture(CCLQueue *cq, GError **err);
+CloGraph *clo_queue_end_capture(CCLQueue *cq, GError **err);
+cl_bool clo_graph_launch(CloGraph *graph, CCLQueue *cq, GError **err);
+size_t clo_graph_get_num_nodes(CloGraph *graph);
+void clo_graph_destroy(CloGraph *graph);
+
 /* Test hook for the bounded lookback waits: tile `tile` of subsequent
  * scans withholds its status, so the next tile's wait runs out, the
  * kernel ends and the next synchronising call reports CLO_ERROR_LIBRARY.

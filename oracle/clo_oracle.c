@@ -411,3 +411,20 @@ void oracle_radix_sort_u32_threaded(uint32_t *keys, size_t n, int threads,
 	free(tmp);
 	free(count);
 }
+
+void oracle_seg_sort(void *keys, const uint64_t *off, size_t nseg, int kb,
+	int sort_bits) {
+	for (size_t i = 0; i < nseg; ++i)
+		oracle_radix_sort((unsigned char *)keys + off[i] * (size_t)kb, NULL,
+			(size_t)(off[i + 1] - off[i]), kb, 0, sort_bits);
+}
+
+void oracle_seg_scan(const void *in, void *out, const uint64_t *off, size_t nseg,
+	int in_type, int out_bytes) {
+	static const int sizes[] = {1, 1, 2, 2, 4, 4, 8, 8};
+	const int ib = sizes[in_type];
+	for (size_t i = 0; i < nseg; ++i)
+		oracle_scan((const unsigned char *)in + off[i] * (size_t)ib,
+			(unsigned char *)out + off[i] * (size_t)out_bytes,
+			(size_t)(off[i + 1] - off[i]), in_type, out_bytes);
+}

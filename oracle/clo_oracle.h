@@ -62,4 +62,15 @@ void oracle_mt19937(uint32_t seed, uint32_t *out, size_t nwords);
  * generator of the tests and the benchmark. */
 void oracle_splitmix64(uint64_t seed, uint64_t *out, size_t n);
 
+/* Segmented forms: each segment [off[i], off[i+1]) (i < nseg) handled as
+ * a separate oracle_radix_sort / oracle_scan call on it would handle it
+ * -- i.e. as a separate clo_sort_with_device_data ("satradix",
+ * src/cl_ops/sort/clo_sort_satradix.c:117-335) or clo_scan_with_device_data
+ * ("blelloch", src/cl_ops/scan/clo_scan_blelloch.c:78-214) call on that
+ * segment. Elements outside every segment are left alone. */
+void oracle_seg_sort(void *keys, const uint64_t *off, size_t nseg, int key_bytes,
+	int sort_bits);
+void oracle_seg_scan(const void *in, void *out, const uint64_t *off, size_t nseg,
+	int in_type, int out_bytes);
+
 #endif

@@ -31,6 +31,8 @@ def lib():
         _lib.oracle_mt19937.argtypes = [C.c_uint32, P, SZ]
         _lib.oracle_splitmix64.argtypes = [C.c_uint64, P, SZ]
         _lib.oracle_radix_sort_u32_threaded.argtypes = [P, SZ, C.c_int, C.c_int]
+        _lib.oracle_seg_sort.argtypes = [P, P, SZ, C.c_int, C.c_int]
+        _lib.oracle_seg_scan.argtypes = [P, P, P, SZ, C.c_int, C.c_int]
     return _lib
 
 
@@ -53,6 +55,28 @@ def radix_sort_u32_threaded(keys, threads, bits=4):
     k = np.ascontiguousarray(keys, dtype=np.uint32)
     lib().oracle_radix_sort_u32_threaded(_p(k), k.size, threads, bits)
     return k
+
+
+def seg_sort(keys, offsets, sort_bits=None):
+    """Each segment [offsets[i], offsets[i+1]) sorted on its own (a copy)."""
+    k = np.ascontiguousarray(keys).copy()
+    off = np.ascontiguousarray(offsets, dtype=np.uint64)
+    kb = k.dtype.itemsize
+    lib().oracle_seg_sort(_p(k), _p(off), off.size - 1, kb,
+                          8 * kb if sort_bits is None else sort_bits)
+    return k
+
+
+def seg_scan(a, offsets, in_type, out_dtype, out_init=None):
+    """Per-segment exclusive scan; elements outside the segments keep
+    out_init (zeros by default)."""
+    a = np.ascontiguousarray(a)
+    off = np.ascontiguousarray(offsets, dtype=np.uint64)
+    out = np.zeros(a.size, dtype=out_dtype) if out_init is None else \
+        np.ascontiguousarray(out_init, dtype=out_dtype).copy()
+    lib().oracle_seg_scan(_p(a), _p(out), _p(off), off.size - 1, in_type,
+                          out.dtype.itemsize)
+    return out
 
 
 def bitonic_sort(a, clo_type):

@@ -77,3 +77,20 @@ def zipf_u32(n, seed, s=1.1, ranks=1 << 20):
 
 def low20_u64(n, seed=47):
     return splitmix64(seed, n) & np.uint64((1 << 20) - 1)
+
+
+def lognormal_lengths(nseg, mu, sigma, lo, hi, seed=48):
+    """Segment lengths: lognormal(mu, sigma) from splitmix64 uniforms
+    (Box-Muller), rounded and clipped to [lo, hi]."""
+    u = (splitmix64(seed, 2 * nseg) >> np.uint64(11)).astype(np.float64) / float(1 << 53)
+    u1 = np.maximum(u[0::2], 1e-300)
+    u2 = u[1::2]
+    z = np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+    ln = np.rint(np.exp(mu + sigma * z))
+    return np.clip(ln, lo, hi).astype(np.uint64)
+
+
+def offsets_of(lengths, start=0):
+    off = np.zeros(len(lengths) + 1, dtype=np.uint64)
+    off[1:] = np.cumsum(np.asarray(lengths, dtype=np.uint64))
+    return off + np.uint64(start)

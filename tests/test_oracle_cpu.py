@@ -201,3 +201,26 @@ def test_rng_fill_bits_and_maxint():
     mod, _ = oracle.rng_fill("lcg", st, 16, 3, 32, 1000)
     np.testing.assert_array_equal(top, full >> 24)
     np.testing.assert_array_equal(mod, full % 1000)
+
+
+def test_segmented_oracle_matches_per_segment_numpy():
+    from inputs import lognormal_lengths, offsets_of, keys_of_type
+    lens = lognormal_lengths(300, 5.0, 2.0, 0, 20000, seed=3)
+    off = offsets_of(lens, start=4)
+    n = int(off[-1]) + 5
+    a = keys_of_type(8, n, np.uint32)
+    got = oracle.seg_sort(a, off)
+    ref = a.copy()
+    for i in range(len(lens)):
+        lo, hi = int(off[i]), int(off[i + 1])
+        ref[lo:hi] = np.sort(a[lo:hi], kind="stable")
+    np.testing.assert_array_equal(got, ref)
+    v = (a >> np.uint32(24)).astype(np.uint32)
+    out = oracle.seg_scan(v, off, 5, np.uint64)
+    ref = np.zeros(n, np.uint64)
+    for i in range(len(lens)):
+        lo, hi = int(off[i]), int(off[i + 1])
+        if hi > lo:
+            c = np.cumsum(v[lo:hi].astype(np.uint64))
+            ref[lo:hi] = np.concatenate([np.zeros(1, np.uint64), c[:-1]])
+    np.testing.assert_array_equal(out, ref)
