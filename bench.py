@@ -381,7 +381,98 @@ def run_suite(clops, ctx, q, args, only=None):
             rng.destroy()
         out.destroy()
 
-    parts = {"abitonic": abitonic, "kv": kv, "scan": scan, "rng": rngs}
+    def segmented():
+        """50,000 segments, lognormal(7, 2) lengths clipped to [1, 2^22]
+        (splitmix64 seed 48): the batched segmented sort and scan (a plain
+        call and its CUDA-graph replay) against one plain call per segment."""
+        from inputs import lognormal_lengths, offsets_of
+        nseg = 50000 if only is None else min(50000, 1 << max(args.log2n - 13, 4))
+        lens = lognormal_lengths(nseg, 7.0, 2.0, 1, 1 << 22, seed=48)
+        off = offsets_of(lens)
+        n = int(off[-1])
+        keys = keys_u32_chunked(148, n)
+        vals = np.empty(n, dtype=np.uint32)
+        for o in range(0, n, 1 << 24):
+            m = min(1 << 24, n - o)
+            vals[o:o + m] = (splitmix64(248, m, offset=o) >> np.uint64(56)).astype(np.uint32)
+        pristine = clops.Buffer.from_array(ctx, q, keys)
+        b = clops.Buffer(ctx, keys.nbytes)
+        ob = clops.Buffer.from_array(ctx, q, off)
+        vi = clops.Buffer.from_array(ctx, q, vals)
+        vo = clops.Buffer(ctx, n * 8)
+        s = clops.Sorter(ctx, "satradix", clops.CLO_UINT)
+        sc = clops.Scanner(ctx, clops.CLO_UINT, clops.CLO_ULONG)
+        copy(pristine, b, keys.nbytes)
+        variant, vtimes = s.tune_segmented(q, b, ob, nseg)
+        ms_copy = timed(lambda: copy(pristine, b, keys.nbytes))
+        ms_sort = timed(lambda: (copy(pristine, b, keys.nbytes),
+                                 s.sort_segmented_device(q, b, ob, nseg))) - ms_copy
+        g = clops.Graph(q)
+        g.begin()
+        s.sort_segmented_device(q, b, ob, nseg)
+        g.end()
+        ms_graph = timed(lambda: (copy(pristine, b, keys.nbytes), g.launch())) - ms_copy
+        got = b.read(q, np.uint32, n)
+        big = lens > 8192
+        ok = True
+        for i in range(0, nseg, max(1, nseg // 64)):  # sampled segment checks
+            lo, hi = int(off[i]), int(off[i + 1])
+            ok = ok and bool(np.array_equal(got[lo:hi], np.sort(keys[lo:hi])))
+        ms_scan = timed(lambda: sc.scan_segmented_device(q, vi, vo, ob, nseg))
+        gs = clops.Graph(q)
+        gs.begin()
+        sc.scan_segmented_device(q, vi, vo, ob, nseg)
+        gs.end()
+        ms_scan_graph = timed(lambda: gs.launch())
+        # One plain call per segment on wrapped sub-buffers (what a caller
+        # without the segmented entry points does).
+        copy(pristine, b, keys.nbytes)
+        q.finish()
+        subs = []
+        for i in range(nseg):
+            lo, ln = int(off[i]), int(lens[i])
+            kb = clops.call(clops.lib.ccl_buffer_new_wrap, ctx.h, b.ptr + 4 * lo, 4 * ln)
+            vb = clops.call(clops.lib.ccl_buffer_new_wrap, ctx.h, vi.ptr + 4 * lo, 4 * ln)
+            ob_ = clops.call(clops.lib.ccl_buffer_new_wrap, ctx.h, vo.ptr + 8 * lo, 8 * ln)
+            subs.append((kb, vb, ob_, ln))
+        t0 = time.perf_counter()
+        for kb, _, _, ln in subs:
+            clops.call(clops.lib.clo_sort_with_device_data, s.h, q.h, None, kb, None, ln, 0)
+        q.finish()
+        ms_plain_sort = (time.perf_counter() - t0) * 1e3
+        q.gc()
+        t0 = time.perf_counter()
+        for _, vb, ob_, ln in subs:
+            clops.call(clops.lib.clo_scan_with_device_data, sc.h, q.h, None, vb, ob_, ln, 0)
+        q.finish()
+        ms_plain_scan = (time.perf_counter() - t0) * 1e3
+        q.gc()
+        for kb, vb, ob_, _ in subs:
+            for h in (kb, vb, ob_):
+                clops.lib.ccl_buffer_destroy(h)
+        model = 36.0 * float(lens[big].sum()) + 8.0 * float(lens[~big].sum())
+        best = min(ms_sort, ms_graph)
+        res["segmented_lognormal_50k"] = {
+            "segments": nseg, "elements": n,
+            "sort_ms": round(ms_sort, 3), "sort_graph_ms": round(ms_graph, 3),
+            "sort_Gkeys/s": round(n / (best * 1e-3) / 1e9, 3),
+            "sort_plain_per_segment_ms": round(ms_plain_sort, 1),
+            "sort_speedup_vs_plain": round(ms_plain_sort / best, 1),
+            "sort_model_bytes": "36 B/key in segments > 8192, 8 B/key in the others",
+            "sort_frac_of_peak": round(model / (best * 1e-3) / 1e9 / peak, 4),
+            "autotuner": {"chosen": variant, "variant_ms": [round(t, 3) for t in vtimes]},
+            "scan_ms": round(ms_scan, 3), "scan_graph_ms": round(ms_scan_graph, 3),
+            "scan_GB/s": round(12.0 * n / (min(ms_scan, ms_scan_graph) * 1e-3) / 1e9, 1),
+            "scan_frac_of_peak": round(12.0 * n / (min(ms_scan, ms_scan_graph) * 1e-3)
+                                       / 1e9 / peak, 4),
+            "scan_plain_per_segment_ms": round(ms_plain_scan, 1),
+            "scan_speedup_vs_plain": round(ms_plain_scan / min(ms_scan, ms_scan_graph), 1),
+            "result_check": "sampled segments sorted" if ok else "FAILED"}
+        for x in (g, gs, pristine, b, ob, vi, vo, s, sc):
+            x.destroy()
+
+    parts = {"abitonic": abitonic, "kv": kv, "scan": scan, "rng": rngs,
+             "segmented": segmented}
     for name, fn in parts.items():
         if only is None or only == name:
             fn()
@@ -458,7 +549,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--log2n", type=int, default=28)
     ap.add_argument("--no-suite", dest="suite", action="store_false")
-    ap.add_argument("--only", choices=["abitonic", "kv", "scan", "rng"],
+    ap.add_argument("--only", choices=["abitonic", "kv", "scan", "rng", "segmented"],
                     help="run one suite primitive alone (profiling cases)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
