@@ -54,6 +54,27 @@ class CloError(RuntimeError):
         self.message = message
 
 
+class ServeRequest(C.Structure):
+    """CloServeRequest (include/clo_serve.h)."""
+    _fields_ = [("op", C.c_int), ("type", C.c_int), ("sum_type", C.c_int),
+                ("n", C.c_size_t), ("draws", C.c_size_t), ("rng", C.c_int),
+                ("in_", C.c_void_p), ("out", C.c_void_p)]
+
+
+class ServeStats(C.Structure):
+    """CloServeStats (include/clo_serve.h)."""
+    _fields_ = [(f, C.c_uint64) for f in ("submitted", "admitted", "completed", "failed",
+                                         "rejected", "batches", "max_queued")] + \
+               [("budget_bytes", C.c_size_t), ("peak_bytes", C.c_size_t)] + \
+               [(f, C.c_double) for f in ("p50_ms", "p99_ms", "max_ms", "mean_ms",
+                                         "elements", "span_s")]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+SERVE_SORT, SERVE_SCAN, SERVE_RNG_FILL = 0, 1, 2
+
 P = C.c_void_p
 PERR = C.POINTER(C.POINTER(GError))
 SZ = C.c_size_t
@@ -172,6 +193,17 @@ _SIGS = {
     "clo_graph_launch": (U32, [P, P, PERR]),
     "clo_graph_get_num_nodes": (SZ, [P]),
     "clo_graph_destroy": (None, [P]),
+    "clo_serve_new": (P, [P, SZ, C.c_int, PERR]),
+    "clo_serve_submit": (U64, [P, C.POINTER(ServeRequest), PERR]),
+    "clo_serve_wait": (U32, [P, U64, C.POINTER(C.c_double), PERR]),
+    "clo_serve_drain": (U32, [P, PERR]),
+    "clo_serve_replay": (U32, [P, C.POINTER(ServeRequest), C.POINTER(C.c_double), SZ,
+                               C.POINTER(U64), PERR]),
+    "clo_serve_get_stats": (None, [P, C.POINTER(ServeStats)]),
+    "clo_serve_reset_stats": (None, [P]),
+    "clo_serve_destroy": (None, [P]),
+    "clo_serve_footprint": (SZ, [C.POINTER(ServeRequest)]),
+    "clo_serve_select": (SZ, [C.POINTER(ServeRequest), SZ, SZ, SZ, SZ, SZ, C.POINTER(SZ)]),
     "clo_gb300_timing_enable": (None, [C.c_int]),
     "clo_gb300_timing_reset": (None, []),
     "clo_gb300_timing_get": (C.c_int, [C.c_char_p, C.POINTER(C.c_double),
@@ -470,3 +502,51 @@ def kernel_timing(name):
     if not lib.clo_gb300_timing_get(name.encode(), C.byref(ms), C.byref(by), C.byref(n)):
         return 0.0, 0.0, 0
     return ms.value, by.value, int(n.value)
+
+
+class Server:
+    """CloServer: continuous batching of host-data requests on one GPU."""
+
+    def __init__(self, ctx, budget_bytes, streams=4):
+        self.h = call(lib.clo_serve_new, ctx.h, budget_bytes, streams)
+
+    @staticmethod
+    def request(op, type_=0, sum_type=0, n=0, draws=0, rng=0, inp=None, out=None):
+        """inp / out: numpy arrays or raw addresses."""
+        def addr(x):
+            if x is None:
+                return None
+            return x.ctypes.data if isinstance(x, np.ndarray) else int(x)
+        return ServeRequest(op, type_, sum_type, n, draws, rng, addr(inp), addr(out))
+
+    def submit(self, req):
+        return call(lib.clo_serve_submit, self.h, C.byref(req))
+
+    def wait(self, ticket):
+        ms = C.c_double()
+        call(lib.clo_serve_wait, self.h, ticket, C.byref(ms))
+        return ms.value
+
+    def drain(self):
+        call(lib.clo_serve_drain, self.h)
+
+    def replay(self, reqs, arrival_s):
+        n = len(reqs)
+        arr = (ServeRequest * n)(*reqs)
+        ts = (C.c_double * n)(*arrival_s)
+        tickets = (U64 * n)()
+        call(lib.clo_serve_replay, self.h, arr, ts, n, tickets)
+        return list(tickets)
+
+    def stats(self):
+        st = ServeStats()
+        lib.clo_serve_get_stats(self.h, C.byref(st))
+        return st.as_dict()
+
+    def reset_stats(self):
+        lib.clo_serve_reset_stats(self.h)
+
+    def destroy(self):
+        if self.h:
+            lib.clo_serve_destroy(self.h)
+            self.h = None

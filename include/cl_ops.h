@@ -10,5 +10,6 @@
 #include "clo_scan_abstract.h"
 #include "clo_rng.h"
 #include "clo_gb300.h"
+#include "clo_serve.h"
 
 #endif /* CL_OPS_H */
