@@ -471,8 +471,119 @@ def run_suite(clops, ctx, q, args, only=None):
         for x in (g, gs, pristine, b, ob, vi, vo, s, sc):
             x.destroy()
 
+    def serve():
+        """Open-loop serving: Poisson arrivals at 20k requests/s (seed 49),
+        60 % sort / 30 % scan / 10 % random fill, n log-uniform in
+        [2^10, 2^26], uint / ulong 50/50, 120 GB admission budget; host
+        data in page-locked pools (requests read and write slices of them).
+        Against the same requests served by serial plain host-data calls."""
+        dur = args.serve_seconds
+        rate = 20000.0
+        u = splitmix64(49, 1 << 22)
+        with np.errstate(divide="ignore"):
+            gaps = -np.log(np.maximum((u[0::8] >> np.uint64(11)).astype(np.float64)
+                                      / float(1 << 53), 1e-300)) / rate
+        arrivals = np.cumsum(gaps)
+        count = int(np.searchsorted(arrivals, dur))
+        arrivals = arrivals[:count]
+        kind = (u[1::8][:count] % np.uint64(10)).astype(np.int64)
+        logn = 10.0 + 16.0 * (u[2::8][:count] >> np.uint64(11)).astype(np.float64) / float(1 << 53)
+        nreq = np.minimum(np.exp2(logn).astype(np.int64), 1 << 26)
+        wide = (u[3::8][:count] & np.uint64(1)).astype(bool)
+        pos_in = u[4::8][:count]
+        pos_out = u[5::8][:count]
+        pool_bytes = 4 << 30
+        hin = clops.lib.clo_host_alloc(pool_bytes, None)
+        hout = clops.lib.clo_host_alloc(pool_bytes, None)
+        pin = np.ctypeslib.as_array((clops.C.c_uint8 * pool_bytes).from_address(hin))
+        block = splitmix64(149, 1 << 26).view(np.uint8)  # 512 MiB, repeated
+        for o in range(0, pool_bytes, block.size):
+            pin[o:o + block.size] = block
+        reqs = []
+        elems = 0.0
+        for i in range(count):
+            n = int(nreq[i])
+            if kind[i] < 6:
+                code, eb = (clops.CLO_ULONG, 8) if wide[i] else (clops.CLO_UINT, 4)
+                ib, ob, op, sc_code, st, dr = eb, eb, clops.SERVE_SORT, 0, n, 0
+            elif kind[i] < 9:
+                code, eb = (clops.CLO_ULONG, 8) if wide[i] else (clops.CLO_UINT, 4)
+                ib, ob, op, sc_code, st, dr = eb, 8, clops.SERVE_SCAN, clops.CLO_ULONG, n, 0
+            else:
+                g = i % 5
+                st, dr = max(1, n // 16), 16
+                ib, ob = clops.RNG_SEED_SIZE[clops.RNG_NAMES[g]], 4 * dr
+                code, op, sc_code = g, clops.SERVE_RNG_FILL, 0
+            span_in, span_out = st * ib, st * ob
+            a = hin + int(pos_in[i] % np.uint64((pool_bytes - span_in) // 16)) * 16
+            b = hout + int(pos_out[i] % np.uint64((pool_bytes - span_out) // 16)) * 16
+            if op == clops.SERVE_RNG_FILL:
+                reqs.append(clops.Server.request(op, 0, 0, st, dr, code, inp=a, out=b))
+                elems += st * dr
+            else:
+                reqs.append(clops.Server.request(op, code, sc_code, n, inp=a, out=b))
+                elems += n
+        srv = clops.Server(ctx, 120 << 30, streams=4)
+        # warm-up: a few requests of each kind
+        for r in reqs[:64]:
+            srv.submit(r)
+        srv.drain()
+        srv.reset_stats()
+        srv.replay(reqs, list(arrivals))
+        srv.drain()
+        st_ = srv.stats()
+        srv.destroy()
+        # Serial plain calls on the first requests (about 2 s of work).
+        sorters = {clops.CLO_UINT: clops.Sorter(ctx, "satradix", clops.CLO_UINT),
+                   clops.CLO_ULONG: clops.Sorter(ctx, "satradix", clops.CLO_ULONG)}
+        scanners = {clops.CLO_UINT: clops.Scanner(ctx, clops.CLO_UINT, clops.CLO_ULONG),
+                    clops.CLO_ULONG: clops.Scanner(ctx, clops.CLO_ULONG, clops.CLO_ULONG)}
+        done_el, t0 = 0.0, time.perf_counter()
+        for r in reqs:
+            if r.op == clops.SERVE_SORT:
+                clops.call(clops.lib.clo_sort_with_host_data, sorters[r.type].h, q.h, None,
+                           r.in_, r.out, r.n, 0)
+                done_el += r.n
+            elif r.op == clops.SERVE_SCAN:
+                clops.call(clops.lib.clo_scan_with_host_data, scanners[r.type].h, q.h, None,
+                           r.in_, r.out, r.n, 0)
+                done_el += r.n
+            else:
+                name = clops.RNG_NAMES[r.rng]
+                seeds = np.ctypeslib.as_array((clops.C.c_uint8 * (r.n * clops.RNG_SEED_SIZE[name]))
+                                              .from_address(r.in_))
+                rng = clops.Rng(ctx, q, name, clops.CLO_RNG_SEED_EXT_HOST, r.n, seeds=seeds)
+                ob_ = clops.Buffer(ctx, r.n * r.draws * 4)
+                clops.wait(rng.fill(q, ob_, r.draws))
+                clops.call(clops.lib.ccl_buffer_enqueue_read, ob_.h, q.h, 1, 0,
+                           r.n * r.draws * 4, r.out, None)
+                ob_.destroy()
+                rng.destroy()
+                done_el += r.n * r.draws
+            if time.perf_counter() - t0 > 2.0:
+                break
+        serial = done_el / (time.perf_counter() - t0)
+        for x in list(sorters.values()) + list(scanners.values()):
+            x.destroy()
+        del pin
+        clops.lib.clo_host_free(hin)
+        clops.lib.clo_host_free(hout)
+        agg = st_["elements"] / st_["span_s"] if st_["span_s"] else 0.0
+        res["serve_poisson_20k"] = {
+            "open_loop_s": dur, "offered_req_per_s": rate, "requests": count,
+            "offered_Gelem_per_s": round(elems / dur / 1e9, 2),
+            "submitted": st_["submitted"], "admitted": st_["admitted"],
+            "completed": st_["completed"], "rejected": st_["rejected"],
+            "batches": st_["batches"], "max_queued": st_["max_queued"],
+            "peak_budget_GB": round(st_["peak_bytes"] / 1e9, 2), "budget_GB": 120 * 1.073741824,
+            "p50_ms": round(st_["p50_ms"], 2), "p99_ms": round(st_["p99_ms"], 2),
+            "mean_ms": round(st_["mean_ms"], 2), "span_s": round(st_["span_s"], 3),
+            "aggregate_Gelem_per_s": round(agg / 1e9, 3),
+            "serial_plain_Gelem_per_s": round(serial / 1e9, 3),
+            "speedup_vs_serial_plain": round(agg / serial, 2) if serial else None}
+
     parts = {"abitonic": abitonic, "kv": kv, "scan": scan, "rng": rngs,
-             "segmented": segmented}
+             "segmented": segmented, "serve": serve}
     for name, fn in parts.items():
         if only is None or only == name:
             fn()
@@ -549,7 +660,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--log2n", type=int, default=28)
     ap.add_argument("--no-suite", dest="suite", action="store_false")
-    ap.add_argument("--only", choices=["abitonic", "kv", "scan", "rng", "segmented"],
+    ap.add_argument("--serve-seconds", type=float, default=1.0,
+                    help="open-loop duration of the serving workload")
+    ap.add_argument("--only", choices=["abitonic", "kv", "scan", "rng", "segmented", "serve"],
                     help="run one suite primitive alone (profiling cases)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
