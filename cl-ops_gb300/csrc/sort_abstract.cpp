@@ -6,9 +6,11 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <string>
 
 #include "clo_internal.h"
+#include "jit.h"
 
 using clo::cuda_ok;
 using clo::set_error;
@@ -20,6 +22,9 @@ struct clo_sort {
 	CloType elem_type;
 	CloType key_type;
 	void *data;
+	// Kernels built by NVRTC for custom compare/get_key macros (or a key
+	// type other than the element type); null for the compiled-in path.
+	std::shared_ptr<clo::JitSort> jit;
 };
 
 namespace {
@@ -91,6 +96,95 @@ CCLBuffer *target_buffer(CloSort *s, CCLQueue *q, CCLBuffer *in,
 			cudaMemcpyDeviceToDevice, q->stream), err, "sort copy"))
 		return nullptr;
 	return out;
+}
+
+// ====================================================== built kernels
+// Sorts `numel` elements of `src` into `dst` (which may be `src`) with the
+// sorter's NVRTC kernels:
+// - satradix: keys from get_key with their indices, the compiled-in stable
+//   radix sort of (key, index) by the key's low 8 * min(element, key)
+//   bytes bits (the passes of clo_sort_satradix.c:167-169 over the key of
+//   clo_sort_satradix.cl:58,140), then a gather;
+// - bitonic: the reference network (clo_sort_sbitonic.cl:38-69), one step
+//   per launch, over the next power of two with padding flags;
+// - gselect: rank by counting (clo_sort_gselect.cl:38-57), out of place.
+enum JitAlgo { JIT_RADIX, JIT_BITONIC, JIT_GSELECT };
+
+bool jit_sort(CloSort *s, CCLQueue *q, void *src, void *dst, size_t numel,
+	JitAlgo algo, GError **err) {
+	clo::JitSort &j = *s->jit;
+	cudaStream_t st = q->stream;
+	const int sms = s->ctx->sm_count;
+	const size_t eb = clo_type_sizeof(s->elem_type), kb = clo_type_sizeof(s->key_type);
+	unsigned long long n = numel;
+	if (numel == 0) return true;
+	if (algo == JIT_GSELECT || numel == 1) {
+		if (numel == 1 || src == dst) {
+			void *tmp = clo::tmp_alloc(s->ctx, numel * eb, st, err);
+			if (!tmp) return false;
+			bool ok = true;
+			if (numel == 1) {
+				ok = cuda_ok(cudaMemcpyAsync(tmp, src, eb, cudaMemcpyDeviceToDevice, st),
+					err, "copy");
+			} else {
+				void *args[] = {&src, &tmp, &n};
+				ok = cuda_ok(clo::jit_launch(j.gselect, numel, args, st, sms), err, "gselect");
+			}
+			ok = ok && cuda_ok(cudaMemcpyAsync(dst, tmp, numel * eb,
+				cudaMemcpyDeviceToDevice, st), err, "copy back");
+			clo::tmp_free(tmp, st);
+			return ok;
+		}
+		void *args[] = {&src, &dst, &n};
+		return cuda_ok(clo::jit_launch(j.gselect, numel, args, st, sms), err, "gselect");
+	}
+	if (algo == JIT_RADIX) {
+		if (numel >= (1ull << 32)) {
+			set_error(err, CLO_ERROR_ARGS, "Custom get_key sorts take fewer than 2^32 elements");
+			return false;
+		}
+		const size_t off_idx = (numel * kb + 255) / 256 * 256;
+		const size_t off_out = off_idx + (numel * 4 + 255) / 256 * 256;
+		char *tmp = (char *)clo::tmp_alloc(s->ctx, off_out + numel * eb, st, err);
+		if (!tmp) return false;
+		void *keys = tmp, *idx = tmp + off_idx, *sorted = tmp + off_out;
+		void *a1[] = {&src, &keys, &idx, &n};
+		bool ok = cuda_ok(clo::jit_launch(j.keys, numel, a1, st, sms), err, "get_key");
+		const int bits = (int)(8 * (eb < kb ? eb : kb));
+		ok = ok && clo::radix_sort(keys, idx, numel, (int)kb, 4, bits, s->ctx, st,
+			!clo::stream_capturing(st), err) == cudaSuccess;
+		void *a2[] = {&src, &idx, &sorted, &n};
+		ok = ok && cuda_ok(clo::jit_launch(j.gather, numel, a2, st, sms), err, "gather");
+		ok = ok && cuda_ok(cudaMemcpyAsync(dst, sorted, numel * eb,
+			cudaMemcpyDeviceToDevice, st), err, "copy back");
+		clo::tmp_free(tmp, st);
+		return ok;
+	}
+	size_t N = 1;
+	while (N < numel) N <<= 1;
+	const size_t off_pad = (N * eb + 255) / 256 * 256;
+	char *tmp = (char *)clo::tmp_alloc(s->ctx, off_pad + N, st, err);
+	if (!tmp) return false;
+	void *data = tmp;
+	void *pad = tmp + off_pad;
+	bool ok = cuda_ok(cudaMemcpyAsync(data, src, numel * eb, cudaMemcpyDeviceToDevice, st),
+		err, "copy");
+	ok = ok && cuda_ok(cudaMemsetAsync(pad, 0, numel, st), err, "pad");
+	if (N > numel) ok = ok && cuda_ok(cudaMemsetAsync((char *)pad + numel, 1, N - numel, st),
+		err, "pad");
+	unsigned long long half = N / 2;
+	unsigned stages = 0;
+	while ((1ull << stages) < N) ++stages;
+	for (unsigned stage = 1; stage <= stages && ok; ++stage)
+		for (unsigned step = stage; step > 0 && ok; --step) {
+			void *args[] = {&data, &pad, &stage, &step, &half};
+			ok = cuda_ok(clo::jit_launch(j.bitonic_step, half, args, st, sms), err,
+				"bitonic step");
+		}
+	ok = ok && cuda_ok(cudaMemcpyAsync(dst, data, numel * eb, cudaMemcpyDeviceToDevice, st),
+		err, "copy back");
+	clo::tmp_free(tmp, st);
+	return ok;
 }
 
 // ============================================================ satradix
@@ -197,6 +291,11 @@ CCLEvent *satradix_sort(CloSort *s, CCLQueue *cq_exec, CCLQueue *cq_comm,
 	ccl_event *ev = clo::event_begin(cq_exec, "satradix");
 	CCLBuffer *tgt = target_buffer(s, cq_exec, in, out, numel, err);
 	if (!tgt) return nullptr;
+	if (s->jit) {
+		if (!jit_sort(s, cq_exec, tgt->ptr, tgt->ptr, numel, JIT_RADIX, err)) return nullptr;
+		clo::event_end(ev);
+		return ev;
+	}
 	int kb = (int)clo_type_sizeof(s->elem_type);
 	bool skip = !clo::stream_capturing(cq_exec->stream);
 	if (clo::radix_sort(tgt->ptr, nullptr, numel, kb, 0, satradix_sort_bits(s),
@@ -244,12 +343,6 @@ struct AbitonicData {
 const char *sbitonic_init(CloSort *s, const char *options, GError **err) {
 	(void)options;
 	s->data = nullptr;
-	if (s->key_type != s->elem_type) {
-		set_error(err, CLO_ERROR_ARGS,
-			"sbitonic: a key type different from the element type needs a "
-			"get_key snippet, which the compiled-in kernels do not take");
-		return nullptr;
-	}
 	return "sm_103a:sbitonic(one network step per launch)";
 }
 
@@ -294,12 +387,6 @@ const char *abitonic_init(CloSort *s, const char *options, GError **err) {
 			d->min_ps, d->max_ps);
 		return nullptr;
 	}
-	if (s->key_type != s->elem_type) {
-		set_error(err, CLO_ERROR_ARGS,
-			"abitonic: a key type different from the element type needs a "
-			"get_key snippet, which the compiled-in kernels do not take");
-		return nullptr;
-	}
 	return "sm_103a:abitonic(shared-memory tiles + register passes)";
 }
 
@@ -330,6 +417,11 @@ CCLEvent *bitonic_sort_common(CloSort *s, CCLQueue *q, CCLBuffer *in,
 	// abitonic's maxps bounds the steps grouped per global pass and maxsfs
 	// the largest step finished in shared memory (clo_sort_abitonic.c:
 	// 155-157); neither changes the result.
+	if (s->jit) {
+		if (!jit_sort(s, q, tgt->ptr, tgt->ptr, numel, JIT_BITONIC, err)) return nullptr;
+		clo::event_end(ev);
+		return ev;
+	}
 	AbitonicData *d = (AbitonicData *)s->data;
 	cudaError_t e = simple
 		? clo::bitonic_sort_simple(tgt->ptr, numel, s->elem_type, s->ctx,
@@ -393,12 +485,6 @@ size_t abitonic_localmem(CloSort *s, cl_uint i, size_t, size_t,
 const char *gselect_init(CloSort *s, const char *options, GError **err) {
 	(void)options;
 	s->data = nullptr;
-	if (s->key_type != s->elem_type) {
-		set_error(err, CLO_ERROR_ARGS,
-			"gselect: a key type different from the element type needs a "
-			"get_key snippet, which the compiled-in kernels do not take");
-		return nullptr;
-	}
 	return "sm_103a:gselect(rank by counting)";
 }
 
@@ -412,6 +498,13 @@ CCLEvent *gselect_sort(CloSort *s, CCLQueue *q, CCLQueue *cq_comm,
 	if (!check_numel(s, in, numel, err)) return nullptr;
 	ccl_event *ev = clo::event_begin(q, "gselect");
 	size_t bytes = numel * clo_type_sizeof(s->elem_type);
+	if (s->jit) {
+		CCLBuffer *dst = out != nullptr ? out : in;
+		if (out != nullptr && out != in && !check_numel(s, out, numel, err)) return nullptr;
+		if (!jit_sort(s, q, in->ptr, dst->ptr, numel, JIT_GSELECT, err)) return nullptr;
+		clo::event_end(ev);
+		return ev;
+	}
 	if (out != nullptr && out != in) {
 		if (!check_numel(s, out, numel, err)) return nullptr;
 		if (clo::gselect_sort(in->ptr, out->ptr, numel, s->elem_type, nullptr,
@@ -504,16 +597,22 @@ CloSort *clo_sort_new(const char *type, const char *options, CCLContext *ctx,
 		return nullptr;
 	}
 	// satradix ignores the compare macro (it always orders by the key's
-	// unsigned bits); the other implementations run the default compare.
-	bool is_radix = def == &clo_sort_satradix_def;
-	if ((!is_radix && !compare_is_default(compare)) ||
-		!get_key_is_default(get_key)) {
-		set_error(err, CLO_ERROR_ARGS,
-			"Custom compare/get_key snippets are not supported by the "
-			"compiled-in sm_103a kernels (compare='%s', get_key='%s')",
-			compare ? compare : "", get_key ? get_key : "");
-		clo_sort_destroy(s);
-		return nullptr;
+	// unsigned bits, clo_sort_satradix.cl:58,140) and handles a narrower or
+	// wider key type through its sort bits; it needs built kernels only for
+	// a custom get_key. The other sorters use them for any custom macro or
+	// a key type other than the element type.
+	const bool is_radix = def == &clo_sort_satradix_def;
+	const bool custom = is_radix ? !get_key_is_default(get_key)
+		: (!compare_is_default(compare) || !get_key_is_default(get_key) ||
+			s->key_type != s->elem_type);
+	if (custom) {
+		s->jit = clo::jit_sort_get(s->elem_type, s->key_type, compare, get_key,
+			ctx->ordinal, &e2);
+		if (!s->jit) {
+			clo::propagate_error(err, e2);
+			clo_sort_destroy(s);
+			return nullptr;
+		}
 	}
 	s->prg = new ccl_program();
 	char macros[512];
@@ -522,7 +621,7 @@ CloSort *clo_sort_new(const char *type, const char *options, CCLContext *ctx,
 		"#define CLO_SORT_COMPARE(a, b) %s\n#define CLO_SORT_KEY_GET(x) %s\n",
 		clo_type_get_name(s->elem_type), clo_type_get_name(s->key_type),
 		compare ? compare : "((a) > (b))", get_key ? get_key : "(x)");
-	s->prg->src = std::string(macros) + src;
+	s->prg->src = s->jit ? s->jit->source : std::string(macros) + src;
 	s->prg->opts = compiler_opts ? compiler_opts : "";
 	clo::wrapper_created();
 	return s;
@@ -665,6 +764,11 @@ CCLEvent *clo_sort_kv_with_device_data(CloSort *sorter, CCLQueue *q,
 		set_error(err, CLO_ERROR_ARGS, "Value type must be 4 or 8 bytes wide");
 		return nullptr;
 	}
+	if (sorter->jit) {
+		set_error(err, CLO_ERROR_ARGS,
+			"Key-value sorting takes the default compare and get_key only");
+		return nullptr;
+	}
 	if (!check_numel(sorter, keys, numel, err)) return nullptr;
 	if (!values || values->size < numel * vb) {
 		set_error(err, CLO_ERROR_ARGS, "Value buffer too small");
@@ -765,6 +869,11 @@ bool seg_args_ok(CloSort *sorter, CCLQueue *q, const char *what, GError **err) {
 		set_error(err, CLO_ERROR_ARGS,
 			"Segmented sorting is implemented for the satradix sorter (stable, "
 			"unsigned key order), not '%s'", sorter->impl_def.name);
+		return false;
+	}
+	if (sorter->jit) {
+		set_error(err, CLO_ERROR_ARGS,
+			"Segmented sorting takes the default get_key only");
 		return false;
 	}
 	return true;

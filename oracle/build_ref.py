@@ -43,6 +43,14 @@ RNGS = ["lcg", "xorshift64", "xorshift128", "mwc64x", "parkmiller", "tauslcg"]
 HASHES = ["x", "(x * 3 + 1)", "KNUTH(x)", "XS1(x)", "x = x << 2",
           "x ^= 0xABCDEF; x = x * 3 + (x >> 7) % 11"]
 SATRADIX_BITS = 4  # the reference's default radix 16
+# Sorters built with custom macros: (element code, key code, compare,
+# get_key), as a caller of clo_sort_new would pass them.
+CUSTOM = [(5, 5, "((a) < (b))", "(x)"),
+          (4, 4, "((a) < (b))", "(x)"),
+          (5, 5, "((a) > (b))", "((x) & 0xF)"),
+          (5, 5, "((a) < (b))", "((x) >> 4)"),
+          (7, 5, "((a) > (b))", "(x)"),
+          (9, 9, "((a) < (b))", "(x)")]
 
 
 def ref_root():
@@ -66,19 +74,21 @@ def cl(rel):
     return to_cxx((ref_root() / rel).read_text())
 
 
-def unit_sort(code):
+def unit_sort(code, key=None, compare="((a) > (b))", get_key="(x)", tag=None):
     cname, hname = TYPES[code]
+    kname = TYPES[code if key is None else key][1]
+    tag = str(code) if tag is None else tag
     scan = cl("src/cl_ops/scan/clo_scan_blelloch.cl")
     srcs = [cl("src/cl_ops/sort/clo_sort_sbitonic.cl"), cl("src/cl_ops/sort/clo_sort_gselect.cl")]
     if code in SORT_INT:
         srcs.insert(0, cl("src/cl_ops/sort/clo_sort_satradix.cl"))
     body = [
-        '#include "clc_host.h"', "#include <vector>", f"namespace ns_sort_{code} {{",
+        '#include "clc_host.h"', "#include <vector>", f"namespace ns_sort_{tag} {{",
         "namespace scan {", "#define CLO_SCAN_ELEM_TYPE uint", "#define CLO_SCAN_SUM_TYPE uint",
         scan, '#include "drv_scan.inc"', "#undef CLO_SCAN_ELEM_TYPE", "#undef CLO_SCAN_SUM_TYPE",
         "}",
-        f"#define CLO_SORT_ELEM_TYPE {hname}", f"#define CLO_SORT_KEY_TYPE {hname}",
-        "#define CLO_SORT_COMPARE(a, b) ((a) > (b))", "#define CLO_SORT_KEY_GET(x) (x)",
+        f"#define CLO_SORT_ELEM_TYPE {hname}", f"#define CLO_SORT_KEY_TYPE {kname}",
+        f"#define CLO_SORT_COMPARE(a, b) {compare}", f"#define CLO_SORT_KEY_GET(x) {get_key}",
         f"#define CLO_SORT_NUM_BITS {SATRADIX_BITS}",
     ] + srcs
     if code in SORT_INT:
@@ -86,8 +96,8 @@ def unit_sort(code):
     else:
         body.append('#define CLC_NO_SATRADIX\n#include "drv_sort.inc"')
     body += ["}",
-             f'extern "C" int ref_sort_{code}(int algo, void *data, size_t n, size_t lws) {{',
-             f"  using namespace ns_sort_{code};"]
+             f'extern "C" int ref_sort_{tag}(int algo, void *data, size_t n, size_t lws) {{',
+             f"  using namespace ns_sort_{tag};"]
     if code in SORT_INT:
         body.append("  if (algo == 0) return drive_satradix(data, n, lws) ? 0 : -1;")
     body += ["  if (algo == 1) return drive_sbitonic(data, n, lws) ? 0 : -1;",
@@ -132,6 +142,8 @@ def unit_rng(gi, name):
 
 def units():
     u = {f"sort_{c}": unit_sort(c) for c in SORT_ALL}
+    u.update({f"sort_c{i}": unit_sort(e, k, cmp, key, tag=f"c{i}")
+              for i, (e, k, cmp, key) in enumerate(CUSTOM)})
     u.update({f"scan_{e}_{s}": unit_scan(e, s) for e, s in SCAN_PAIRS})
     u.update({f"rng_{i}": unit_rng(i, n) for i, n in enumerate(RNGS)})
     return u

@@ -130,3 +130,73 @@ def splitmix64(seed, n):
     out = np.empty(n, dtype=np.uint64)
     lib().oracle_splitmix64(seed, _p(out), n)
     return out
+
+
+# ---- custom compare / get_key (small sizes, numpy) ----------------------
+# The reference builds its kernels with CLO_SORT_COMPARE(a, b) and
+# CLO_SORT_KEY_GET(x) macros (src/cl_ops/sort/clo_sort_abstract.c:141-179);
+# here they are numpy callables: key_fn(elements) -> keys (already of the
+# key type) and cmp_fn(k1, k2) -> bool array.
+
+def custom_satradix(a, key_fn, key_dtype):
+    """Stable sort by the key's low 8*min(element, key) bytes bits, as the
+    unsigned pattern (clo_sort_satradix.c:167-169, clo_sort_satradix.cl:58,140)."""
+    a = np.ascontiguousarray(a)
+    k = np.ascontiguousarray(key_fn(a)).astype(key_dtype)
+    kb = np.dtype(key_dtype).itemsize
+    bits = 8 * min(a.dtype.itemsize, kb)
+    u = k.view(f"u{kb}").astype(np.uint64)
+    if bits < 64:
+        u = u & np.uint64((1 << bits) - 1)
+    return a[np.argsort(u, kind="stable")]
+
+
+def custom_bitonic(a, key_fn, cmp_fn):
+    """The reference network (clo_sort_sbitonic.c:86-108,
+    clo_sort_sbitonic.cl:38-69) over the next power of two; positions past
+    the elements compare greater than every element and equal to each
+    other."""
+    a = np.ascontiguousarray(a)
+    n = a.size
+    if n < 2:
+        return a.copy()
+    N = 1
+    while N < n:
+        N <<= 1
+    d = np.concatenate([a, np.zeros(N - n, dtype=a.dtype)])
+    pad = np.concatenate([np.zeros(n, bool), np.ones(N - n, bool)])
+    g = np.arange(N // 2, dtype=np.int64)
+    stages = N.bit_length() - 1
+    for stage in range(1, stages + 1):
+        desc = ((g >> (stage - 1)) & 1).astype(bool)
+        for step in range(stage, 0, -1):
+            s = 1 << (step - 1)
+            i1 = g + (g // s) * s
+            i2 = i1 + s
+            p1, p2 = pad[i1], pad[i2]
+            real = ~(p1 | p2)
+            gt = p1 & ~p2
+            if real.any():
+                gt = gt.copy()
+                gt[real] = np.asarray(cmp_fn(key_fn(d[i1[real]]), key_fn(d[i2[real]])), bool)
+            sw = gt ^ desc
+            x1, x2 = d[i1[sw]].copy(), d[i2[sw]].copy()
+            d[i1[sw]], d[i2[sw]] = x2, x1
+            q1, q2 = pad[i1[sw]].copy(), pad[i2[sw]].copy()
+            pad[i1[sw]], pad[i2[sw]] = q2, q1
+    return d[:n]
+
+
+def custom_gselect(a, key_fn, cmp_fn):
+    """out[#{i : COMPARE(k_g, k_i) or (k_i == k_g and i < g)}] = a[g]
+    (clo_sort_gselect.cl:38-57)."""
+    a = np.ascontiguousarray(a)
+    n = a.size
+    k = key_fn(a)
+    out = np.empty_like(a)
+    idx = np.arange(n)
+    for g in range(n):
+        c = np.asarray(cmp_fn(np.full(n, k[g]), k), bool)
+        pos = int(np.count_nonzero(c | ((k == k[g]) & (idx < g))))
+        out[pos] = a[g]
+    return out

@@ -40,10 +40,14 @@ def _check(rc, what):
         raise RuntimeError(f"reference kernel run failed ({what}, rc={rc})")
 
 
-def sort(a, code, algo, lws=256):
-    """algo: 'satradix' (radix 16), 'sbitonic' or 'gselect'; returns a sorted copy."""
+CUSTOM = build_ref.CUSTOM
+
+
+def sort(a, code, algo, lws=256, custom=None):
+    """algo: 'satradix' (radix 16), 'sbitonic' or 'gselect'; returns a sorted
+    copy. custom: index into CUSTOM for a sorter built with those macros."""
     d = np.ascontiguousarray(a).copy()
-    f = getattr(lib(), f"ref_sort_{code}")
+    f = getattr(lib(), f"ref_sort_{code}" if custom is None else f"ref_sort_c{custom}")
     f.argtypes = [C.c_int, C.c_void_p, C.c_size_t, C.c_size_t]
     _check(f({"satradix": 0, "sbitonic": 1, "gselect": 2}[algo], _p(d), d.size, lws),
            algo)

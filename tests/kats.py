@@ -68,3 +68,19 @@ def state_bytes(name, s):
     if name == "tauslcg":
         return np.array([s, s], dtype=np.uint64).view(np.uint8)
     raise ValueError(name)
+
+
+# numpy forms of the custom macros of the known answers (oracle/build_ref.py
+# CUSTOM, same order): custom index -> (key_fn, cmp_fn, key dtype).
+def _low32(x):
+    return np.asarray(x).astype(np.uint32)
+
+
+CUSTOM_FNS = {
+    0: (lambda x: x, lambda a, b: a < b, np.uint32),
+    1: (lambda x: x, lambda a, b: a < b, np.int32),
+    2: (lambda x: x & np.uint32(0xF), lambda a, b: a > b, np.uint32),
+    3: (lambda x: x >> np.uint32(4), lambda a, b: a < b, np.uint32),
+    4: (_low32, lambda a, b: a > b, np.uint32),
+    5: (lambda x: x, lambda a, b: a < b, np.float32),
+}

@@ -51,3 +51,17 @@ def test_oracle_rng_draws_match_reference(k):
     out, st2 = oracle.rng_fill(k["rng"], st, k["count"], k["draws"], k["bits"] or 32,
                                k["maxint"])
     assert digest(out) == k["sha256"] and digest(st2) == k["states_sha256"]
+
+
+@pytest.mark.parametrize("k", select("sort_custom"), ids=lambda k: f"c{k['custom']}-{k['algo']}")
+def test_oracle_custom_macros_match_reference(k):
+    from kats import CUSTOM_FNS
+    key_fn, cmp_fn, kdt = CUSTOM_FNS[k["custom"]]
+    a = sort_input(k)
+    if k["algo"] == "satradix":
+        out = oracle.custom_satradix(a, key_fn, kdt)
+    elif k["algo"] == "sbitonic":
+        out = oracle.custom_bitonic(a, key_fn, cmp_fn)
+    else:
+        out = oracle.custom_gselect(a, key_fn, cmp_fn)
+    assert digest(out) == k["sha256"]

@@ -58,3 +58,17 @@ def test_cuda_rng_draws_match_reference(clops, ctx, queue, k):
     assert digest(rng.states(queue)) == k["states_sha256"]
     out.destroy()
     rng.destroy()
+
+
+@pytest.mark.parametrize("k", select("sort_custom"), ids=lambda k: f"c{k['custom']}-{k['algo']}")
+def test_cuda_custom_macros_match_reference(clops, ctx, queue, k):
+    a = sort_input(k)
+    algos = ["sbitonic", "abitonic"] if k["algo"] == "sbitonic" else [k["algo"]]
+    for algo in algos:
+        s = clops.Sorter(ctx, algo, k["code"], key_type=k["key"], compare=k["compare"],
+                         get_key=k["get_key"])
+        b = clops.Buffer.from_array(ctx, queue, a)
+        clops.wait(s.sort_device(queue, b, a.size))
+        assert digest(b.read(queue, a.dtype, a.size)) == k["sha256"], algo
+        b.destroy()
+        s.destroy()
