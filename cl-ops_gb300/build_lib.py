@@ -93,9 +93,34 @@ def build(force: bool = False, verbose: bool = False) -> pathlib.Path:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    build_cli(force)
     if verbose:
         print(f"built {LIB}")
     return LIB
+
+
+CLI = HERE / "cli"
+BIN = HERE / "bin"
+
+
+def build_cli(force: bool = False) -> None:
+    """The benchmark programs (cli/*.c) against libclops.so, into bin/."""
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        return
+    BIN.mkdir(exist_ok=True)
+    hdr = max(p.stat().st_mtime for p in list(CLI.glob("*.h")) + list(INCLUDE.glob("*.h")))
+    for src in sorted(CLI.glob("*.c")):
+        exe = BIN / src.stem
+        if not force and exe.exists() and exe.stat().st_mtime >= max(
+                src.stat().st_mtime, hdr, LIB.stat().st_mtime):
+            continue
+        cmd = [cc, "-O2", "-std=c11", "-D_POSIX_C_SOURCE=200809L", "-Wall", f"-I{INCLUDE}",
+               f"-I{CLI}", str(src), "-o", str(exe), f"-L{HERE}", "-lclops",
+               "-Wl,-rpath,$ORIGIN/.."]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"CLI build failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
 
 
 if __name__ == "__main__":
