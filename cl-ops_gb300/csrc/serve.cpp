@@ -160,9 +160,18 @@ void launch_batch(clo_server *srv, Batch *b, Lane *lane) {
 						cudaMemcpyHostToDevice, s);
 			}
 			if (e == cudaSuccess && total > 0) {
-				if (r0.op == CLO_SERVE_SORT)
+				// A request alone takes the plain kernels (the chunked
+				// onesweep sort, without the host readback of pass skipping);
+				// a batch takes one segmented call.
+				if (r0.op == CLO_SERVE_SORT && k == 1)
+					e = clo::radix_sort(din, nullptr, total, (int)ib, 0, (int)(8 * ib),
+						srv->ctx, s, false, &err);
+				else if (r0.op == CLO_SERVE_SORT)
 					e = clo::seg_sort(din, total, d_off, k, (int)ib, (int)(8 * ib), 0,
 						srv->ctx, s, &err);
+				else if (k == 1)
+					e = clo::scan_exclusive(din, dout, total, r0.type, (int)ob, srv->ctx, s,
+						&err);
 				else
 					e = clo::seg_scan(din, dout, total, d_off, k, r0.type, (int)ob,
 						srv->ctx, s, &err);

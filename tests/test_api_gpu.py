@@ -38,15 +38,22 @@ def test_satradix_bad_scan_impl_fails_at_first_sort(clops, ctx, queue):
     s.destroy()
 
 
-def test_custom_snippets_are_rejected(clops, ctx):
-    with pytest.raises(clops.CloError) as ei:
-        clops.Sorter(ctx, "abitonic", 5, compare="((a) < (b))")
-    assert ei.value.code == clops.CLO_ERROR_ARGS
-    # satradix ignores compare, like the reference.
-    s = clops.Sorter(ctx, "satradix", 5, compare="((a) < (b))")
+def test_custom_snippets_build_and_satradix_ignores_compare(clops, ctx):
+    # Custom macros build a program (NVRTC); satradix ignores compare, like
+    # the reference, and so needs no program for it.
+    s = clops.Sorter(ctx, "abitonic", 5, compare="((a) < (b))")
+    assert "CLO_SORT_COMPARE(a, b) ((a) < (b))" in clops.lib.ccl_program_get_source(
+        clops.lib.clo_sort_get_program(s.h)).decode()
     s.destroy()
-    with pytest.raises(clops.CloError):
-        clops.Sorter(ctx, "satradix", 5, get_key="((x) >> 1)")
+    s = clops.Sorter(ctx, "satradix", 5, compare="((a) < (b))")
+    src = clops.lib.ccl_program_get_source(clops.lib.clo_sort_get_program(s.h)).decode()
+    assert "clo_jit_keys" not in src
+    s.destroy()
+    s = clops.Sorter(ctx, "satradix", 5, get_key="((x) >> 1)")
+    s.destroy()
+    with pytest.raises(clops.CloError) as ei:
+        clops.Sorter(ctx, "gselect", 5, get_key="((x) >> )")
+    assert ei.value.code == clops.CLO_ERROR_LIBRARY
 
 
 def test_satradix_rejects_float(clops, ctx):
