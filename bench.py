@@ -589,8 +589,60 @@ def run_suite(clops, ctx, q, args, only=None):
             "serial_plain_Gelem_per_s": round(serial / 1e9, 3),
             "speedup_vs_serial_plain": round(agg / serial, 2) if serial else None}
 
+    def c1_c3():
+        """C1: 2^20 uint32 keys with the reference's radix=16 option
+        (latency-bound, informational). C3: 2^28 uint32 keys sorted,
+        reverse-sorted, all equal, 16 distinct values, Zipf(1.1) over 2^20
+        ranks, and 2^27 uint64 keys with only the low 20 bits random; each
+        with the passes the digit histograms leave (constant digits are
+        skipped)."""
+        from inputs import adversarial_u32, low20_u64
+        s32 = clops.Sorter(ctx, "satradix", clops.CLO_UINT, options="radix=16")
+        a = keys_u32_chunked(42, 1 << 20)
+        pr = clops.Buffer.from_array(ctx, q, a)
+        b = clops.Buffer(ctx, a.nbytes)
+        t_copy = timed(lambda: copy(pr, b, a.nbytes), reps=20)
+        ms = timed(lambda: (copy(pr, b, a.nbytes), s32.sort_device(q, b, a.size)),
+                   reps=20) - t_copy
+        res["c1_satradix_2pow20_u32_radix16"] = {"Gkeys/s": round(a.size / (ms * 1e-3) / 1e9, 3),
+                                                  "ms": round(ms, 4)}
+        for x in (pr, b):
+            x.destroy()
+        n = 1 << 28 if only is None else 1 << min(args.log2n, 28)
+        out = {}
+        # Sorted and reverse-sorted inputs come from sorting uniform keys on
+        # the device (a host sort of 2^28 keys would dominate the run).
+        base = keys_u32_chunked(47, n)
+        bb = clops.Buffer.from_array(ctx, q, base)
+        clops.wait(s32.sort_device(q, bb, n))
+        srt = bb.read(q, np.uint32, n)
+        bb.destroy()
+        cases = [("sorted", lambda: srt), ("reverse", lambda: srt[::-1].copy())]
+        cases += [(k, lambda k=k: adversarial_u32(k, n)) for k in ("equal", "distinct16", "zipf")]
+        cases.append(("u64_low20", lambda: low20_u64(n // 2)))
+        for name, gen in cases:
+            a = gen()
+            s = s32 if a.dtype == np.uint32 else clops.Sorter(ctx, "satradix", clops.CLO_ULONG)
+            pr = clops.Buffer.from_array(ctx, q, a)
+            b = clops.Buffer(ctx, a.nbytes)
+            t_copy = timed(lambda: copy(pr, b, a.nbytes))
+            before = clops.launch_count()
+            ms = timed(lambda: (copy(pr, b, a.nbytes), s.sort_device(q, b, a.size))) - t_copy
+            launches = (clops.launch_count() - before) / 5.0  # 2 warm-up + 3 timed
+            got = b.read(q, a.dtype, a.size)
+            ok = bool(np.all(got[1:] >= got[:-1]))
+            out[name] = {"n": int(a.size), "Gkeys/s": round(a.size / (ms * 1e-3) / 1e9, 3),
+                         "ms": round(ms, 3), "kernels_per_sort": launches,
+                         "sorted": ok}
+            for x in (pr, b):
+                x.destroy()
+            if s is not s32:
+                s.destroy()
+        res["c3_satradix_adversarial"] = out
+        s32.destroy()
+
     parts = {"abitonic": abitonic, "kv": kv, "scan": scan, "rng": rngs,
-             "segmented": segmented, "serve": serve}
+             "segmented": segmented, "serve": serve, "c1c3": c1_c3}
     for name, fn in parts.items():
         if only is None or only == name:
             fn()
@@ -669,7 +721,8 @@ def main():
     ap.add_argument("--no-suite", dest="suite", action="store_false")
     ap.add_argument("--serve-seconds", type=float, default=1.0,
                     help="open-loop duration of the serving workload")
-    ap.add_argument("--only", choices=["abitonic", "kv", "scan", "rng", "segmented", "serve"],
+    ap.add_argument("--only", choices=["abitonic", "kv", "scan", "rng", "segmented", "serve",
+                                       "c1c3"],
                     help="run one suite primitive alone (profiling cases)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
