@@ -127,6 +127,12 @@ cudaError_t radix_sort(void *keys, void *vals, size_t n, int key_bytes,
 	int val_bytes, int sort_bits, CCLContext *ctx, cudaStream_t s,
 	bool allow_skip, GError **err);
 
+// Stable partition of n keys (key_bytes 2, 4 or 8) by the top 8 bits of
+// their low sort_bits bits, into keys_out; counts (host, 256 entries)
+// receives the size of each group. Synchronises the stream once.
+cudaError_t radix_msd_partition(const void *keys_in, void *keys_out, size_t n, int key_bytes,
+	int sort_bits, uint32_t *counts, CCLContext *ctx, cudaStream_t s, GError **err);
+
 // Exclusive scan: out[i] = sum_{j<i} (sum type) in[j] modulo
 // 2^(8*out_bytes). in_type is an integer CloType, out_bytes in {1,2,4,8}.
 cudaError_t scan_exclusive(const void *in, void *out, size_t n,

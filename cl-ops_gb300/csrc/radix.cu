@@ -64,7 +64,8 @@ __device__ __forceinline__ uint32_t digit_of(K k, int shift) {
 // detects with one AND/OR reduction and adds once.
 template <typename K, int PASSES>
 __global__ void __launch_bounds__(256)
-radix_upsweep(const K *__restrict__ keys, size_t n, uint32_t *__restrict__ hist) {
+radix_upsweep(const K *__restrict__ keys, size_t n, uint32_t *__restrict__ hist,
+	int base_shift) {
 	constexpr int passes = PASSES;
 	__shared__ uint32_t h[PASSES][kRadix];
 	for (int i = threadIdx.x; i < PASSES * kRadix; i += blockDim.x) (&h[0][0])[i] = 0;
@@ -87,7 +88,7 @@ radix_upsweep(const K *__restrict__ keys, size_t n, uint32_t *__restrict__ hist)
 			uint32_t a = 0xffffffffu, o = 0u;
 #pragma unroll
 			for (int q = 0; q < PER; ++q) {
-				dd[q] = digit_of(e[q], p * kRadixBits);
+				dd[q] = digit_of(e[q], base_shift + p * kRadixBits);
 				a &= dd[q];
 				o |= dd[q];
 			}
@@ -108,7 +109,7 @@ radix_upsweep(const K *__restrict__ keys, size_t n, uint32_t *__restrict__ hist)
 	for (size_t i = done + tid_global; i < n; i += threads_total) {
 		K key = keys[i];
 		for (int p = 0; p < passes; ++p)
-			atomicAdd(&h[p][digit_of(key, p * kRadixBits)], 1u);
+			atomicAdd(&h[p][digit_of(key, base_shift + p * kRadixBits)], 1u);
 	}
 	__syncthreads();
 	for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) {
@@ -868,16 +869,16 @@ size_t chunked_smem() {
 
 template <typename K>
 void launch_upsweep(int passes, int grid, cudaStream_t s, const K *keys, size_t n,
-	uint32_t *hist) {
+	uint32_t *hist, int base_shift = 0) {
 	switch (passes) {
-	case 1: radix_upsweep<K, 1><<<grid, 256, 0, s>>>(keys, n, hist); break;
-	case 2: radix_upsweep<K, 2><<<grid, 256, 0, s>>>(keys, n, hist); break;
-	case 3: radix_upsweep<K, 3><<<grid, 256, 0, s>>>(keys, n, hist); break;
-	case 4: radix_upsweep<K, 4><<<grid, 256, 0, s>>>(keys, n, hist); break;
-	case 5: radix_upsweep<K, 5><<<grid, 256, 0, s>>>(keys, n, hist); break;
-	case 6: radix_upsweep<K, 6><<<grid, 256, 0, s>>>(keys, n, hist); break;
-	case 7: radix_upsweep<K, 7><<<grid, 256, 0, s>>>(keys, n, hist); break;
-	default: radix_upsweep<K, 8><<<grid, 256, 0, s>>>(keys, n, hist); break;
+	case 1: radix_upsweep<K, 1><<<grid, 256, 0, s>>>(keys, n, hist, base_shift); break;
+	case 2: radix_upsweep<K, 2><<<grid, 256, 0, s>>>(keys, n, hist, base_shift); break;
+	case 3: radix_upsweep<K, 3><<<grid, 256, 0, s>>>(keys, n, hist, base_shift); break;
+	case 4: radix_upsweep<K, 4><<<grid, 256, 0, s>>>(keys, n, hist, base_shift); break;
+	case 5: radix_upsweep<K, 5><<<grid, 256, 0, s>>>(keys, n, hist, base_shift); break;
+	case 6: radix_upsweep<K, 6><<<grid, 256, 0, s>>>(keys, n, hist, base_shift); break;
+	case 7: radix_upsweep<K, 7><<<grid, 256, 0, s>>>(keys, n, hist, base_shift); break;
+	default: radix_upsweep<K, 8><<<grid, 256, 0, s>>>(keys, n, hist, base_shift); break;
 	}
 }
 
@@ -990,6 +991,68 @@ cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
 	return e;
 }
 
+// Stable partition of n keys by the top 8 of their sort_bits low bits:
+// keys_out receives the keys grouped by that digit, in input order within a
+// digit; counts (host) receives the 256 group sizes. One histogram kernel
+// for the digit, a host readback of its 256 counts, one chunked pass.
+template <typename K>
+cudaError_t msd_partition_typed(const K *keys_in, K *keys_out, size_t n, int sort_bits,
+	uint32_t *counts, CCLContext *ctx, cudaStream_t s, GError **err) {
+	constexpr int CT = kChunkThreads;
+	constexpr int CTILE = ChunkCfg<K, CT>::kTile;
+	const int shift = sort_bits - kRadixBits;
+	const size_t ctiles = (n + CTILE - 1) / CTILE;
+	const uint32_t chunks = (uint32_t)std::min<size_t>(ctiles,
+		(size_t)ChunkCfg<K, CT>::kMinBlocks * ctx->sm_count);
+	const size_t status_words = (size_t)chunks * kRadix;
+	const size_t off_cnt = kRadix * 4, off_st0 = off_cnt + 64;
+	const size_t off_st1 = off_st0 + status_words * 4;
+	char *tmp = (char *)tmp_alloc(ctx, off_st1 + status_words * 4, s, err);
+	if (!tmp) return cudaErrorMemoryAllocation;
+	uint32_t *hist = (uint32_t *)tmp;
+	uint32_t *cnt = (uint32_t *)(tmp + off_cnt);
+	cudaError_t e = cudaMemsetAsync(tmp, 0, off_st1, s);
+	if (e == cudaSuccess) {
+		int grid = ctx->sm_count * 4;
+		const size_t need = ((n * sizeof(K) + 15) / 16 + 255) / 256;
+		if ((size_t)grid > need) grid = (int)std::max<size_t>(need, 1);
+		KernelTimer t("satradix_upsweep", s, (double)n * sizeof(K));
+		launch_upsweep<K>(1, grid, s, keys_in, n, hist, shift);
+		t.stop();
+		e = cudaGetLastError();
+	}
+	if (e == cudaSuccess) e = cudaMemcpyAsync(counts, hist, kRadix * 4, cudaMemcpyDeviceToHost, s);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+	bool trivial = false;
+	for (int d = 0; d < kRadix && e == cudaSuccess; ++d) trivial = trivial || counts[d] == n;
+	if (e == cudaSuccess && trivial) {
+		e = cudaMemcpyAsync(keys_out, keys_in, n * sizeof(K), cudaMemcpyDeviceToDevice, s);
+	} else if (e == cudaSuccess) {
+		const size_t smem = chunked_smem<K, uint32_t, false, CT>();
+		auto kern = radix_pass_chunked<K, uint32_t, false, CT>;
+		e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		PassArgs pa;
+		pa.hist = hist;
+		pa.status = (uint32_t *)(tmp + off_st0);
+		pa.status_next = (uint32_t *)(tmp + off_st1);
+		pa.tile_counter = cnt;
+		pa.dev_status = ctx->d_status;
+		pa.n = n;
+		pa.shift = shift;
+		if (e == cudaSuccess) {
+			KernelTimer t("satradix_onesweep", s, 2.0 * (double)n * sizeof(K));
+			kern<<<chunks, CT, smem, s>>>(keys_in, keys_out, nullptr, nullptr, pa,
+				(uint32_t)ctiles, chunks);
+			t.stop();
+			e = cudaGetLastError();
+		}
+	}
+	count_launches(trivial ? 1 : 2);
+	tmp_free(tmp, s);
+	if (e != cudaSuccess) cuda_ok(e, err, "satradix partition");
+	return e;
+}
+
 template <typename K>
 cudaError_t sort_keys_vals(void *keys, void *vals, size_t n, int val_bytes,
 	int sort_bits, CCLContext *ctx, cudaStream_t s, bool skip, GError **err) {
@@ -1003,6 +1066,21 @@ cudaError_t sort_keys_vals(void *keys, void *vals, size_t n, int val_bytes,
 }
 
 }  // namespace
+
+cudaError_t radix_msd_partition(const void *keys_in, void *keys_out, size_t n, int key_bytes,
+	int sort_bits, uint32_t *counts, CCLContext *ctx, cudaStream_t s, GError **err) {
+	if (sort_bits < kRadixBits || n >= (size_t)kStValue) {
+		set_error(err, CLO_ERROR_ARGS, "satradix partition: %d sort bits, %zu keys", sort_bits, n);
+		return cudaErrorInvalidValue;
+	}
+	switch (key_bytes) {
+	case 2: return msd_partition_typed<uint16_t>((const uint16_t *)keys_in, (uint16_t *)keys_out, n, sort_bits, counts, ctx, s, err);
+	case 4: return msd_partition_typed<uint32_t>((const uint32_t *)keys_in, (uint32_t *)keys_out, n, sort_bits, counts, ctx, s, err);
+	case 8: return msd_partition_typed<uint64_t>((const uint64_t *)keys_in, (uint64_t *)keys_out, n, sort_bits, counts, ctx, s, err);
+	}
+	set_error(err, CLO_ERROR_ARGS, "satradix partition: key width %d", key_bytes);
+	return cudaErrorInvalidValue;
+}
 
 cudaError_t radix_sort(void *keys, void *vals, size_t n, int key_bytes,
 	int val_bytes, int sort_bits, CCLContext *ctx, cudaStream_t s,

@@ -8,6 +8,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <vector>
 
 #include "clo_internal.h"
 #include "jit.h"
@@ -650,6 +651,86 @@ CCLEvent *clo_sort_with_device_data(CloSort *sorter, CCLQueue *cq_exec,
 		data_in, data_out, numel, lws_max, err);
 }
 
+}  // extern "C"
+
+namespace {
+
+// Host-data satradix for large arrays, with the copy back overlapped by
+// the sort: after the copy in, one stable partition pass by the top digit
+// splits the keys into 256 ordered groups; groups of kBucketsPerGroup are
+// then sorted (each group's buckets as segments, by the remaining bits)
+// one after the other, and each group's copy to the host starts, on a
+// second stream, as soon as it is sorted. Stable throughout, so the result
+// is the single satradix sort's.
+constexpr int kBucketsPerGroup = 16;
+
+bool satradix_host_pipelined(CloSort *s, CCLQueue *q, const void *h_in, void *h_out,
+	size_t n, GError **err) {
+	CCLContext *ctx = s->ctx;
+	const size_t eb = clo_type_sizeof(s->elem_type);
+	const int bits = satradix_sort_bits(s);
+	const int groups = 256 / kBucketsPerGroup;
+	cudaStream_t cs = q->stream, xs = nullptr;
+	if (!cuda_ok(cudaStreamCreateWithFlags(&xs, cudaStreamNonBlocking), err, "stream"))
+		return false;
+	const size_t off_b = (n * eb + 255) / 256 * 256;
+	const size_t off_rel = off_b + (n * eb + 255) / 256 * 256;
+	const size_t rel_words = (size_t)groups * (kBucketsPerGroup + 1);
+	char *dev = (char *)clo::tmp_alloc(ctx, off_rel + rel_words * 8, cs, err);
+	uint64_t *h_rel = nullptr;
+	std::vector<cudaEvent_t> evs;
+	bool ok = dev != nullptr;
+	ok = ok && cuda_ok(cudaMallocHost(&h_rel, rel_words * 8), err, "cudaMallocHost");
+	char *da = dev, *db = dev + off_b;
+	uint64_t *d_rel = (uint64_t *)(dev + off_rel);
+	uint32_t counts[256];
+	ok = ok && cuda_ok(cudaMemcpyAsync(da, h_in, n * eb, cudaMemcpyHostToDevice, cs), err,
+		"copy in");
+	ok = ok && clo::radix_msd_partition(da, db, n, (int)eb, bits, counts, ctx, cs, err) ==
+		cudaSuccess;
+	uint64_t off[257];
+	off[0] = 0;
+	for (int d = 0; d < 256; ++d) off[d + 1] = off[d] + (ok ? counts[d] : 0);
+	if (ok) {
+		for (int g = 0; g < groups; ++g)
+			for (int j = 0; j <= kBucketsPerGroup; ++j)
+				h_rel[(size_t)g * (kBucketsPerGroup + 1) + j] =
+					off[g * kBucketsPerGroup + j] - off[g * kBucketsPerGroup];
+		ok = cuda_ok(cudaMemcpyAsync(d_rel, h_rel, rel_words * 8, cudaMemcpyHostToDevice, cs),
+			err, "offsets");
+	}
+	for (int g = 0; g < groups && ok; ++g) {
+		const uint64_t base = off[g * kBucketsPerGroup];
+		const uint64_t len = off[(g + 1) * kBucketsPerGroup] - base;
+		if (len == 0) continue;
+		char *gp = db + base * eb;
+		if (bits > 8)
+			ok = clo::seg_sort(gp, len, d_rel + (size_t)g * (kBucketsPerGroup + 1),
+				kBucketsPerGroup, (int)eb, bits - 8, 0, ctx, cs, err) == cudaSuccess;
+		cudaEvent_t ev = nullptr;
+		ok = ok && cuda_ok(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), err, "event");
+		if (!ok) break;
+		evs.push_back(ev);
+		ok = cuda_ok(cudaEventRecord(ev, cs), err, "event") &&
+			cuda_ok(cudaStreamWaitEvent(xs, ev, 0), err, "wait") &&
+			cuda_ok(cudaMemcpyAsync((char *)h_out + base * eb, gp, len * eb,
+				cudaMemcpyDeviceToHost, xs), err, "copy out");
+	}
+	cudaStreamSynchronize(xs);
+	cudaStreamSynchronize(cs);
+	ok = ok && clo::check_device_status(ctx, err);
+	for (cudaEvent_t ev : evs) cudaEventDestroy(ev);
+	cudaStreamDestroy(xs);
+	if (h_rel) cudaFreeHost(h_rel);
+	clo::tmp_free(dev, cs);
+	cudaStreamSynchronize(cs);
+	return ok;
+}
+
+}  // namespace
+
+extern "C" {
+
 cl_bool clo_sort_with_host_data(CloSort *sorter, CCLQueue *cq_exec,
 	CCLQueue *cq_comm, void *data_in, void *data_out, size_t numel,
 	size_t lws_max, GError **err) {
@@ -659,6 +740,18 @@ cl_bool clo_sort_with_host_data(CloSort *sorter, CCLQueue *cq_exec,
 	}
 	CCLContext *ctx = sorter->ctx;
 	cudaSetDevice(ctx->ordinal);
+	// Large satradix sorts overlap the copy back with the sort.
+	if (strcmp(sorter->impl_def.name, "satradix") == 0 && !sorter->jit &&
+		numel >= ((size_t)1 << 22) && numel < ((size_t)1 << 30) &&
+		satradix_sort_bits(sorter) >= 16 && clo_type_sizeof(sorter->elem_type) >= 2) {
+		CCLQueue *q = cq_exec;
+		GError *e3 = nullptr;
+		if (!q) q = ccl_queue_new(ctx, &ctx->device, 0, &e3);
+		bool ok = q && satradix_host_pipelined(sorter, q, data_in, data_out, numel, &e3);
+		if (q && q != cq_exec) ccl_queue_destroy(q);
+		clo::propagate_error(err, e3);
+		return ok ? CL_TRUE : CL_FALSE;
+	}
 	GError *e2 = nullptr;
 	CCLQueue *own = nullptr;
 	if (cq_exec == nullptr) {

@@ -175,3 +175,32 @@ def test_gselect_out_of_place(clops, ctx, queue):
     bi.destroy()
     bo.destroy()
     s.destroy()
+
+
+# ------------------------------------------ large host-data satradix path
+@pytest.mark.parametrize("code,dt,n", [(5, np.uint32, (1 << 22) + 333), (6, np.int64, 1 << 22),
+                                       (3, np.uint16, (1 << 23) + 1), (0, np.int8, 1 << 22)])
+def test_satradix_host_data_large_matches_oracle(clops, ctx, queue, code, dt, n):
+    a = keys_of_type(77 + code, n, dt)
+    s = clops.Sorter(ctx, "satradix", code)
+    out = np.empty_like(a)
+    clops.call(clops.lib.clo_sort_with_host_data, s.h, queue.h, None, clops.np_ptr(a),
+               clops.np_ptr(out), n, 0)
+    np.testing.assert_array_equal(out, oracle.radix_sort(a))
+    s.destroy()
+
+
+@pytest.mark.parametrize("kind", ["equal", "distinct16", "sorted"])
+def test_satradix_host_data_large_low_entropy_and_narrow_key(clops, ctx, queue, kind):
+    n = 1 << 22
+    a = adversarial_u32(kind, n)
+    s = clops.Sorter(ctx, "satradix", 5)
+    got = s.sort_host(queue, a.copy())
+    np.testing.assert_array_equal(got, oracle.radix_sort(a))
+    s.destroy()
+    # ulong elements, uint key: stable by the low 32 bits.
+    b = (np.arange(n, dtype=np.uint64) << np.uint64(32)) | a.astype(np.uint64)
+    s = clops.Sorter(ctx, "satradix", 7, key_type=5)
+    got = s.sort_host(queue, b.copy())
+    np.testing.assert_array_equal(got, oracle.radix_sort(b, sort_bits=32))
+    s.destroy()
