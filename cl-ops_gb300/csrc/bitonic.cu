@@ -15,7 +15,7 @@
 // abitonic groups the steps:
 //   - abitonic_tile_sort: each shared-memory tile of 2^t elements runs
 //     stages 1..t (the stage-t direction comes from the tile's index);
-//   - abitonic_global_steps<g>: g (<= 4) consecutive steps with strides
+//   - abitonic_global_steps<g>: g (<= 5) consecutive steps with strides
 //     >= the tile, 2^g elements per thread held in registers;
 //   - abitonic_tile_finish: the remaining steps t..1 of a stage in shared
 //     memory.
@@ -139,7 +139,7 @@ __device__ __forceinline__ void smem_steps(T *s, uint32_t tile_n, int j,
 	}
 }
 
-// Steps j..1 of one stage, at most 4 per barrier interval.
+// Steps j..1 of one stage, at most maxg (<= 4) per barrier interval.
 template <typename T, typename DescFn>
 __device__ __forceinline__ void smem_stage_tail(T *s, uint32_t tile_n, int j,
 	int maxg, DescFn desc_fn) {
@@ -242,7 +242,13 @@ cudaError_t run_abitonic(T *d, size_t N, int max_ps, int max_sfs,
 	const int logN = ilog2(N);
 	int t = std::min(default_tile_log2<T>(), logN);
 	if (max_sfs >= 1 && max_sfs < t) t = max_sfs;
+	// Steps per register round: at most 4 (16 elements per thread) in the
+	// shared-memory tiles; in the global passes 5 (32) for types of up to 4
+	// bytes when the maxps option allows the most grouping (the network,
+	// hence the result, is the same for any grouping; 5 in the tiles would
+	// leave one 512-thread CTA per SM).
 	const int maxg = std::max(1, std::min(4, max_ps));
+	const int gmaxg = max_ps >= 4 && sizeof(T) <= 4 ? 5 : maxg;
 	const uint32_t tile_n = 1u << t;
 	const size_t smem = (size_t)(tile_n + tile_n / 32 + 1) * sizeof(T);
 	const int threads = (int)std::min<uint32_t>(kTileThreads, std::max<uint32_t>(tile_n / 2, 32));
@@ -263,11 +269,12 @@ cudaError_t run_abitonic(T *d, size_t N, int max_ps, int max_sfs,
 	for (int stage = t + 1; stage <= logN && e == cudaSuccess; ++stage) {
 		int j = stage;
 		while (j > t) {
-			int g = std::min(maxg, j - t);
+			int g = std::min(gmaxg, j - t);
 			size_t groups = N >> g;
 			unsigned blocks = (unsigned)((groups + 255) / 256);
 			KernelTimer tm("abitonic_global_steps", s, pass_bytes);
 			switch (g) {
+			case 5: abitonic_global_steps<T, 5><<<blocks, 256, 0, s>>>(d, groups, stage, j); break;
 			case 4: abitonic_global_steps<T, 4><<<blocks, 256, 0, s>>>(d, groups, stage, j); break;
 			case 3: abitonic_global_steps<T, 3><<<blocks, 256, 0, s>>>(d, groups, stage, j); break;
 			case 2: abitonic_global_steps<T, 2><<<blocks, 256, 0, s>>>(d, groups, stage, j); break;
