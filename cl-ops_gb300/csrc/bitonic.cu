@@ -169,7 +169,7 @@ __device__ __forceinline__ void tile_store(T *g, const T *s, uint32_t tile_n) {
 
 // Stages 1..t of every tile of 2^t elements.
 template <typename T>
-__global__ void __launch_bounds__(kTileThreads)
+__global__ void __launch_bounds__(kTileThreads, sizeof(T) <= 4 ? 3 : 2)
 abitonic_tile_sort(T *data, int t, int maxg) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	T *s = reinterpret_cast<T *>(smem_raw);
@@ -191,7 +191,7 @@ abitonic_tile_sort(T *data, int t, int maxg) {
 
 // Steps t..1 of `stage` (> t) for every tile.
 template <typename T>
-__global__ void __launch_bounds__(kTileThreads)
+__global__ void __launch_bounds__(kTileThreads, sizeof(T) <= 4 ? 3 : 2)
 abitonic_tile_finish(T *data, int t, int stage, int maxg) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	T *s = reinterpret_cast<T *>(smem_raw);
