@@ -139,6 +139,13 @@ cudaError_t scan_exclusive(const void *in, void *out, size_t n,
 	CloType in_type, int out_bytes, CCLContext *ctx, cudaStream_t s,
 	GError **err);
 
+// The same scan continuing an earlier one: the sums start from the value
+// at carry_in (device, the sum type; null = 0), and the total (carry plus
+// this part's sum) is written to carry_out (device; null = not written).
+cudaError_t scan_exclusive_carry(const void *in, void *out, size_t n,
+	CloType in_type, int out_bytes, const void *carry_in, void *carry_out,
+	CCLContext *ctx, cudaStream_t s, GError **err);
+
 // Bitonic network sort of n elements (default compare "a > b" on the
 // element's own type), reproducing the reference network exactly:
 // pairs, directions and the strict-compare-xor-direction swap rule.
@@ -156,10 +163,13 @@ cudaError_t gselect_sort(const void *in, void *out, size_t n, CloType type,
 // of keys; off is a device array of S + 1 non-decreasing offsets within
 // n_cap elements), in a fixed launch sequence with no host readback.
 // variant selects the CTA class layout (0 .. seg_sort_num_variants()-1).
+// With `alt` (n_cap elements) and `in_alt`, the multi-CTA passes use `alt`
+// as their second buffer and, after an odd number of passes, leave every
+// segment's result there (*in_alt = true) instead of copying it back.
 int seg_sort_num_variants();
 cudaError_t seg_sort(void *keys, uint64_t n_cap, const uint64_t *off, size_t S,
 	int key_bytes, int sort_bits, int variant, CCLContext *ctx, cudaStream_t s,
-	GError **err);
+	GError **err, void *alt = nullptr, bool *in_alt = nullptr);
 
 // Segmented exclusive scan: within each segment, out as the scan of that
 // segment alone; elements outside [off[0], off[S]) are not written.

@@ -54,7 +54,8 @@ template <typename InT, typename OutT>
 __global__ void __launch_bounds__(kThreads, 5)
 scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, size_t n,
 	TileStatus ts,
-	int *dev_status, bool vec_ok, long long debug_skip_tile) {
+	int *dev_status, bool vec_ok, long long debug_skip_tile,
+	const void *carry_in, void *carry_out) {
 	using Acc = typename std::conditional<(sizeof(OutT) <= 4), uint32_t,
 		uint64_t>::type;
 	constexpr int ESZ = sizeof(InT) > sizeof(OutT) ? sizeof(InT) : sizeof(OutT);
@@ -126,14 +127,21 @@ scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, size_t n,
 		constexpr int PT = Slots<Acc>::kPerTile;
 		Acc excl = 0;
 		if (tile == 0) {
-			if (lane == 0 && do_publish) publish<Acc>(ts.words + Slots<Acc>::kWords, aggregate);
+			// A scan continuing an earlier one starts from its carry.
+			if (carry_in) excl = *reinterpret_cast<const Acc *>(carry_in);
+			if (lane == 0 && do_publish)
+				publish<Acc>(ts.words + Slots<Acc>::kWords, excl + aggregate);
 		} else {
 			if (lane == 0 && do_publish) publish<Acc>(ts.words + (size_t)tile * PT, aggregate);
 			excl = lb::lookback_warp<Acc>(ts.words, tile, dev_status);
 			if (lane == 0 && do_publish)
 				publish<Acc>(ts.words + (size_t)tile * PT + Slots<Acc>::kWords, excl + aggregate);
 		}
-		if (lane == 0) s_excl = excl;
+		if (lane == 0) {
+			s_excl = excl;
+			if (carry_out && (size_t)(tile + 1) * kTile >= n)
+				*reinterpret_cast<Acc *>(carry_out) = excl + aggregate;
+		}
 	}
 	__syncthreads();
 
@@ -163,7 +171,8 @@ scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, size_t n,
 
 template <typename InT, typename OutT>
 cudaError_t launch_scan(const void *in, void *out, size_t n, CCLContext *ctx,
-	cudaStream_t s, GError **err, long long debug_skip_tile) {
+	cudaStream_t s, GError **err, long long debug_skip_tile,
+	const void *carry_in = nullptr, void *carry_out = nullptr) {
 	using Acc = typename std::conditional<(sizeof(OutT) <= 4), uint32_t,
 		uint64_t>::type;
 	const size_t tiles = (n + kTile - 1) / kTile;
@@ -184,7 +193,7 @@ cudaError_t launch_scan(const void *in, void *out, size_t n, CCLContext *ctx,
 		KernelTimer t("scan_lookback", s, (double)n * (sizeof(InT) + sizeof(OutT)));
 		scan_lookback<InT, OutT><<<(unsigned)tiles, kThreads, 0, s>>>(
 			(const InT *)in, (OutT *)out, n, ts, ctx->d_status, vec_ok,
-			debug_skip_tile);
+			debug_skip_tile, carry_in, carry_out);
 		t.stop();
 		count_launches(1);
 		e = cudaGetLastError();
@@ -196,12 +205,13 @@ cudaError_t launch_scan(const void *in, void *out, size_t n, CCLContext *ctx,
 
 template <typename InT>
 cudaError_t dispatch_out(const void *in, void *out, size_t n, int out_bytes,
-	CCLContext *ctx, cudaStream_t s, GError **err, long long dbg) {
+	CCLContext *ctx, cudaStream_t s, GError **err, long long dbg,
+	const void *ci = nullptr, void *co = nullptr) {
 	switch (out_bytes) {
-	case 1: return launch_scan<InT, uint8_t>(in, out, n, ctx, s, err, dbg);
-	case 2: return launch_scan<InT, uint16_t>(in, out, n, ctx, s, err, dbg);
-	case 4: return launch_scan<InT, uint32_t>(in, out, n, ctx, s, err, dbg);
-	case 8: return launch_scan<InT, uint64_t>(in, out, n, ctx, s, err, dbg);
+	case 1: return launch_scan<InT, uint8_t>(in, out, n, ctx, s, err, dbg, ci, co);
+	case 2: return launch_scan<InT, uint16_t>(in, out, n, ctx, s, err, dbg, ci, co);
+	case 4: return launch_scan<InT, uint32_t>(in, out, n, ctx, s, err, dbg, ci, co);
+	case 8: return launch_scan<InT, uint64_t>(in, out, n, ctx, s, err, dbg, ci, co);
 	}
 	set_error(err, CLO_ERROR_ARGS, "Unsupported sum width %d", out_bytes);
 	return cudaErrorInvalidValue;
@@ -216,17 +226,23 @@ static long long g_debug_skip_tile = -1;
 cudaError_t scan_exclusive(const void *in, void *out, size_t n,
 	CloType in_type, int out_bytes, CCLContext *ctx, cudaStream_t s,
 	GError **err) {
+	return scan_exclusive_carry(in, out, n, in_type, out_bytes, nullptr, nullptr, ctx, s, err);
+}
+
+cudaError_t scan_exclusive_carry(const void *in, void *out, size_t n,
+	CloType in_type, int out_bytes, const void *ci, void *co, CCLContext *ctx,
+	cudaStream_t s, GError **err) {
 	if (n == 0) return cudaSuccess;
 	long long dbg = g_debug_skip_tile;
 	switch (in_type) {
-	case CLO_CHAR: return dispatch_out<int8_t>(in, out, n, out_bytes, ctx, s, err, dbg);
-	case CLO_UCHAR: return dispatch_out<uint8_t>(in, out, n, out_bytes, ctx, s, err, dbg);
-	case CLO_SHORT: return dispatch_out<int16_t>(in, out, n, out_bytes, ctx, s, err, dbg);
-	case CLO_USHORT: return dispatch_out<uint16_t>(in, out, n, out_bytes, ctx, s, err, dbg);
-	case CLO_INT: return dispatch_out<int32_t>(in, out, n, out_bytes, ctx, s, err, dbg);
-	case CLO_UINT: return dispatch_out<uint32_t>(in, out, n, out_bytes, ctx, s, err, dbg);
-	case CLO_LONG: return dispatch_out<int64_t>(in, out, n, out_bytes, ctx, s, err, dbg);
-	case CLO_ULONG: return dispatch_out<uint64_t>(in, out, n, out_bytes, ctx, s, err, dbg);
+	case CLO_CHAR: return dispatch_out<int8_t>(in, out, n, out_bytes, ctx, s, err, dbg, ci, co);
+	case CLO_UCHAR: return dispatch_out<uint8_t>(in, out, n, out_bytes, ctx, s, err, dbg, ci, co);
+	case CLO_SHORT: return dispatch_out<int16_t>(in, out, n, out_bytes, ctx, s, err, dbg, ci, co);
+	case CLO_USHORT: return dispatch_out<uint16_t>(in, out, n, out_bytes, ctx, s, err, dbg, ci, co);
+	case CLO_INT: return dispatch_out<int32_t>(in, out, n, out_bytes, ctx, s, err, dbg, ci, co);
+	case CLO_UINT: return dispatch_out<uint32_t>(in, out, n, out_bytes, ctx, s, err, dbg, ci, co);
+	case CLO_LONG: return dispatch_out<int64_t>(in, out, n, out_bytes, ctx, s, err, dbg, ci, co);
+	case CLO_ULONG: return dispatch_out<uint64_t>(in, out, n, out_bytes, ctx, s, err, dbg, ci, co);
 	default: break;
 	}
 	set_error(err, CLO_ERROR_ARGS, "Unsupported scan element type %d", (int)in_type);
@@ -311,7 +327,7 @@ cudaError_t launch_scan_noalloc(const void *in, void *out, size_t n,
 	if (e != cudaSuccess) return e;
 	bool vec_ok = ((uintptr_t)in % 16 == 0) && ((uintptr_t)out % 16 == 0);
 	scan_lookback<InT, OutT><<<(unsigned)tiles, kThreads, 0, s>>>(
-		(const InT *)in, (OutT *)out, n, ts, dev_status, vec_ok, -1);
+		(const InT *)in, (OutT *)out, n, ts, dev_status, vec_ok, -1, nullptr, nullptr);
 	count_launches(1);
 	return cudaGetLastError();
 }

@@ -4,6 +4,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "clo_internal.h"
 
@@ -159,6 +160,73 @@ CCLEvent *clo_scan_with_device_data(CloScan *scanner, CCLQueue *cq_exec,
 		data_in, data_out, numel, lws_max, err);
 }
 
+}  // extern "C"
+
+namespace {
+
+// Host-data scans of large arrays in chunks on three streams: chunk c is
+// copied in, scanned continuing from the running sum of the chunks before
+// it (a device-side carry), and copied out, while its neighbours are in
+// flight the other ways; the two copy directions overlap each other and
+// the scans.
+constexpr size_t kScanChunk = (size_t)1 << 24;
+
+bool scan_host_pipelined(CloScan *sc, CCLQueue *q, const void *h_in, void *h_out,
+	size_t n, GError **err) {
+	CCLContext *ctx = sc->ctx;
+	const size_t ib = clo_type_sizeof(sc->elem_type), ob = clo_type_sizeof(sc->sum_type);
+	const size_t nc = (n + kScanChunk - 1) / kScanChunk;
+	cudaStream_t cs = q->stream, si = nullptr, so = nullptr;
+	bool ok = cuda_ok(cudaStreamCreateWithFlags(&si, cudaStreamNonBlocking), err, "stream") &&
+		cuda_ok(cudaStreamCreateWithFlags(&so, cudaStreamNonBlocking), err, "stream");
+	const size_t off_out = (n * ib + 255) / 256 * 256;
+	const size_t off_carry = off_out + (n * ob + 255) / 256 * 256;
+	char *dev = ok ? (char *)clo::tmp_alloc(ctx, off_carry + (nc + 1) * 8, cs, err) : nullptr;
+	ok = ok && dev != nullptr;
+	std::vector<cudaEvent_t> evs;
+	auto event = [&]() {
+		cudaEvent_t e = nullptr;
+		if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return e;
+		evs.push_back(e);
+		return e;
+	};
+	cudaEvent_t ready = ok ? event() : nullptr;
+	ok = ok && ready && cuda_ok(cudaMemsetAsync(dev + off_carry, 0, (nc + 1) * 8, cs), err,
+		"carry") && cuda_ok(cudaEventRecord(ready, cs), err, "event") &&
+		cuda_ok(cudaStreamWaitEvent(si, ready, 0), err, "wait");
+	for (size_t c = 0; c < nc && ok; ++c) {
+		const size_t off = c * kScanChunk;
+		const size_t len = n - off < kScanChunk ? n - off : kScanChunk;
+		cudaEvent_t ein = event(), esc = event();
+		ok = ein && esc &&
+			cuda_ok(cudaMemcpyAsync(dev + off * ib, (const char *)h_in + off * ib, len * ib,
+				cudaMemcpyHostToDevice, si), err, "copy in") &&
+			cuda_ok(cudaEventRecord(ein, si), err, "event") &&
+			cuda_ok(cudaStreamWaitEvent(cs, ein, 0), err, "wait");
+		ok = ok && clo::scan_exclusive_carry(dev + off * ib, dev + off_out + off * ob, len,
+			sc->elem_type, (int)ob, dev + off_carry + c * 8, dev + off_carry + (c + 1) * 8,
+			ctx, cs, err) == cudaSuccess;
+		ok = ok && cuda_ok(cudaEventRecord(esc, cs), err, "event") &&
+			cuda_ok(cudaStreamWaitEvent(so, esc, 0), err, "wait") &&
+			cuda_ok(cudaMemcpyAsync((char *)h_out + off * ob, dev + off_out + off * ob,
+				len * ob, cudaMemcpyDeviceToHost, so), err, "copy out");
+	}
+	if (si) cudaStreamSynchronize(si);
+	if (so) cudaStreamSynchronize(so);
+	cudaStreamSynchronize(cs);
+	ok = ok && clo::check_device_status(ctx, err);
+	for (cudaEvent_t e : evs) cudaEventDestroy(e);
+	if (si) cudaStreamDestroy(si);
+	if (so) cudaStreamDestroy(so);
+	if (dev) clo::tmp_free(dev, cs);
+	cudaStreamSynchronize(cs);
+	return ok;
+}
+
+}  // namespace
+
+extern "C" {
+
 cl_bool clo_scan_with_host_data(CloScan *scanner, CCLQueue *cq_exec,
 	CCLQueue *cq_comm, void *data_in, void *data_out, size_t numel,
 	size_t lws_max, GError **err) {
@@ -168,6 +236,15 @@ cl_bool clo_scan_with_host_data(CloScan *scanner, CCLQueue *cq_exec,
 	}
 	CCLContext *ctx = scanner->ctx;
 	cudaSetDevice(ctx->ordinal);
+	if (numel >= ((size_t)1 << 22) && strcmp(scanner->impl_def.name, "blelloch") == 0) {
+		CCLQueue *q = cq_exec;
+		GError *e3 = nullptr;
+		if (!q) q = ccl_queue_new(ctx, &ctx->device, 0, &e3);
+		bool ok = q && scan_host_pipelined(scanner, q, data_in, data_out, numel, &e3);
+		if (q && q != cq_exec) ccl_queue_destroy(q);
+		clo::propagate_error(err, e3);
+		return ok ? CL_TRUE : CL_FALSE;
+	}
 	GError *e2 = nullptr;
 	CCLQueue *own = nullptr;
 	if (cq_exec == nullptr) {

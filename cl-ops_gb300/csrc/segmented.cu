@@ -599,6 +599,23 @@ __global__ void __launch_bounds__(256) seg_copy_large(K *dst, const K *src,
 	}
 }
 
+// Copies the segments sorted in place (warp and CTA classes) from `src`
+// to `dst`, one warp per segment.
+template <typename K>
+__global__ void __launch_bounds__(256) seg_copy_short(K *dst, const K *src,
+	const uint64_t *off, const uint32_t *lists, const uint32_t *counts, uint32_t S) {
+	const uint32_t lane = threadIdx.x & 31u;
+	const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+	for (int c = 0; c < 3; ++c) {
+		const uint32_t cnt = counts[c];
+		for (uint32_t i = gw; i < cnt; i += nw) {
+			const uint32_t s = lists[(size_t)c * S + i];
+			for (uint64_t j = off[s] + lane; j < off[s + 1]; j += 32) dst[j] = src[j];
+		}
+	}
+}
+
 // Class layouts the autotuner chooses from: (threads, keys per thread) of
 // classes A and B for keys of up to 4 bytes; 8-byte keys halve the keys
 // per thread.
@@ -687,10 +704,12 @@ void launch_seg_upsweep(int passes, uint32_t grid, cudaStream_t s, const K *keys
 
 template <typename K>
 cudaError_t seg_sort_typed(K *keys, uint64_t n_cap, const uint64_t *off, uint32_t S,
-	int sort_bits, int variant, CCLContext *ctx, cudaStream_t s, GError **err) {
+	int sort_bits, int variant, CCLContext *ctx, cudaStream_t s, GError **err,
+	K *alt_ext, bool *in_alt) {
 	constexpr int KPT_DIV = sizeof(K) > 4 ? 2 : 1;
 	constexpr int LTILE = LCfg<K>::kTile;
 	const int passes = sort_bits / kRadixBits;
+	if (in_alt) *in_alt = false;
 	if (S == 0 || passes == 0 || n_cap < 2) return cudaSuccess;
 	if (variant < 0 || variant >= kNumVariants) variant = 0;
 	const Variant &v = kVariants[variant];
@@ -711,7 +730,7 @@ cudaError_t seg_sort_typed(K *keys, uint64_t n_cap, const uint64_t *off, uint32_
 	size_t off_st0 = (off_hist + L_bound * passes * kRadix * 4 + 255) / 256 * 256;
 	size_t off_st1 = off_st0 + T_bound * kRadix * 4;
 	size_t off_alt = (off_st1 + T_bound * kRadix * 4 + 255) / 256 * 256;
-	size_t total = L_bound ? off_alt + n_cap * sizeof(K) : off_tseg;
+	size_t total = L_bound ? off_alt + (alt_ext ? 0 : n_cap * sizeof(K)) : off_tseg;
 	char *tmp = (char *)tmp_alloc(ctx, total, s, err);
 	if (!tmp) return cudaErrorMemoryAllocation;
 	uint32_t *counts = (uint32_t *)(tmp + off_cnt);
@@ -721,7 +740,7 @@ cudaError_t seg_sort_typed(K *keys, uint64_t n_cap, const uint64_t *off, uint32_
 	uint32_t *tile_seg = (uint32_t *)(tmp + off_tseg);
 	uint32_t *seg_hist = (uint32_t *)(tmp + off_hist);
 	uint32_t *st[2] = {(uint32_t *)(tmp + off_st0), (uint32_t *)(tmp + off_st1)};
-	K *alt = (K *)(tmp + off_alt);
+	K *alt = alt_ext ? alt_ext : (K *)(tmp + off_alt);
 	unsigned launches = 0;
 	cudaError_t e = cudaMemsetAsync(counts, 0, 64, s);
 	if (e == cudaSuccess) {
@@ -809,7 +828,16 @@ cudaError_t seg_sort_typed(K *keys, uint64_t n_cap, const uint64_t *off, uint32_
 			e = cudaGetLastError();
 			std::swap(src, dst);
 		}
-		if (e == cudaSuccess && (passes & 1)) {
+		if (e == cudaSuccess && (passes & 1) && alt_ext && in_alt) {
+			// The caller takes the long segments from its alternate buffer;
+			// the short ones, sorted in place, are copied there.
+			const uint32_t grid = (uint32_t)std::min<uint64_t>(((uint64_t)S + 7) / 8,
+				(uint64_t)ctx->sm_count * 8);
+			seg_copy_short<K><<<grid, 256, 0, s>>>(alt, keys, off, lists, counts, S);
+			launches++;
+			e = cudaGetLastError();
+			*in_alt = true;
+		} else if (e == cudaSuccess && (passes & 1)) {
 			const uint32_t grid = (uint32_t)std::min<uint64_t>(T_bound,
 				(uint64_t)ctx->sm_count * 8);
 			seg_copy_large<K><<<grid, 256, 0, s>>>(keys, alt, off, tstart, tile_seg, S);
@@ -1064,17 +1092,17 @@ int seg_sort_num_variants() { return kNumVariants; }
 
 cudaError_t seg_sort(void *keys, uint64_t n_cap, const uint64_t *off, size_t S,
 	int key_bytes, int sort_bits, int variant, CCLContext *ctx, cudaStream_t s,
-	GError **err) {
+	GError **err, void *alt, bool *in_alt) {
 	if (S >= (1ull << 31)) {
 		set_error(err, CLO_ERROR_ARGS, "Too many segments (%zu)", S);
 		return cudaErrorInvalidValue;
 	}
 	const uint32_t s32 = (uint32_t)S;
 	switch (key_bytes) {
-	case 1: return seg_sort_typed<uint8_t>((uint8_t *)keys, n_cap, off, s32, sort_bits, variant, ctx, s, err);
-	case 2: return seg_sort_typed<uint16_t>((uint16_t *)keys, n_cap, off, s32, sort_bits, variant, ctx, s, err);
-	case 4: return seg_sort_typed<uint32_t>((uint32_t *)keys, n_cap, off, s32, sort_bits, variant, ctx, s, err);
-	case 8: return seg_sort_typed<uint64_t>((uint64_t *)keys, n_cap, off, s32, sort_bits, variant, ctx, s, err);
+	case 1: return seg_sort_typed<uint8_t>((uint8_t *)keys, n_cap, off, s32, sort_bits, variant, ctx, s, err, (uint8_t *)alt, in_alt);
+	case 2: return seg_sort_typed<uint16_t>((uint16_t *)keys, n_cap, off, s32, sort_bits, variant, ctx, s, err, (uint16_t *)alt, in_alt);
+	case 4: return seg_sort_typed<uint32_t>((uint32_t *)keys, n_cap, off, s32, sort_bits, variant, ctx, s, err, (uint32_t *)alt, in_alt);
+	case 8: return seg_sort_typed<uint64_t>((uint64_t *)keys, n_cap, off, s32, sort_bits, variant, ctx, s, err, (uint64_t *)alt, in_alt);
 	}
 	set_error(err, CLO_ERROR_ARGS, "Unsupported key width %d", key_bytes);
 	return cudaErrorInvalidValue;

@@ -677,10 +677,9 @@ bool satradix_host_pipelined(CloSort *s, CCLQueue *q, const void *h_in, void *h_
 	const size_t off_rel = off_b + (n * eb + 255) / 256 * 256;
 	const size_t rel_words = (size_t)groups * (kBucketsPerGroup + 1);
 	char *dev = (char *)clo::tmp_alloc(ctx, off_rel + rel_words * 8, cs, err);
-	uint64_t *h_rel = nullptr;
+	std::vector<uint64_t> h_rel(rel_words);
 	std::vector<cudaEvent_t> evs;
 	bool ok = dev != nullptr;
-	ok = ok && cuda_ok(cudaMallocHost(&h_rel, rel_words * 8), err, "cudaMallocHost");
 	char *da = dev, *db = dev + off_b;
 	uint64_t *d_rel = (uint64_t *)(dev + off_rel);
 	uint32_t counts[256];
@@ -696,17 +695,24 @@ bool satradix_host_pipelined(CloSort *s, CCLQueue *q, const void *h_in, void *h_
 			for (int j = 0; j <= kBucketsPerGroup; ++j)
 				h_rel[(size_t)g * (kBucketsPerGroup + 1) + j] =
 					off[g * kBucketsPerGroup + j] - off[g * kBucketsPerGroup];
-		ok = cuda_ok(cudaMemcpyAsync(d_rel, h_rel, rel_words * 8, cudaMemcpyHostToDevice, cs),
-			err, "offsets");
+		// Pageable source: the call stages the copy before it returns.
+		ok = cuda_ok(cudaMemcpyAsync(d_rel, h_rel.data(), rel_words * 8,
+			cudaMemcpyHostToDevice, cs), err, "offsets");
 	}
 	for (int g = 0; g < groups && ok; ++g) {
 		const uint64_t base = off[g * kBucketsPerGroup];
 		const uint64_t len = off[(g + 1) * kBucketsPerGroup] - base;
 		if (len == 0) continue;
 		char *gp = db + base * eb;
+		// The input buffer is free after the partition: it is the groups'
+		// second buffer, and a group whose passes end there is copied from
+		// there.
+		bool in_alt = false;
 		if (bits > 8)
 			ok = clo::seg_sort(gp, len, d_rel + (size_t)g * (kBucketsPerGroup + 1),
-				kBucketsPerGroup, (int)eb, bits - 8, 0, ctx, cs, err) == cudaSuccess;
+				kBucketsPerGroup, (int)eb, bits - 8, 0, ctx, cs, err, da + base * eb,
+				&in_alt) == cudaSuccess;
+		if (in_alt) gp = da + base * eb;
 		cudaEvent_t ev = nullptr;
 		ok = ok && cuda_ok(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), err, "event");
 		if (!ok) break;
@@ -721,7 +727,6 @@ bool satradix_host_pipelined(CloSort *s, CCLQueue *q, const void *h_in, void *h_
 	ok = ok && clo::check_device_status(ctx, err);
 	for (cudaEvent_t ev : evs) cudaEventDestroy(ev);
 	cudaStreamDestroy(xs);
-	if (h_rel) cudaFreeHost(h_rel);
 	clo::tmp_free(dev, cs);
 	cudaStreamSynchronize(cs);
 	return ok;

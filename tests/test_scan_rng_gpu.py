@@ -191,3 +191,19 @@ def test_rng_unknown_and_bad_seed_args(clops, ctx, queue):
     with pytest.raises(clops.CloError) as ei:
         clops.Rng(ctx, queue, "lcg", clops.CLO_RNG_SEED_EXT_HOST, 10, seeds=None)
     assert ei.value.code == clops.CLO_ERROR_ARGS
+
+
+# ------------------------------------------ large host-data scans (chunked)
+@pytest.mark.parametrize("in_code,in_dt,sum_code,sum_dt,n", [
+    (5, np.uint32, 7, np.uint64, (1 << 22) + 12345),
+    (0, np.int8, 4, np.int32, (1 << 25) + 7),
+    (7, np.uint64, 7, np.uint64, 1 << 24),
+    (4, np.int32, 5, np.uint32, (1 << 24) + (1 << 23))])
+def test_scan_host_data_large_matches_oracle(clops, ctx, queue, in_code, in_dt, sum_code,
+                                             sum_dt, n):
+    a = keys_of_type(900 + in_code, n, in_dt)
+    out = np.zeros(n, sum_dt)
+    sc = clops.Scanner(ctx, in_code, sum_code)
+    sc.scan_host(queue, a, out)
+    np.testing.assert_array_equal(out, oracle.scan(a, in_code, sum_dt))
+    sc.destroy()
