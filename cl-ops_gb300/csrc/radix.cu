@@ -811,13 +811,13 @@ radix_pass_chunked(const K *__restrict__ kin, K *__restrict__ kout,
 			atomicOr(my_match + d, 1u << lane);
 			__syncwarp();
 			const uint32_t peers = my_match[d];
-			const uint32_t start = my_hist[d];
 			__syncwarp();
 			const uint32_t below = __popc(peers & lt);
-			if (below == 0) {
-				my_hist[d] = start + __popc(peers);
-				my_match[d] = 0;
-			}
+			// The lowest peer advances the warp's counter and clears the
+			// mask; the counter's old value reaches its peers by shuffle.
+			uint32_t start = atomic_add_shared_if(below == 0, my_hist + d, __popc(peers));
+			if (below == 0) my_match[d] = 0;
+			start = __shfl_sync(0xffffffffu, start, __ffs(peers) - 1);
 			__syncwarp();
 			const uint32_t pos = start + below;
 			if (pos < (uint32_t)TILE) sk[pos] = k[j];
