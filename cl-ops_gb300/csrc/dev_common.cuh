@@ -70,5 +70,39 @@ __device__ __forceinline__ void report_timeout(int *status, int code,
 	if (atomicCAS(status, 0, code) == 0) atomicExch(status + 1, detail);
 }
 
+// old = atomicAdd(p, v) on shared memory for the lanes where `pred` holds,
+// as a predicated instruction (no branch around it).
+__device__ __forceinline__ uint32_t atomic_add_shared_if(bool pred, uint32_t *p,
+	uint32_t v) {
+	uint32_t old = 0;
+	const uint32_t addr = (uint32_t)__cvta_generic_to_shared(p);
+	asm volatile(
+		"{\n\t.reg .pred q;\n\t"
+		"setp.ne.u32 q, %1, 0;\n\t"
+		"@q atom.shared.add.u32 %0, [%2], %3;\n\t}"
+		: "+r"(old) : "r"((uint32_t)pred), "r"(addr), "r"(v) : "memory");
+	return old;
+}
+
+// Stable rank of a key among the lanes of its warp holding the same digit
+// `d` in this round, and the warp's run position for it: peers are found
+// through a shared-memory OR into match[d] (cleared again by the lowest
+// peer), the lowest peer advances the warp's counter hist[d] by the number
+// of peers, and the counter's old value reaches the peers by shuffle.
+// Returns the key's position (old counter + lanes below it with d).
+__device__ __forceinline__ uint32_t warp_rank_digit(uint32_t *match, uint32_t *hist,
+	uint32_t d, uint32_t lane, uint32_t lt) {
+	atomicOr(match + d, 1u << lane);
+	__syncwarp();
+	const uint32_t peers = match[d];
+	__syncwarp();
+	const uint32_t below = __popc(peers & lt);
+	uint32_t start = atomic_add_shared_if(below == 0, hist + d, __popc(peers));
+	if (below == 0) match[d] = 0;
+	start = __shfl_sync(0xffffffffu, start, __ffs(peers) - 1);
+	__syncwarp();
+	return start + below;
+}
+
 }  // namespace dev
 }  // namespace clo

@@ -9,18 +9,19 @@
 // Per sort:
 //   1. radix_upsweep: one read of the keys builds the 256-bin histogram
 //      of every digit position at once.
-//   2. per digit position, radix_onesweep (one launch per pass):
-//      a. a tile of keys (8192 x 32-bit or 4096 x 64-bit) is loaded
-//         warp-striped, so that each warp's keys are in index order;
-//      b. warp-level multisplit ranks every key among equal digits of its
-//         warp (stable: lanes in order, rounds in order), with per-warp
-//         counters in shared memory;
-//      c. per-digit counts are combined across warps, published for the
-//         tile, and a decoupled lookback (one thread per digit, bounded
-//         waits) yields each digit's global offset;
-//      d. keys (then values) are staged in shared memory in tile-sorted
+//   2. per digit position, radix_pass_chunked (one launch per pass), one
+//      CTA per contiguous chunk of 4096-key tiles (2048 for 64-bit keys):
+//      a. the CTA counts its chunk's digits, publishes the counts and looks
+//         back over the preceding chunks once (decoupled lookback, one
+//         thread per digit, bounded waits) for its digits' global offsets;
+//      b. per tile, keys are loaded warp-striped (a warp's keys are in
+//         index order) and ranked among equal digits of their warp, stably
+//         (lanes in order, rounds in order): peers found through a
+//         shared-memory OR mask, the lowest advancing the warp's counter;
+//      c. keys (then values) are staged in shared memory in tile-sorted
 //         order and written out so that consecutive threads write
-//         consecutive addresses of a digit's run.
+//         consecutive addresses of a digit's run, each digit's run
+//         continuing where the previous tile's ended.
 // Passes whose digit has a single populated bin are skipped (the order of
 // a stable sort by a constant digit is the identity).
 //
@@ -38,19 +39,11 @@ namespace {
 
 constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;
-constexpr int kThreads = 512;
-constexpr int kWarps = kThreads / 32;
 
 // Tile status word: 2-bit flag | 30-bit count.
 constexpr uint32_t kStAgg = 1u << 30;
 constexpr uint32_t kStPrefix = 2u << 30;
 constexpr uint32_t kStValue = (1u << 30) - 1u;
-
-template <typename K>
-struct KeyCfg {
-	static constexpr int kKpt = sizeof(K) <= 4 ? 16 : 8;
-	static constexpr int kTile = kThreads * kKpt;
-};
 
 template <typename K>
 __device__ __forceinline__ uint32_t digit_of(K k, int shift) {
@@ -129,19 +122,6 @@ struct PassArgs {
 	int shift;
 };
 
-// Lanes of the warp holding the same 8-bit digit, from one ballot per bit
-// (ALU votes; warp match would run on the much slower ADU pipe).
-__device__ __forceinline__ uint32_t peer_mask(uint32_t d) {
-	uint32_t m = 0xffffffffu;
-#pragma unroll
-	for (int b = 0; b < kRadixBits; ++b) {
-		const uint32_t bit = (d >> b) & 1u;
-		const uint32_t bal = __ballot_sync(0xffffffffu, bit);
-		m &= bit ? bal : ~bal;
-	}
-	return m;
-}
-
 // Lookback window: predecessor statuses read per round trip per digit.
 constexpr int kLookWindow = 32;
 
@@ -180,422 +160,6 @@ __device__ __forceinline__ bool lookback_window(const uint32_t *status, int digi
 	return done;
 }
 
-// old = atomicAdd(p, v) on shared memory for the lanes where `pred` holds,
-// as a predicated instruction (no branch around it).
-__device__ __forceinline__ uint32_t atomic_add_shared_if(bool pred, uint32_t *p,
-	uint32_t v) {
-	uint32_t old = 0;
-	const uint32_t addr = (uint32_t)__cvta_generic_to_shared(p);
-	asm volatile(
-		"{\n\t.reg .pred q;\n\t"
-		"setp.ne.u32 q, %1, 0;\n\t"
-		"@q atom.shared.add.u32 %0, [%2], %3;\n\t}"
-		: "+r"(old) : "r"((uint32_t)pred), "r"(addr), "r"(v) : "memory");
-	return old;
-}
-
-template <typename K, typename V, bool HAS_V>
-__global__ void __launch_bounds__(kThreads, (HAS_V || sizeof(K) > 4) ? 2 : 3)
-radix_onesweep(const K *__restrict__ kin, K *__restrict__ kout,
-	const V *__restrict__ vin, V *__restrict__ vout, PassArgs a) {
-	constexpr int KPT = KeyCfg<K>::kKpt;
-	constexpr int TILE = KeyCfg<K>::kTile;
-	// Narrower window when the value pass keeps tile positions live.
-	constexpr int kWin = kLookWindow / 2;
-	extern __shared__ __align__(16) unsigned char smem[];
-	uint32_t *s_hist = reinterpret_cast<uint32_t *>(smem);   // [kWarps][256]
-	uint32_t *s_match = s_hist + kWarps * kRadix;            // [kWarps][256]
-	uint32_t *s_tile_off = s_match + kWarps * kRadix;        // [256]
-	uint32_t *s_glob = s_tile_off + kRadix;                  // [256]
-	uint32_t *s_misc = s_glob + kRadix;                      // [64]
-	unsigned char *s_stage = reinterpret_cast<unsigned char *>(s_misc + 64);
-
-	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-	uint32_t *my_hist = s_hist + warp * kRadix;
-	uint32_t *my_match = s_match + warp * kRadix;
-	if (tid == 0) s_misc[0] = atomicAdd(a.tile_counter, 1u);
-	for (int i = lane; i < kRadix; i += 32) {
-		my_hist[i] = 0;
-		my_match[i] = 0;
-	}
-	__syncthreads();
-	const uint32_t tile = s_misc[0];
-	const size_t tile_base = (size_t)tile * TILE;
-	const size_t wbase = tile_base + (size_t)warp * (KPT * 32);
-	const int shift = a.shift;
-
-	// a. load keys, warp-striped (out-of-range keys read as all-ones so they
-	//    rank last within digit 255 and are never written).
-	K k[KPT];
-#pragma unroll
-	for (int j = 0; j < KPT; ++j) {
-		size_t idx = wbase + (size_t)j * 32 + lane;
-		k[j] = idx < a.n ? kin[idx] : (K)~(K)0;
-	}
-
-	// b. early per-warp digit counts (order-free), so the tile can publish
-	//    its aggregate before it ranks.
-#pragma unroll
-	for (int j = 0; j < KPT; ++j) atomicAdd(my_hist + digit_of(k[j], shift), 1u);
-	__syncthreads();
-
-	// c. per-digit tile counts and warp prefixes; publish the aggregate;
-	//    exclusive scans over digits of the tile counts and of the global
-	//    histogram of this digit position.
-	uint32_t tile_cnt = 0;
-	if (tid < kRadix) {
-		uint32_t sum = 0;
-#pragma unroll
-		for (int w = 0; w < kWarps; ++w) {
-			uint32_t c = s_hist[w * kRadix + tid];
-			s_hist[w * kRadix + tid] = sum;
-			sum += c;
-		}
-		tile_cnt = sum;
-		uint32_t *st = a.status + (size_t)tile * kRadix + tid;
-		if (tile == 0) dev::st_relaxed_u32(st, kStPrefix | tile_cnt);
-		else dev::st_relaxed_u32(st, kStAgg | tile_cnt);
-		a.status_next[(size_t)tile * kRadix + tid] = 0;
-		uint32_t inc = tile_cnt;
-#pragma unroll
-		for (int d = 1; d < 32; d <<= 1) {
-			uint32_t t = __shfl_up_sync(0xffffffffu, inc, d);
-			if (lane >= d) inc += t;
-		}
-		if (lane == 31) s_misc[8 + warp] = inc;
-		s_tile_off[tid] = inc - tile_cnt;
-	}
-	if (tid >= kRadix && tid < 2 * kRadix) {
-		int d = tid - kRadix;
-		uint32_t hv = a.hist[d];
-		uint32_t inc = hv;
-#pragma unroll
-		for (int s = 1; s < 32; s <<= 1) {
-			uint32_t t = __shfl_up_sync(0xffffffffu, inc, s);
-			if (lane >= s) inc += t;
-		}
-		if (lane == 31) s_misc[16 + (warp - 8)] = inc;
-		s_glob[d] = inc - hv;
-	}
-	__syncthreads();
-	uint32_t digit_base = 0;
-	if (tid < kRadix) {
-		uint32_t woff = 0, goff = 0;
-#pragma unroll
-		for (int w = 0; w < 8; ++w) {
-			if (w < warp) {
-				woff += s_misc[8 + w];
-				goff += s_misc[16 + w];
-			}
-		}
-		const uint32_t to = s_tile_off[tid] + woff;
-		s_tile_off[tid] = to;
-		digit_base = s_glob[tid] + goff;
-		// Tile position where each warp's run of digit tid starts.
-#pragma unroll
-		for (int w = 0; w < kWarps; ++w) s_hist[w * kRadix + tid] += to;
-	}
-	__syncthreads();
-
-	// d. lookback over predecessor tiles (warps 0..7, one thread per digit)
-	//    while warps 8..15 already rank: a short window, then wide windows;
-	//    an unpublished predecessor is polled alone (bounded).
-	if (tid < kRadix) {
-		uint32_t excl = 0;
-		if (tile > 0) {
-			long long base = (long long)tile - 1;
-			uint32_t iter = 0;
-			bool done = lookback_window<4>(a.status, tid, base, excl);
-			while (!done && base >= 0) {
-				uint32_t sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + tid);
-				while ((sv & ~kStValue) == 0) {
-					if (++iter >= dev::kSpinLimit) break;
-					dev::backoff(iter);
-					sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + tid);
-				}
-				if ((sv & ~kStValue) == 0) {
-					dev::report_timeout(a.dev_status, DEV_ERR_LOOKBACK_TIMEOUT, (int)tile);
-					break;
-				}
-				done = lookback_window<kWin>(a.status, tid, base, excl);
-			}
-			dev::st_relaxed_u32(a.status + (size_t)tile * kRadix + tid,
-				kStPrefix | (excl + tile_cnt));
-		}
-		s_glob[tid] = digit_base + excl - s_tile_off[tid];
-	}
-
-	// e. stable ranks within each warp, written straight to tile positions:
-	//    lanes holding the same digit in a round find each other through a
-	//    shared-memory OR (in lane order, rounds in index order); the lowest
-	//    of them advances the warp's run start and clears the mask.
-	K *sk = reinterpret_cast<K *>(s_stage);
-	uint32_t tpos[HAS_V ? KPT : 1];
-	const uint32_t lt = dev::lanemask_lt();
-#pragma unroll
-	for (int j = 0; j < KPT; ++j) {
-		const uint32_t d = digit_of(k[j], shift);
-		atomicOr(my_match + d, 1u << lane);
-		__syncwarp();
-		const uint32_t peers = my_match[d];
-		const uint32_t start = my_hist[d];
-		__syncwarp();
-		const uint32_t below = __popc(peers & lt);
-		if (below == 0) {
-			my_hist[d] = start + __popc(peers);
-			my_match[d] = 0;
-		}
-		__syncwarp();
-		const uint32_t pos = start + below;
-		if (pos < (uint32_t)TILE) sk[pos] = k[j];
-		if (HAS_V) tpos[j] = pos;
-	}
-	__syncthreads();
-
-	// f. write each digit run out coalesced.
-	uint32_t outpos[HAS_V ? KPT : 1];
-#pragma unroll
-	for (int i = 0; i < KPT; ++i) {
-		int p = i * kThreads + tid;
-		K key = sk[p];
-		size_t o = (size_t)s_glob[digit_of(key, shift)] + p;
-		if (o < a.n) kout[o] = key;
-		if (HAS_V) outpos[i] = (uint32_t)o;
-	}
-	if (HAS_V) {
-		V v[KPT];
-#pragma unroll
-		for (int j = 0; j < KPT; ++j) {
-			size_t idx = wbase + (size_t)j * 32 + lane;
-			v[j] = idx < a.n ? vin[idx] : (V)0;
-		}
-		__syncthreads();
-		V *sv = reinterpret_cast<V *>(s_stage);
-#pragma unroll
-		for (int j = 0; j < KPT; ++j)
-			if (tpos[j] < (uint32_t)TILE) sv[tpos[j]] = v[j];
-		__syncthreads();
-#pragma unroll
-		for (int i = 0; i < KPT; ++i) {
-			int p = i * kThreads + tid;
-			if (outpos[i] < a.n) vout[outpos[i]] = sv[p];
-		}
-	}
-}
-
-// ----------------------------------------------------- pipelined pass
-// Keys-only pass run by persistent CTAs with two tiles in flight each.
-// Per iteration a CTA counts, publishes and ranks its current tile c; in
-// the same interval its warps 0..7 look back for its previous tile p,
-// whose predecessors have had a whole iteration to publish, so the window
-// usually ends at the first round trip; then it loads the next tile's keys
-// into registers and writes p out while those loads are in flight.
-// Deadlock-free: a tile publishes its aggregate before its CTA waits on
-// anything, and a CTA holding an unpublished (just claimed) tile waits only
-// on tiles below its previous tile, so the lowest unpublished tile always
-// belongs to a CTA whose wait ends.
-template <typename K>
-__device__ __forceinline__ void load_tile_keys(K (&k)[KeyCfg<K>::kKpt],
-	const K *__restrict__ kin, size_t n, uint32_t tile, int warp, int lane) {
-	constexpr int KPT = KeyCfg<K>::kKpt;
-	const size_t wbase = (size_t)tile * KeyCfg<K>::kTile + (size_t)warp * (KPT * 32);
-#pragma unroll
-	for (int j = 0; j < KPT; ++j) {
-		size_t idx = wbase + (size_t)j * 32 + lane;
-		k[j] = idx < n ? kin[idx] : (K)~(K)0;
-	}
-}
-
-template <typename K>
-__global__ void __launch_bounds__(kThreads, 2)
-radix_onesweep_pp(const K *__restrict__ kin, K *__restrict__ kout, PassArgs a,
-	uint32_t num_tiles) {
-	constexpr int KPT = KeyCfg<K>::kKpt;
-	constexpr int TILE = KeyCfg<K>::kTile;
-	constexpr int kWin = kLookWindow / 2;
-	extern __shared__ __align__(16) unsigned char smem[];
-	uint32_t *s_hist = reinterpret_cast<uint32_t *>(smem);   // [kWarps][256]
-	uint32_t *s_match = s_hist + kWarps * kRadix;            // [kWarps][256]
-	uint32_t *s_tile_off = s_match + kWarps * kRadix;        // [2][256]
-	uint32_t *s_tile_cnt = s_tile_off + 2 * kRadix;          // [2][256]
-	uint32_t *s_glob = s_tile_cnt + 2 * kRadix;              // [256]
-	uint32_t *s_dbase = s_glob + kRadix;                     // [256]
-	uint32_t *s_half = s_dbase + kRadix;                     // [2][256]
-	uint32_t *s_part = s_half + 2 * kRadix;                  // [256]
-	uint32_t *s_misc = s_part + kRadix;                      // [64]
-	K *s_stage = reinterpret_cast<K *>(s_misc + 64);         // [2][TILE]
-
-	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-	uint32_t *my_hist = s_hist + warp * kRadix;
-	uint32_t *my_match = s_match + warp * kRadix;
-	const int shift = a.shift;
-	const uint32_t lt = dev::lanemask_lt();
-
-	// Global digit base of this pass: exclusive scan of its histogram.
-	if (tid >= kRadix && tid < 2 * kRadix) {
-		const int d = tid - kRadix;
-		const uint32_t hv = a.hist[d];
-		uint32_t inc = hv;
-#pragma unroll
-		for (int s = 1; s < 32; s <<= 1) {
-			uint32_t t = __shfl_up_sync(0xffffffffu, inc, s);
-			if (lane >= s) inc += t;
-		}
-		if (lane == 31) s_misc[16 + (warp - 8)] = inc;
-		s_dbase[d] = inc - hv;
-	}
-	if (tid == 0) s_misc[0] = atomicAdd(a.tile_counter, 1u);
-	for (int i = lane; i < kRadix; i += 32) my_match[i] = 0;
-	__syncthreads();
-	if (tid >= kRadix && tid < 2 * kRadix) {
-		uint32_t goff = 0;
-#pragma unroll
-		for (int w = 8; w < 16; ++w)
-			if (w < warp) goff += s_misc[16 + (w - 8)];
-		s_dbase[tid - kRadix] += goff;
-	}
-	uint32_t c = s_misc[0];
-	K k[KPT];
-	if (c < num_tiles) load_tile_keys<K>(k, kin, a.n, c, warp, lane);
-	long long p = -1;
-	int it = 0;
-	for (;;) {
-		const bool have_c = c < num_tiles;
-		const int sc = it & 1, sp = sc ^ 1;
-		if (have_c) {
-			for (int i = lane; i < kRadix; i += 32) my_hist[i] = 0;
-			__syncwarp();
-#pragma unroll
-			for (int j = 0; j < KPT; ++j) atomicAdd(my_hist + digit_of(k[j], shift), 1u);
-		}
-		__syncthreads();  // counts complete; previous write-out done
-		// Warp prefixes per digit, by all 512 threads: thread (d, h) takes
-		// warps 8h..8h+7 of digit d with independent loads.
-		const int pd = tid & (kRadix - 1), ph = tid >> 8;
-		uint32_t cw[8];
-		if (have_c) {
-#pragma unroll
-			for (int i = 0; i < 8; ++i) cw[i] = s_hist[(8 * ph + i) * kRadix + pd];
-			uint32_t run = 0;
-#pragma unroll
-			for (int i = 0; i < 8; ++i) {
-				uint32_t t = cw[i];
-				cw[i] = run;
-				run += t;
-			}
-			s_half[ph * kRadix + pd] = run;
-		}
-		__syncthreads();
-		if (have_c) {
-			const uint32_t lo = s_half[pd];
-			const uint32_t sum = lo + s_half[kRadix + pd];
-			if (ph == 1) {
-#pragma unroll
-				for (int i = 0; i < 8; ++i) cw[i] += lo;
-			} else {
-				s_tile_cnt[sc * kRadix + pd] = sum;
-				uint32_t *st = a.status + (size_t)c * kRadix + pd;
-				if (c == 0) dev::st_relaxed_u32(st, kStPrefix | sum);
-				else dev::st_relaxed_u32(st, kStAgg | sum);
-				a.status_next[(size_t)c * kRadix + pd] = 0;
-				uint32_t inc = sum;
-#pragma unroll
-				for (int d = 1; d < 32; d <<= 1) {
-					uint32_t t = __shfl_up_sync(0xffffffffu, inc, d);
-					if (lane >= d) inc += t;
-				}
-				if (lane == 31) s_misc[8 + warp] = inc;
-				s_part[pd] = inc - sum;
-			}
-		}
-		if (tid == 0) s_misc[1] = have_c ? atomicAdd(a.tile_counter, 1u) : num_tiles;
-		__syncthreads();
-		if (have_c) {
-			uint32_t woff = 0;
-			const int dw = pd >> 5;
-#pragma unroll
-			for (int w = 0; w < 8; ++w)
-				if (w < dw) woff += s_misc[8 + w];
-			const uint32_t to = s_part[pd] + woff;
-#pragma unroll
-			for (int i = 0; i < 8; ++i) s_hist[(8 * ph + i) * kRadix + pd] = to + cw[i];
-			if (ph == 0) s_tile_off[sc * kRadix + pd] = to;
-		}
-		__syncthreads();
-
-		// Lookback for the previous tile (warps 0..7, one digit each).
-		if (p >= 0 && tid < kRadix) {
-			uint32_t excl = 0;
-			if (p > 0) {
-				long long base = p - 1;
-				uint32_t iter = 0;
-				bool done = lookback_window<4>(a.status, tid, base, excl);
-				while (!done && base >= 0) {
-					uint32_t sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + tid);
-					while ((sv & ~kStValue) == 0) {
-						if (++iter >= dev::kSpinLimit) break;
-						dev::backoff(iter);
-						sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + tid);
-					}
-					if ((sv & ~kStValue) == 0) {
-						dev::report_timeout(a.dev_status, DEV_ERR_LOOKBACK_TIMEOUT, (int)p);
-						break;
-					}
-					done = lookback_window<kWin>(a.status, tid, base, excl);
-				}
-				dev::st_relaxed_u32(a.status + (size_t)p * kRadix + tid,
-					kStPrefix | (excl + s_tile_cnt[sp * kRadix + tid]));
-			}
-			s_glob[tid] = s_dbase[tid] + excl - s_tile_off[sp * kRadix + tid];
-		}
-
-		// Stable warp ranks of the current tile, staged in its slot.
-		if (have_c) {
-			K *sk = s_stage + (size_t)sc * TILE;
-#pragma unroll
-			for (int j = 0; j < KPT; ++j) {
-				const uint32_t d = digit_of(k[j], shift);
-				atomicOr(my_match + d, 1u << lane);
-				__syncwarp();
-				const uint32_t peers = my_match[d];
-				const uint32_t start = my_hist[d];
-				__syncwarp();
-				const uint32_t below = __popc(peers & lt);
-				if (below == 0) {
-					my_hist[d] = start + __popc(peers);
-					my_match[d] = 0;
-				}
-				__syncwarp();
-				const uint32_t pos = start + below;
-				if (pos < (uint32_t)TILE) sk[pos] = k[j];
-			}
-		}
-		__syncthreads();  // ranks staged, lookback results and next id visible
-
-		const uint32_t next = s_misc[1];
-		if (next < num_tiles) load_tile_keys<K>(k, kin, a.n, next, warp, lane);
-		if (p >= 0) {
-			const K *sp_stage = s_stage + (size_t)sp * TILE;
-#pragma unroll
-			for (int i = 0; i < KPT; ++i) {
-				const int q = i * kThreads + tid;
-				const K key = sp_stage[q];
-				const size_t o = (size_t)s_glob[digit_of(key, shift)] + q;
-				if (o < a.n) kout[o] = key;
-			}
-		}
-		if (!have_c) break;
-		p = c;
-		c = next;
-		++it;
-	}
-}
-
-template <typename K>
-size_t onesweep_pp_smem() {
-	return (2 * kWarps * kRadix + 9 * kRadix + 64) * sizeof(uint32_t) +
-		2 * (size_t)KeyCfg<K>::kTile * sizeof(K);
-}
 
 // ------------------------------------------------------- chunked pass
 // One CTA per contiguous chunk of tiles (chunks claimed in order from an
@@ -807,19 +371,8 @@ radix_pass_chunked(const K *__restrict__ kin, K *__restrict__ kout,
 		uint32_t tpos[HAS_V ? KPT : 1];
 #pragma unroll
 		for (int j = 0; j < KPT; ++j) {
-			const uint32_t d = digit_of(k[j], shift);
-			atomicOr(my_match + d, 1u << lane);
-			__syncwarp();
-			const uint32_t peers = my_match[d];
-			__syncwarp();
-			const uint32_t below = __popc(peers & lt);
-			// The lowest peer advances the warp's counter and clears the
-			// mask; the counter's old value reaches its peers by shuffle.
-			uint32_t start = atomic_add_shared_if(below == 0, my_hist + d, __popc(peers));
-			if (below == 0) my_match[d] = 0;
-			start = __shfl_sync(0xffffffffu, start, __ffs(peers) - 1);
-			__syncwarp();
-			const uint32_t pos = start + below;
+			const uint32_t pos = dev::warp_rank_digit(my_match, my_hist,
+				digit_of(k[j], shift), lane, lt);
 			if (pos < (uint32_t)TILE) sk[pos] = k[j];
 			if (HAS_V) tpos[j] = pos;
 		}
@@ -883,16 +436,8 @@ void launch_upsweep(int passes, int grid, cudaStream_t s, const K *keys, size_t 
 }
 
 template <typename K, typename V, bool HAS_V>
-size_t onesweep_smem() {
-	constexpr int TILE = KeyCfg<K>::kTile;
-	size_t stage = (size_t)TILE * (sizeof(K) > sizeof(V) || !HAS_V ? sizeof(K) : sizeof(V));
-	return (2 * kWarps * kRadix + 2 * kRadix + 64) * sizeof(uint32_t) + stage;
-}
-
-template <typename K, typename V, bool HAS_V>
 cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
 	CCLContext *ctx, cudaStream_t s, bool allow_skip, GError **err) {
-	constexpr int TILE = KeyCfg<K>::kTile;
 	const int passes = sort_bits / kRadixBits;
 	if (n < 2 || passes == 0) return cudaSuccess;
 	if (n >= (size_t)kStValue) {
@@ -900,15 +445,14 @@ cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
 			"satradix: %zu elements exceed the single-sort limit of 2^30 - 1", n);
 		return cudaErrorInvalidValue;
 	}
-	const size_t tiles = (n + TILE - 1) / TILE;
 	// The chunked pass: tiles of ChunkCfg size, one chunk per CTA.
 	constexpr int CT = kChunkThreads;
 	constexpr int CTILE = ChunkCfg<K, CT>::kTile;
 	const size_t ctiles = (n + CTILE - 1) / CTILE;
 	const uint32_t chunks = (uint32_t)std::min<size_t>(ctiles,
 		(size_t)ChunkCfg<K, CT>::kMinBlocks * ctx->sm_count);
-	// Status slots: one per chunk (chunked pass) or per tile (tile passes).
-	const size_t status_words = std::max<size_t>(tiles, chunks) * kRadix;
+	// Status slots: one per chunk.
+	const size_t status_words = (size_t)chunks * kRadix;
 	// Scratch: [hist passes*256][counters 8][status0][status1][alt keys][alt vals]
 	size_t off_hist = 0;
 	size_t off_cnt = off_hist + (size_t)passes * kRadix * 4;

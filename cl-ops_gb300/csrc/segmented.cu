@@ -277,19 +277,8 @@ __global__ void __launch_bounds__(THREADS) seg_sort_cta(K *keys, const uint64_t 
 			__syncthreads();
 #pragma unroll
 			for (int j = 0; j < KPT; ++j) {
-				const uint32_t d = digit_of(k[j], shift);
-				atomicOr(my_match + d, 1u << lane);
-				__syncwarp();
-				const uint32_t peers = my_match[d];
-				const uint32_t start = my_hist[d];
-				__syncwarp();
-				const uint32_t below = __popc(peers & lt);
-				if (below == 0) {
-					my_hist[d] = start + __popc(peers);
-					my_match[d] = 0;
-				}
-				__syncwarp();
-				sk[start + below] = k[j];
+				sk[dev::warp_rank_digit(my_match, my_hist, digit_of(k[j], shift), lane, lt)] =
+					k[j];
 			}
 			__syncthreads();
 #pragma unroll
@@ -550,19 +539,8 @@ seg_pass(const K *__restrict__ kin, K *__restrict__ kout, SegPassArgs a) {
 		K *sk = reinterpret_cast<K *>(s_stage);
 #pragma unroll
 		for (int j = 0; j < KPT; ++j) {
-			const uint32_t d = digit_of(k[j], shift);
-			atomicOr(my_match + d, 1u << lane);
-			__syncwarp();
-			const uint32_t peers = my_match[d];
-			const uint32_t start = my_hist[d];
-			__syncwarp();
-			const uint32_t below = __popc(peers & lt);
-			if (below == 0) {
-				my_hist[d] = start + __popc(peers);
-				my_match[d] = 0;
-			}
-			__syncwarp();
-			const uint32_t pos = start + below;
+			const uint32_t pos = dev::warp_rank_digit(my_match, my_hist, digit_of(k[j], shift),
+				lane, lt);
 			if (pos < (uint32_t)TILE) sk[pos] = k[j];
 		}
 		__syncthreads();
