@@ -51,63 +51,93 @@ __device__ __forceinline__ uint32_t digit_of(K k, int shift) {
 }
 
 // ----------------------------------------------------------- upsweep
-// Histograms of all `passes` digit positions in one read: one shared-memory
-// atomic per key and digit position, except when all 32 x PER keys of a
-// warp step share the digit (sorted or constant input), which the warp
-// detects with one AND/OR reduction and adds once.
+// Histograms of all `passes` digit positions in one read. Up to four
+// positions count into lane columns: the (d & 1) 16-bit half of word
+// (d >> 1) * 32 + lane per position, shared by the CTA's warps through
+// atomics, so a warp's 32 increments hit 32 different banks; more positions
+// count into one 256-bin row per warp and position. Each thread keeps four
+// 16-byte loads in flight.
+//
+// A column half receives at most kWarps x (keys per thread) increments;
+// the grid is sized so that a thread sees at most kUpsweepKeysPerThread
+// keys (8 x (4096 + 16) < 2^16).
+constexpr int kUpsweepThreads = 256;
+constexpr size_t kUpsweepKeysPerThread = 4096;
+constexpr int kUpsweepColumnPasses = 4;  // most positions counted in columns
+constexpr int kUpsweepInFlight = 4;
+
+template <int PASSES>
+constexpr size_t upsweep_smem() {
+	return PASSES <= kUpsweepColumnPasses ? (size_t)PASSES * (kRadix / 2) * 32 * 4
+										  : (size_t)PASSES * (kUpsweepThreads / 32) * kRadix * 4;
+}
+
 template <typename K, int PASSES>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kUpsweepThreads)
 radix_upsweep(const K *__restrict__ keys, size_t n, uint32_t *__restrict__ hist,
 	int base_shift) {
-	constexpr int passes = PASSES;
-	__shared__ uint32_t h[PASSES][kRadix];
-	for (int i = threadIdx.x; i < PASSES * kRadix; i += blockDim.x) (&h[0][0])[i] = 0;
+	constexpr bool COLS = PASSES <= kUpsweepColumnPasses;
+	constexpr int kWarps = kUpsweepThreads / 32;
+	constexpr int kPosWords = COLS ? (kRadix / 2) * 32 : kWarps * kRadix;
+	extern __shared__ __align__(16) uint32_t up_smem[];
+	for (int i = threadIdx.x; i < PASSES * kPosWords; i += kUpsweepThreads) up_smem[i] = 0;
 	__syncthreads();
-	const int lane = threadIdx.x & 31;
-	const size_t warp_global = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
-	const size_t warps_total = ((size_t)gridDim.x * blockDim.x) >> 5;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	uint32_t *base = COLS ? up_smem + lane : up_smem + warp * kRadix;
+	auto count = [&](int p, K key) {
+		const uint32_t d = digit_of(key, base_shift + p * kRadixBits);
+		if (COLS) atomicAdd(base + p * kPosWords + (d >> 1) * 32, 1u << ((d & 1) << 4));
+		else atomicAdd(base + p * kPosWords + d, 1u);
+	};
 	constexpr int PER = 16 / sizeof(K);  // keys per 16-byte load
 	const bool aligned = ((uintptr_t)keys % 16) == 0;
-	// Full 16-byte chunks, processed 32 per warp step with the fast path.
-	const size_t full_chunks = aligned ? n / PER : 0;
-	const size_t full_steps = full_chunks / 32;
+	const size_t nvec = aligned ? n / PER : 0;
 	const uint4 *kv4 = reinterpret_cast<const uint4 *>(keys);
-	for (size_t step = warp_global; step < full_steps; step += warps_total) {
-		uint4 v = dev::ld_stream_v4(kv4 + step * 32 + lane);
-		const K *e = reinterpret_cast<const K *>(&v);
+	const size_t stride = (size_t)gridDim.x * kUpsweepThreads;
+	size_t i = blockIdx.x * (size_t)kUpsweepThreads + threadIdx.x;
+	for (; i + (kUpsweepInFlight - 1) * stride < nvec; i += kUpsweepInFlight * stride) {
+		uint4 v[kUpsweepInFlight];
 #pragma unroll
-		for (int p = 0; p < passes; ++p) {
-			uint32_t dd[PER];
-			uint32_t a = 0xffffffffu, o = 0u;
+		for (int u = 0; u < kUpsweepInFlight; ++u) v[u] = dev::ld_stream_v4(kv4 + i + u * stride);
 #pragma unroll
-			for (int q = 0; q < PER; ++q) {
-				dd[q] = digit_of(e[q], base_shift + p * kRadixBits);
-				a &= dd[q];
-				o |= dd[q];
-			}
-			uint32_t wa = __reduce_and_sync(0xffffffffu, a);
-			uint32_t wo = __reduce_or_sync(0xffffffffu, o);
-			if (wa == wo) {
-				if (lane == 0) atomicAdd(&h[p][wa], 32u * PER);
-			} else {
+		for (int u = 0; u < kUpsweepInFlight; ++u) {
+			const K *e = reinterpret_cast<const K *>(&v[u]);
 #pragma unroll
-				for (int q = 0; q < PER; ++q) atomicAdd(&h[p][dd[q]], 1u);
-			}
+			for (int p = 0; p < PASSES; ++p)
+#pragma unroll
+				for (int q = 0; q < PER; ++q) count(p, e[q]);
 		}
 	}
+	for (; i < nvec; i += stride) {
+		uint4 v = dev::ld_stream_v4(kv4 + i);
+		const K *e = reinterpret_cast<const K *>(&v);
+#pragma unroll
+		for (int p = 0; p < PASSES; ++p)
+#pragma unroll
+			for (int q = 0; q < PER; ++q) count(p, e[q]);
+	}
 	// Remaining keys (and unaligned inputs): one key per thread.
-	const size_t done = full_steps * 32 * PER;
-	const size_t tid_global = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-	const size_t threads_total = (size_t)gridDim.x * blockDim.x;
-	for (size_t i = done + tid_global; i < n; i += threads_total) {
-		K key = keys[i];
-		for (int p = 0; p < passes; ++p)
-			atomicAdd(&h[p][digit_of(key, base_shift + p * kRadixBits)], 1u);
+	for (size_t j = nvec * PER + blockIdx.x * (size_t)kUpsweepThreads + threadIdx.x; j < n;
+		 j += stride) {
+		const K key = keys[j];
+#pragma unroll
+		for (int p = 0; p < PASSES; ++p) count(p, key);
 	}
 	__syncthreads();
-	for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) {
-		uint32_t v = (&h[0][0])[i];
-		if (v) atomicAdd(hist + i, v);
+	for (int b = threadIdx.x; b < PASSES * kRadix; b += kUpsweepThreads) {
+		const int p = b / kRadix, d = b % kRadix;
+		uint32_t v = 0;
+		if (COLS) {
+			// Digit d's 32 column halves, from a rotated start (no conflicts).
+			const uint32_t *row = up_smem + p * kPosWords + (d >> 1) * 32;
+			const int hs = (d & 1) << 4;
+#pragma unroll 8
+			for (int c = 0; c < 32; ++c) v += (row[(c + lane) & 31] >> hs) & 0xFFFFu;
+		} else {
+#pragma unroll
+			for (int w = 0; w < kWarps; ++w) v += up_smem[p * kPosWords + w * kRadix + d];
+		}
+		if (v) atomicAdd(hist + b, v);
 	}
 }
 
@@ -169,69 +199,155 @@ __device__ __forceinline__ bool lookback_window(const uint32_t *status, int digi
 // pass instead of one per tile, so no tile ever waits on another CTA --
 // then ranks and scatters its tiles in order, each digit's run continuing
 // where the previous tile's ended. The counting read costs key-size bytes
-// per key on top of the pass's read and write. THREADS is 256 or 512;
-// with 256 threads (4096-key tiles) four CTAs share an SM and hide each
-// other's per-tile latency.
+// per key on top of the pass's read and write. With 256 threads
+// (4096-key tiles) four CTAs share an SM and hide each other's per-tile
+// latency.
+//
+// Shared-memory work per key is what bounds the pass, so both counting
+// steps and the ranking are built to touch few shared words:
+//  - phase 1 counts into lane columns: digit d of lane l is the (d & 1)
+//    16-bit half of word (d >> 1) * 32 + l, shared by the CTA's warps
+//    through atomics. A warp's 32 increments hit 32 different banks.
+//  - phase 2 ranks in half-warp units (16 lanes, KPT rounds): the unit's
+//    word for digit d holds the unit's next tile position for d in its
+//    upper half and the round's peer mask in its lower half, so a round is
+//    one OR, one read and one store by the lowest peer.
 template <typename K, int THREADS>
 struct ChunkCfg {
+	static_assert(THREADS == kRadix, "one thread per digit in the per-tile scans");
 	static constexpr int kWarps = THREADS / 32;
+	static constexpr int kUnits = 2 * kWarps;          // half-warp ranking units
 	static constexpr int kKpt = sizeof(K) <= 4 ? 16 : 8;
+	static constexpr int kUnitKeys = 16 * kKpt;        // a unit's keys in one tile
 	static constexpr int kTile = THREADS * kKpt;
-	static constexpr int kHalves = THREADS / kRadix;          // 1 or 2
-	static constexpr int kWarpsPerHalf = kWarps / kHalves;    // 8
-	static constexpr int kMinBlocks = THREADS == 256 ? 4 : 2;
+	// Largest chunk: a lane-column counter half receives at most kWarps x
+	// (keys per thread) = kWarps x (2^20 / THREADS + 4) < 2^16 increments.
+	static constexpr size_t kMaxChunkKeys = (size_t)1 << 20;
 };
 
+// Chunks (CTAs) of a pass over ctiles tiles: one per resident CTA
+// (per_sm x SMs), more when the chunks would exceed kMaxChunkKeys.
+template <typename K>
+uint32_t chunk_count(size_t ctiles, int sm_count, int per_sm) {
+	using Cfg = ChunkCfg<K, kChunkThreads>;
+	constexpr size_t kMaxTiles = Cfg::kMaxChunkKeys / Cfg::kTile;
+	const size_t c = std::max<size_t>((size_t)std::max(per_sm, 1) * sm_count,
+		(ctiles + kMaxTiles - 1) / kMaxTiles);
+	return (uint32_t)std::max<size_t>(std::min(c, ctiles), 1);
+}
+
+// Ranking and count rows: 256 digits each, 264 words apart, odd rows 8
+// words later, so rows 2w and 2w + 1 (the two units of warp w) hold a digit
+// 16 banks apart and a digit both halves of a warp hold does not conflict.
+constexpr int kRowWords = kRadix + 8;
+__device__ __forceinline__ int row_of(int r) { return r * kRowWords + (r & 1) * 8; }
+
+// Keys of one unit in a tile, round-major: round j of lane l holds key
+// ubase + 16 j + l, so the unit's (round, lane) order is index order.
 template <typename K, int THREADS>
 __device__ __forceinline__ void chunk_load_keys(K (&k)[ChunkCfg<K, THREADS>::kKpt],
-	const K *__restrict__ kin, size_t n, uint32_t tile, int warp, int lane) {
-	constexpr int KPT = ChunkCfg<K, THREADS>::kKpt;
-	const size_t wbase = (size_t)tile * ChunkCfg<K, THREADS>::kTile +
-		(size_t)warp * (KPT * 32);
+	const K *__restrict__ kin, size_t n, uint32_t tile, int unit, int l16) {
+	using Cfg = ChunkCfg<K, THREADS>;
+	const size_t ubase = (size_t)tile * Cfg::kTile + (size_t)unit * Cfg::kUnitKeys;
 #pragma unroll
-	for (int j = 0; j < KPT; ++j) {
-		size_t idx = wbase + (size_t)j * 32 + lane;
+	for (int j = 0; j < Cfg::kKpt; ++j) {
+		size_t idx = ubase + (size_t)j * 16 + l16;
 		k[j] = idx < n ? kin[idx] : (K)~(K)0;
 	}
 }
 
+// Values of one unit in a tile, in the keys' layout.
+template <typename K, typename V, int THREADS>
+__device__ __forceinline__ void chunk_load_vals(V (&v)[ChunkCfg<K, THREADS>::kKpt],
+	const V *__restrict__ vin, size_t n, uint32_t tile, int unit, int l16) {
+	using Cfg = ChunkCfg<K, THREADS>;
+	const size_t ubase = (size_t)tile * Cfg::kTile + (size_t)unit * Cfg::kUnitKeys;
+#pragma unroll
+	for (int j = 0; j < Cfg::kKpt; ++j) {
+		size_t idx = ubase + (size_t)j * 16 + l16;
+		v[j] = idx < n ? vin[idx] : (V)0;
+	}
+}
+
+// Stable rank of a key within its half-warp unit for one round: w is the
+// unit's word for the key's digit (next position << 16 | peer mask). Lanes
+// OR in their bit and read the word back; the lowest peer stores the
+// advanced position with the mask cleared. Returns the key's position.
+__device__ __forceinline__ uint32_t unit_rank_digit(uint32_t *w, uint32_t l16,
+	uint32_t lt16) {
+	atomicOr(w, 1u << l16);
+	__syncwarp();
+	const uint32_t v = *w;
+	__syncwarp();
+	const uint32_t peers = v & 0xFFFFu;
+	const uint32_t below = __popc(peers & lt16);
+	if (below == 0) *w = (v & 0xFFFF0000u) + ((uint32_t)__popc(peers) << 16);
+	__syncwarp();
+	return (v >> 16) + below;
+}
+
+// Shared memory of the pass: the ranking words, the unit counts, five
+// 256-entry tables, and the key (and value) stage of one tile.
 template <typename K, typename V, bool HAS_V, int THREADS>
-__global__ void __launch_bounds__(THREADS, ChunkCfg<K, THREADS>::kMinBlocks)
+constexpr size_t chunked_smem() {
+	using Cfg = ChunkCfg<K, THREADS>;
+	return ((Cfg::kUnits + Cfg::kUnits / 2) * kRowWords + 4 * kRadix + 64) * sizeof(uint32_t) +
+		(size_t)Cfg::kTile * (sizeof(K) + (HAS_V ? sizeof(V) : 0));
+}
+
+// Resident CTAs per SM the pass is compiled for: four for keys only, three
+// with values (keys and values of a tile stay in registers), fewer when
+// the shared memory (228 KB per SM, 1 KB reserved per CTA) allows fewer.
+template <typename K, typename V, bool HAS_V, int THREADS>
+constexpr int chunked_min_blocks() {
+	constexpr int by_smem = (int)((228 * 1024) / (chunked_smem<K, V, HAS_V, THREADS>() + 1024));
+	constexpr int want = HAS_V ? 3 : 4;
+	return by_smem < want ? by_smem : want;
+}
+
+template <typename K, typename V, bool HAS_V, int THREADS>
+__global__ void __launch_bounds__(THREADS, (chunked_min_blocks<K, V, HAS_V, THREADS>()))
 radix_pass_chunked(const K *__restrict__ kin, K *__restrict__ kout,
 	const V *__restrict__ vin, V *__restrict__ vout, PassArgs a,
 	uint32_t num_tiles, uint32_t num_chunks) {
 	using Cfg = ChunkCfg<K, THREADS>;
 	constexpr int KPT = Cfg::kKpt;
 	constexpr int TILE = Cfg::kTile;
-	constexpr int WARPS = Cfg::kWarps;
-	constexpr int WPH = Cfg::kWarpsPerHalf;
+	constexpr int UNITS = Cfg::kUnits;
+	constexpr int HALF = UNITS / 2;
 	constexpr int kWin = kLookWindow / 2;
 	extern __shared__ __align__(16) unsigned char smem[];
-	uint32_t *s_hist = reinterpret_cast<uint32_t *>(smem);   // [WARPS][256]
-	uint32_t *s_match = s_hist + WARPS * kRadix;             // [WARPS][256]
-	uint32_t *s_tile_off = s_match + WARPS * kRadix;         // [256]
+	// Ranking rows of units and count rows, kRowWords apart (row_of).
+	uint32_t *s_rank = reinterpret_cast<uint32_t *>(smem);   // [UNITS] rows
+	uint32_t *s_cnt = s_rank + UNITS * kRowWords;            // [HALF] rows
+	uint32_t *s_tile_off = s_cnt + HALF * kRowWords;         // [256]
 	uint32_t *s_tile_cnt = s_tile_off + kRadix;              // [256]
 	uint32_t *s_run = s_tile_cnt + kRadix;                   // [256]
-	uint32_t *s_half = s_run + kRadix;                       // [2][256]
-	uint32_t *s_part = s_half + 2 * kRadix;                  // [256]
+	uint32_t *s_part = s_run + kRadix;                       // [256]
 	uint32_t *s_misc = s_part + kRadix;                      // [64]
 	unsigned char *s_stage = reinterpret_cast<unsigned char *>(s_misc + 64);
+	// Phase 1 only: [128][32] lane-column counters over s_rank.
+	uint32_t *s_col = s_rank;
+	static_assert(UNITS * kRowWords >= (kRadix / 2) * 32, "column counters fit");
 
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-	uint32_t *my_hist = s_hist + warp * kRadix;
-	uint32_t *my_match = s_match + warp * kRadix;
+	const int unit = 2 * warp + (lane >> 4);
+	const uint32_t l16 = lane & 15;
+	const uint32_t lt16 = (1u << l16) - 1u;
+	uint32_t *my_rank = s_rank + row_of(unit);
+	// Tile counts: units u and u + HALF share row u % HALF (16-bit halves).
+	uint32_t *my_cnt = s_cnt + row_of(unit % HALF);
+	const uint32_t cnt_inc = 1u << ((unit / HALF) * 16);
 	const int shift = a.shift;
-	const uint32_t lt = dev::lanemask_lt();
-	const int pd = tid & (kRadix - 1), ph = tid >> 8;
-	const int dw = pd >> 5;  // warp (within a half) that owns digit pd
+	const int pd = tid;        // the digit this thread scans
+	const int dw = pd >> 5;    // the warp that owns digit pd
 
 	if (tid == 0) s_misc[0] = atomicAdd(a.tile_counter, 1u);
-	for (int i = lane; i < kRadix; i += 32) {
-		my_hist[i] = 0;
-		my_match[i] = 0;
-	}
+	for (int i = tid; i < (kRadix / 2) * 32; i += THREADS) s_col[i] = 0;
+#pragma unroll
+	for (int i = 0; i < HALF; ++i) s_cnt[row_of(i) + pd] = 0;
 	// Global digit base of this pass: exclusive scan of its histogram.
-	if (ph == 0) {
+	{
 		const uint32_t hv = a.hist[pd];
 		uint32_t inc = hv;
 #pragma unroll
@@ -245,8 +361,8 @@ radix_pass_chunked(const K *__restrict__ kin, K *__restrict__ kout,
 	__syncthreads();
 	const uint32_t c = s_misc[0];
 	if (c >= num_chunks) return;
-	uint32_t run_init = 0;
-	if (ph == 0) {
+	uint32_t run_init;
+	{
 		uint32_t goff = 0;
 #pragma unroll
 		for (int w = 0; w < 8; ++w)
@@ -258,27 +374,51 @@ radix_pass_chunked(const K *__restrict__ kin, K *__restrict__ kout,
 	const size_t k_lo = (size_t)t0 * TILE;
 	const size_t k_hi = (size_t)t1 * TILE < a.n ? (size_t)t1 * TILE : a.n;
 
-	// Phase 1: digit counts of the whole chunk.
+	// Phase 1: digit counts of the whole chunk, in lane columns.
 	{
 		constexpr int PER = 16 / sizeof(K);
+		uint32_t *col = s_col + lane;
 		const bool vec = ((uintptr_t)(kin + k_lo) % 16) == 0;
 		const size_t nvec = vec ? (k_hi - k_lo) / PER : 0;
 		const uint4 *src = reinterpret_cast<const uint4 *>(kin + k_lo);
-#pragma unroll 4
-		for (size_t i = tid; i < nvec; i += THREADS) {
+		constexpr int kIn = 4;  // 16-byte loads in flight per thread
+		size_t i = tid;
+		for (; i + (kIn - 1) * THREADS < nvec; i += kIn * THREADS) {
+			uint4 v[kIn];
+#pragma unroll
+			for (int u = 0; u < kIn; ++u) v[u] = dev::ld_stream_v4(src + i + u * THREADS);
+#pragma unroll
+			for (int u = 0; u < kIn; ++u) {
+				const K *e = reinterpret_cast<const K *>(&v[u]);
+#pragma unroll
+				for (int q = 0; q < PER; ++q) {
+					const uint32_t d = digit_of(e[q], shift);
+					atomicAdd(col + (d >> 1) * 32, 1u << ((d & 1) << 4));
+				}
+			}
+		}
+		for (; i < nvec; i += THREADS) {
 			uint4 v = dev::ld_stream_v4(src + i);
 			const K *e = reinterpret_cast<const K *>(&v);
 #pragma unroll
-			for (int q = 0; q < PER; ++q) atomicAdd(my_hist + digit_of(e[q], shift), 1u);
+			for (int q = 0; q < PER; ++q) {
+				const uint32_t d = digit_of(e[q], shift);
+				atomicAdd(col + (d >> 1) * 32, 1u << ((d & 1) << 4));
+			}
 		}
-		for (size_t i = k_lo + nvec * PER + tid; i < k_hi; i += THREADS)
-			atomicAdd(my_hist + digit_of(kin[i], shift), 1u);
+		for (size_t i = k_lo + nvec * PER + tid; i < k_hi; i += THREADS) {
+			const uint32_t d = digit_of(kin[i], shift);
+			atomicAdd(col + (d >> 1) * 32, 1u << ((d & 1) << 4));
+		}
 	}
 	__syncthreads();
-	if (ph == 0) {
+	{
+		// Sum digit pd's 32 column halves (rotated start: no bank conflicts).
+		const uint32_t *row = s_col + (pd >> 1) * 32;
+		const int hs = (pd & 1) << 4;
 		uint32_t cnt = 0;
-#pragma unroll
-		for (int w = 0; w < WARPS; ++w) cnt += s_hist[w * kRadix + pd];
+#pragma unroll 8
+		for (int i = 0; i < 32; ++i) cnt += (row[(i + lane) & 31] >> hs) & 0xFFFFu;
 		uint32_t *st = a.status + (size_t)c * kRadix + pd;
 		if (c == 0) dev::st_relaxed_u32(st, kStPrefix | cnt);
 		else dev::st_relaxed_u32(st, kStAgg | cnt);
@@ -310,40 +450,42 @@ radix_pass_chunked(const K *__restrict__ kin, K *__restrict__ kout,
 
 	// Phase 2: tiles of the chunk in order.
 	K k[KPT];
-	if (t0 < t1) chunk_load_keys<K, THREADS>(k, kin, a.n, t0, warp, lane);
+	V v[HAS_V ? KPT : 1];
+	if (t0 < t1) {
+		chunk_load_keys<K, THREADS>(k, kin, a.n, t0, unit, l16);
+		if constexpr (HAS_V) chunk_load_vals<K, V, THREADS>(v, vin, a.n, t0, unit, l16);
+	}
 	for (uint32_t t = t0; t < t1; ++t) {
-		for (int i = lane; i < kRadix; i += 32) my_hist[i] = 0;
-		__syncwarp();
 #pragma unroll
-		for (int j = 0; j < KPT; ++j) atomicAdd(my_hist + digit_of(k[j], shift), 1u);
+		for (int j = 0; j < KPT; ++j) atomicAdd(my_cnt + digit_of(k[j], shift), cnt_inc);
 		__syncthreads();
-		// Warp prefixes per digit: thread (pd, ph) takes warps
-		// WPH*ph .. WPH*ph + WPH - 1 with independent loads.
-		uint32_t cw[WPH];
+		// Unit prefixes of digit pd in unit order (rows' low halves are
+		// units 0..HALF-1, high halves units HALF..UNITS-1); the rows are
+		// cleared for the next tile as they are read.
+		uint32_t c2[HALF];
 #pragma unroll
-		for (int i = 0; i < WPH; ++i) cw[i] = s_hist[(WPH * ph + i) * kRadix + pd];
+		for (int i = 0; i < HALF; ++i) {
+			c2[i] = s_cnt[row_of(i) + pd];
+			s_cnt[row_of(i) + pd] = 0;
+		}
 		uint32_t run = 0;
 #pragma unroll
-		for (int i = 0; i < WPH; ++i) {
-			uint32_t tmp = cw[i];
-			cw[i] = run;
-			run += tmp;
+		for (int i = 0; i < HALF; ++i) {
+			const uint32_t lo = c2[i] & 0xFFFFu;
+			c2[i] = (c2[i] & 0xFFFF0000u) | run;
+			run += lo;
 		}
-		uint32_t sum = run;
-		if (Cfg::kHalves == 2) {
-			s_half[ph * kRadix + pd] = run;
-			__syncthreads();
-			const uint32_t lo = s_half[pd];
-			sum = lo + s_half[kRadix + pd];
-			if (ph == 1) {
 #pragma unroll
-				for (int i = 0; i < WPH; ++i) cw[i] += lo;
-			}
+		for (int i = 0; i < HALF; ++i) {
+			const uint32_t hi = c2[i] >> 16;
+			c2[i] = (c2[i] & 0xFFFFu) | (run << 16);
+			run += hi;
 		}
-		if (ph == 0) {
-			// Advance the run by the previous tile's count (or the lookback).
-			s_run[pd] += s_tile_cnt[pd];
-			s_tile_cnt[pd] = sum;
+		const uint32_t sum = run;
+		// Advance the run by the previous tile's count (or the lookback).
+		s_run[pd] += s_tile_cnt[pd];
+		s_tile_cnt[pd] = sum;
+		{
 			uint32_t inc = sum;
 #pragma unroll
 			for (int d = 1; d < 32; d <<= 1) {
@@ -361,77 +503,74 @@ radix_pass_chunked(const K *__restrict__ kin, K *__restrict__ kout,
 				if (w < dw) woff += s_misc[8 + w];
 			const uint32_t to = s_part[pd] + woff;
 #pragma unroll
-			for (int i = 0; i < WPH; ++i) s_hist[(WPH * ph + i) * kRadix + pd] = to + cw[i];
+			for (int i = 0; i < HALF; ++i) {
+				s_rank[row_of(i) + pd] = (to + (c2[i] & 0xFFFFu)) << 16;
+				s_rank[row_of(i + HALF) + pd] = (to + (c2[i] >> 16)) << 16;
+			}
 			// Output index of staged position q of digit d is q + G[d]
 			// (modulo 2^32), G[d] = global run start - tile offset.
-			if (ph == 0) s_tile_off[pd] = s_run[pd] - to;
+			s_tile_off[pd] = s_run[pd] - to;
 		}
 		__syncthreads();
 		K *sk = reinterpret_cast<K *>(s_stage);
-		uint32_t tpos[HAS_V ? KPT : 1];
+		V *sv = reinterpret_cast<V *>(s_stage + (size_t)TILE * sizeof(K));
 #pragma unroll
 		for (int j = 0; j < KPT; ++j) {
-			const uint32_t pos = dev::warp_rank_digit(my_match, my_hist,
-				digit_of(k[j], shift), lane, lt);
-			if (pos < (uint32_t)TILE) sk[pos] = k[j];
-			if (HAS_V) tpos[j] = pos;
+			const uint32_t pos = unit_rank_digit(my_rank + digit_of(k[j], shift), l16, lt16);
+			if (pos < (uint32_t)TILE) {
+				sk[pos] = k[j];
+				if (HAS_V) sv[pos] = v[j];
+			}
 		}
 		__syncthreads();
-		if (!HAS_V && t + 1 < t1) chunk_load_keys<K, THREADS>(k, kin, a.n, t + 1, warp, lane);
-		uint32_t outpos[HAS_V ? KPT : 1];
+		if (t + 1 < t1) {
+			chunk_load_keys<K, THREADS>(k, kin, a.n, t + 1, unit, l16);
+			if constexpr (HAS_V) chunk_load_vals<K, V, THREADS>(v, vin, a.n, t + 1, unit, l16);
+		}
 #pragma unroll
 		for (int i = 0; i < KPT; ++i) {
 			const int q = i * THREADS + tid;
 			const K key = sk[q];
 			const size_t o = (uint32_t)(s_tile_off[digit_of(key, shift)] + (uint32_t)q);
-			if (o < a.n) kout[o] = key;
-			if (HAS_V) outpos[i] = (uint32_t)o;
-		}
-		if (HAS_V) {
-			V v[KPT];
-			const size_t wbase = (size_t)t * TILE + (size_t)warp * (KPT * 32);
-#pragma unroll
-			for (int j = 0; j < KPT; ++j) {
-				size_t idx = wbase + (size_t)j * 32 + lane;
-				v[j] = idx < a.n ? vin[idx] : (V)0;
+			if (o < a.n) {
+				kout[o] = key;
+				if (HAS_V) vout[o] = sv[q];
 			}
-			__syncthreads();
-			V *sv = reinterpret_cast<V *>(s_stage);
-#pragma unroll
-			for (int j = 0; j < KPT; ++j)
-				if (tpos[j] < (uint32_t)TILE) sv[tpos[j]] = v[j];
-			__syncthreads();
-#pragma unroll
-			for (int i = 0; i < KPT; ++i) {
-				const int q = i * THREADS + tid;
-				if (outpos[i] < a.n) vout[outpos[i]] = sv[q];
-			}
-			if (t + 1 < t1) chunk_load_keys<K, THREADS>(k, kin, a.n, t + 1, warp, lane);
-			__syncthreads();
 		}
 	}
 }
 
-template <typename K, typename V, bool HAS_V, int THREADS>
-size_t chunked_smem() {
-	constexpr int TILE = ChunkCfg<K, THREADS>::kTile;
-	size_t stage = (size_t)TILE * (sizeof(K) > sizeof(V) || !HAS_V ? sizeof(K) : sizeof(V));
-	return (2 * ChunkCfg<K, THREADS>::kWarps * kRadix + 7 * kRadix + 64) * sizeof(uint32_t) +
-		stage;
+
+template <typename K, int PASSES>
+void launch_upsweep_p(cudaStream_t s, const K *keys, size_t n, uint32_t *hist,
+	int base_shift, int sm_count) {
+	constexpr size_t smem = upsweep_smem<PASSES>();
+	auto kern = radix_upsweep<K, PASSES>;
+	if (smem > 48 * 1024)
+		cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	// Resident CTAs per SM by shared memory (228 KB per SM, 1 KB reserved
+	// per CTA), at most 4; at least enough CTAs for the per-thread key cap.
+	const int per_sm = (int)std::min<size_t>(4, (228 * 1024) / (smem + 1024));
+	size_t grid = (size_t)sm_count * std::max(per_sm, 1);
+	const size_t need = ((n * sizeof(K) + 15) / 16 + kUpsweepThreads - 1) / kUpsweepThreads;
+	if (grid > need) grid = std::max<size_t>(need, 1);
+	const size_t cap = kUpsweepThreads * kUpsweepKeysPerThread;
+	grid = std::max(grid, (n + cap - 1) / cap);
+	kern<<<(unsigned)grid, kUpsweepThreads, smem, s>>>(keys, n, hist, base_shift);
 }
 
 template <typename K>
-void launch_upsweep(int passes, int grid, cudaStream_t s, const K *keys, size_t n,
-	uint32_t *hist, int base_shift = 0) {
+void launch_upsweep(int passes, cudaStream_t s, const K *keys, size_t n, uint32_t *hist,
+	int sm_count, int base_shift = 0) {
 	switch (passes) {
-	case 1: radix_upsweep<K, 1><<<grid, 256, 0, s>>>(keys, n, hist, base_shift); break;
-	case 2: radix_upsweep<K, 2><<<grid, 256, 0, s>>>(keys, n, hist, base_shift); break;
-	case 3: radix_upsweep<K, 3><<<grid, 256, 0, s>>>(keys, n, hist, base_shift); break;
-	case 4: radix_upsweep<K, 4><<<grid, 256, 0, s>>>(keys, n, hist, base_shift); break;
-	case 5: radix_upsweep<K, 5><<<grid, 256, 0, s>>>(keys, n, hist, base_shift); break;
-	case 6: radix_upsweep<K, 6><<<grid, 256, 0, s>>>(keys, n, hist, base_shift); break;
-	case 7: radix_upsweep<K, 7><<<grid, 256, 0, s>>>(keys, n, hist, base_shift); break;
-	default: radix_upsweep<K, 8><<<grid, 256, 0, s>>>(keys, n, hist, base_shift); break;
+	case 1: launch_upsweep_p<K, 1>(s, keys, n, hist, base_shift, sm_count); break;
+	case 2: launch_upsweep_p<K, 2>(s, keys, n, hist, base_shift, sm_count); break;
+	case 3: launch_upsweep_p<K, 3>(s, keys, n, hist, base_shift, sm_count); break;
+	case 4: launch_upsweep_p<K, 4>(s, keys, n, hist, base_shift, sm_count); break;
+	case 5: launch_upsweep_p<K, 5>(s, keys, n, hist, base_shift, sm_count); break;
+	case 6: launch_upsweep_p<K, 6>(s, keys, n, hist, base_shift, sm_count); break;
+	case 7: launch_upsweep_p<K, 7>(s, keys, n, hist, base_shift, sm_count); break;
+	default: launch_upsweep_p<K, 8>(s, keys, n, hist, base_shift, sm_count); break;
 	}
 }
 
@@ -449,8 +588,18 @@ cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
 	constexpr int CT = kChunkThreads;
 	constexpr int CTILE = ChunkCfg<K, CT>::kTile;
 	const size_t ctiles = (n + CTILE - 1) / CTILE;
-	const uint32_t chunks = (uint32_t)std::min<size_t>(ctiles,
-		(size_t)ChunkCfg<K, CT>::kMinBlocks * ctx->sm_count);
+	const size_t smem = chunked_smem<K, V, HAS_V, CT>();
+	auto kern = radix_pass_chunked<K, V, HAS_V, CT>;
+	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		(int)smem);
+	int per_sm = 0;
+	if (e == cudaSuccess)
+		e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, CT, smem);
+	if (e != cudaSuccess) {
+		cuda_ok(e, err, "satradix");
+		return e;
+	}
+	const uint32_t chunks = chunk_count<K>(ctiles, ctx->sm_count, per_sm);
 	// Status slots: one per chunk.
 	const size_t status_words = (size_t)chunks * kRadix;
 	// Scratch: [hist passes*256][counters 8][status0][status1][alt keys][alt vals]
@@ -468,15 +617,11 @@ cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
 	uint32_t *st[2] = {(uint32_t *)(tmp + off_st0), (uint32_t *)(tmp + off_st1)};
 	K *alt_k = (K *)(tmp + off_keys);
 	V *alt_v = (V *)(tmp + off_vals);
-	cudaError_t e = cudaMemsetAsync(tmp, 0, off_st1, s);
+	e = cudaMemsetAsync(tmp, 0, off_st1, s);
 	unsigned launches = 0;
 	if (e == cudaSuccess) {
-		int grid = ctx->sm_count * 4;
-		size_t chunks = (n * sizeof(K) + 15) / 16;
-		size_t need = (chunks + 255) / 256;
-		if ((size_t)grid > need) grid = (int)std::max<size_t>(need, 1);
 		KernelTimer t("satradix_upsweep", s, (double)n * sizeof(K));
-		launch_upsweep<K>(passes, grid, s, (const K *)keys, n, hist);
+		launch_upsweep<K>(passes, s, (const K *)keys, n, hist, ctx->sm_count);
 		t.stop();
 		launches++;
 		e = cudaGetLastError();
@@ -498,10 +643,6 @@ cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
 		}
 	}
 	if (e == cudaSuccess) {
-		const size_t smem = chunked_smem<K, V, HAS_V, CT>();
-		auto kern = radix_pass_chunked<K, V, HAS_V, CT>;
-		e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-			(int)smem);
 		K *src_k = (K *)keys, *dst_k = alt_k;
 		V *src_v = (V *)vals, *dst_v = alt_v;
 		for (size_t q = 0; q < active.size() && e == cudaSuccess; ++q) {
@@ -546,8 +687,18 @@ cudaError_t msd_partition_typed(const K *keys_in, K *keys_out, size_t n, int sor
 	constexpr int CTILE = ChunkCfg<K, CT>::kTile;
 	const int shift = sort_bits - kRadixBits;
 	const size_t ctiles = (n + CTILE - 1) / CTILE;
-	const uint32_t chunks = (uint32_t)std::min<size_t>(ctiles,
-		(size_t)ChunkCfg<K, CT>::kMinBlocks * ctx->sm_count);
+	const size_t smem = chunked_smem<K, uint32_t, false, CT>();
+	auto kern = radix_pass_chunked<K, uint32_t, false, CT>;
+	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		(int)smem);
+	int per_sm = 0;
+	if (e == cudaSuccess)
+		e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, CT, smem);
+	if (e != cudaSuccess) {
+		cuda_ok(e, err, "satradix partition");
+		return e;
+	}
+	const uint32_t chunks = chunk_count<K>(ctiles, ctx->sm_count, per_sm);
 	const size_t status_words = (size_t)chunks * kRadix;
 	const size_t off_cnt = kRadix * 4, off_st0 = off_cnt + 64;
 	const size_t off_st1 = off_st0 + status_words * 4;
@@ -555,13 +706,10 @@ cudaError_t msd_partition_typed(const K *keys_in, K *keys_out, size_t n, int sor
 	if (!tmp) return cudaErrorMemoryAllocation;
 	uint32_t *hist = (uint32_t *)tmp;
 	uint32_t *cnt = (uint32_t *)(tmp + off_cnt);
-	cudaError_t e = cudaMemsetAsync(tmp, 0, off_st1, s);
+	e = cudaMemsetAsync(tmp, 0, off_st1, s);
 	if (e == cudaSuccess) {
-		int grid = ctx->sm_count * 4;
-		const size_t need = ((n * sizeof(K) + 15) / 16 + 255) / 256;
-		if ((size_t)grid > need) grid = (int)std::max<size_t>(need, 1);
 		KernelTimer t("satradix_upsweep", s, (double)n * sizeof(K));
-		launch_upsweep<K>(1, grid, s, keys_in, n, hist, shift);
+		launch_upsweep<K>(1, s, keys_in, n, hist, ctx->sm_count, shift);
 		t.stop();
 		e = cudaGetLastError();
 	}
@@ -572,9 +720,6 @@ cudaError_t msd_partition_typed(const K *keys_in, K *keys_out, size_t n, int sor
 	if (e == cudaSuccess && trivial) {
 		e = cudaMemcpyAsync(keys_out, keys_in, n * sizeof(K), cudaMemcpyDeviceToDevice, s);
 	} else if (e == cudaSuccess) {
-		const size_t smem = chunked_smem<K, uint32_t, false, CT>();
-		auto kern = radix_pass_chunked<K, uint32_t, false, CT>;
-		e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 		PassArgs pa;
 		pa.hist = hist;
 		pa.status = (uint32_t *)(tmp + off_st0);
