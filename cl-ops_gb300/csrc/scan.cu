@@ -7,18 +7,27 @@
 // Integer addition is associative, so the result is bit-identical to the
 // reference's work-group Blelloch trees whatever the summation order.
 //
-// Layout: tiles of 4096 elements, 256 threads, 16 consecutive elements per
-// thread. Each warp moves its 512-element segment between global memory
-// and registers through a padded shared-memory transpose, so every global
-// access is a coalesced 16-byte vector access. Tiles take ids from an
-// atomic counter (so a tile only ever waits on tiles already running),
-// publish their aggregate, then warp 0 looks back over a 64-tile window
-// per round trip until it meets an inclusive prefix. Status words carry
-// their own ready bits, so neither side needs a memory fence. Every wait
-// is bounded.
+// Layout: tiles of 8192 elements, 256 threads. Each warp owns 1024
+// consecutive elements as two blocks of 512, lane l holding elements
+// 16 l .. 16 l + 15 of each block. A block moves between global memory and
+// shared memory with coalesced 16-byte vector accesses through a padded
+// transpose (conflict-free per-lane runs). Inputs stay in shared memory:
+// the thread and warp sums are taken before the lookback and the outputs
+// are formed by a second read after it, so no per-element state is held
+// in registers across the wait. Tiles take ids from an atomic counter (so
+// a tile only ever waits on tiles already running), publish their
+// aggregate, then warp 0 looks back over a 64-tile window per round trip
+// until it meets an inclusive prefix. Status words carry their own ready
+// bits, so neither side needs a memory fence. Every wait is bounded.
+//
+// The lookback bounds the rate of tiles, not of bytes: a window of 64
+// tiles per L2 round trip, so the tile is made large enough (8192
+// elements, 96 KB of uint -> ulong traffic) that the tile rate HBM needs
+// stays well inside it.
 //
 // HBM roofline: sizeof(in) + sizeof(out) bytes per element (12 B for
-// uint -> ulong), plus 32 B of tile status per 4096 elements.
+// uint -> ulong), plus 32 B of tile status per 8192 elements.
+#include <atomic>
 #include <mutex>
 #include <type_traits>
 
@@ -32,10 +41,12 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kItems = 16;
-constexpr int kWarpElems = 32 * kItems;
-constexpr int kTile = kWarps * kWarpElems;
-constexpr int kPadded = kWarpElems + kWarpElems / 32;
+constexpr int kItems = 16;                       // a lane's run in one block
+constexpr int kBlock = 32 * kItems;              // 512 elements
+constexpr int kBlocks = 2;                       // blocks per warp
+constexpr int kWarpElems = kBlocks * kBlock;     // 1024
+constexpr int kTile = kWarps * kWarpElems;       // 8192
+constexpr int kPadded = kBlock + kBlock / 32;    // padded block in shared memory
 
 __device__ __forceinline__ int pidx(int i) { return i + (i >> 5); }
 
@@ -50,123 +61,297 @@ __device__ __forceinline__ Acc shfl_up(Acc v, int d) {
 	return __shfl_up_sync(0xffffffffu, v, d);
 }
 
+// Shared memory of one CTA: per warp, its two input blocks and one output
+// staging block.
 template <typename InT, typename OutT>
-__global__ void __launch_bounds__(kThreads, 5)
+constexpr size_t scan_smem() {
+	return (size_t)kWarps * kPadded * (kBlocks * sizeof(InT) + sizeof(OutT));
+}
+
+// Resident CTAs per SM (228 KB per SM, 1 KB reserved per CTA), at most 4,
+// and at most 2 for 8-byte inputs (their prefetch takes 64 registers).
+template <typename InT, typename OutT>
+constexpr int scan_min_blocks() {
+	constexpr int by_smem = (int)((228 * 1024) / (scan_smem<InT, OutT>() + 1024 + 128));
+	constexpr int cap = sizeof(InT) == 8 ? 2 : 4;
+	return by_smem < cap ? by_smem : cap;
+}
+
+// One warp's block b of a tile, global -> padded shared memory.
+template <typename InT>
+__device__ __forceinline__ void load_block_scalar(const InT *__restrict__ in, size_t n,
+	size_t seg, InT *sin, int lane) {
+	for (int i = lane; i < kBlock; i += 32)
+		sin[pidx(i)] = (seg + i < n) ? in[seg + i] : (InT)0;
+}
+
+template <typename InT>
+struct BlockRegs {
+	static constexpr int kEpc = 16 / sizeof(InT);          // elements per 16 B
+	static constexpr int kPerLane = kBlock / kEpc / 32;    // 16-byte loads per lane
+	uint4 v[kBlocks][kPerLane];
+};
+
+// Issues the 16-byte loads of a warp's full blocks (prefetch).
+template <typename InT>
+__device__ __forceinline__ void issue_loads(BlockRegs<InT> &r, const InT *__restrict__ in,
+	size_t wseg, int lane) {
+#pragma unroll
+	for (int b = 0; b < kBlocks; ++b) {
+		const uint4 *src = reinterpret_cast<const uint4 *>(in + wseg + (size_t)b * kBlock);
+#pragma unroll
+		for (int k = 0; k < BlockRegs<InT>::kPerLane; ++k)
+			r.v[b][k] = dev::ld_stream_v4(src + lane + 32 * k);
+	}
+}
+
+// Transposes prefetched loads into the warp's padded blocks.
+template <typename InT>
+__device__ __forceinline__ void store_loads(const BlockRegs<InT> &r, InT *s_in, int lane) {
+	constexpr int EPC = BlockRegs<InT>::kEpc;
+#pragma unroll
+	for (int b = 0; b < kBlocks; ++b) {
+		InT *sin = s_in + b * kPadded;
+#pragma unroll
+		for (int k = 0; k < BlockRegs<InT>::kPerLane; ++k) {
+			const int c = lane + 32 * k;
+			const InT *e = reinterpret_cast<const InT *>(&r.v[b][k]);
+#pragma unroll
+			for (int q = 0; q < EPC; ++q) sin[pidx(c * EPC + q)] = e[q];
+		}
+	}
+}
+
+// Persistent CTAs (one per resident slot) take tiles in order from an
+// atomic counter. Per tile: the sums of the tile already in shared memory
+// and publication of its aggregate; then, while warp 0 looks back, every
+// warp issues the loads of the CTA's next tile (claimed at the top of the
+// iteration) into registers and sums them, so the next tile's aggregate is
+// published as soon as the lookback ends -- before this tile's outputs are
+// written -- and no later tile waits on it longer than on a freshly
+// launched one; after the outputs the prefetched data is transposed into
+// shared memory. Every wait is on a lower tile id (down to tile 0, which
+// publishes its prefix at once), so the waits cannot form a cycle.
+template <typename InT, typename OutT>
+__global__ void __launch_bounds__(kThreads, (scan_min_blocks<InT, OutT>()))
 scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, size_t n,
 	TileStatus ts,
 	int *dev_status, bool vec_ok, long long debug_skip_tile,
 	const void *carry_in, void *carry_out) {
 	using Acc = typename std::conditional<(sizeof(OutT) <= 4), uint32_t,
 		uint64_t>::type;
-	constexpr int ESZ = sizeof(InT) > sizeof(OutT) ? sizeof(InT) : sizeof(OutT);
-	__shared__ __align__(16) unsigned char s_buf[kWarps][kPadded * ESZ];
+	extern __shared__ __align__(16) unsigned char s_dyn[];
 	__shared__ Acc s_warp_tot[kWarps];
+	__shared__ Acc s_next_tot[kWarps];
 	__shared__ Acc s_excl;
-	__shared__ uint32_t s_tile;
+	__shared__ uint32_t s_tile, s_next;
 
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const uint32_t num_tiles = (uint32_t)((n + kTile - 1) / kTile);
-	(void)num_tiles;
+	InT *s_in = reinterpret_cast<InT *>(s_dyn + (size_t)warp * kPadded *
+		(kBlocks * sizeof(InT) + sizeof(OutT)));
+	OutT *s_out = reinterpret_cast<OutT *>(s_in + kBlocks * kPadded);
+	auto full_tile = [&](uint32_t t) {
+		return vec_ok && (size_t)(t + 1) * kTile <= n;
+	};
 	if (tid == 0) s_tile = atomicAdd(ts.counter, 1u);
 	__syncthreads();
-	const uint32_t tile = s_tile;
-	const size_t seg = (size_t)tile * kTile + (size_t)warp * kWarpElems;
-	const bool full = seg + kWarpElems <= n;
-
-	// ---- load the warp's segment (coalesced) into padded smem -----------
-	InT *sin = reinterpret_cast<InT *>(s_buf[warp]);
-	if (full && vec_ok) {
-		constexpr int EPC = 16 / sizeof(InT);
-		constexpr int CHUNKS = kWarpElems / EPC;
-		const uint4 *src = reinterpret_cast<const uint4 *>(in + seg);
+	uint32_t tile = s_tile;
+	if (tile >= num_tiles) return;
+	{
+		const size_t wseg = (size_t)tile * kTile + (size_t)warp * kWarpElems;
+		if (full_tile(tile)) {
+			BlockRegs<InT> r;
+			issue_loads<InT>(r, in, wseg, lane);
+			store_loads<InT>(r, s_in, lane);
+		} else {
 #pragma unroll
-		for (int c = lane; c < CHUNKS; c += 32) {
-			uint4 v = dev::ld_stream_v4(src + c);
-			const InT *e = reinterpret_cast<const InT *>(&v);
-#pragma unroll
-			for (int k = 0; k < EPC; ++k) sin[pidx(c * EPC + k)] = e[k];
+			for (int b = 0; b < kBlocks; ++b)
+				load_block_scalar<InT>(in, n, wseg + (size_t)b * kBlock, s_in + b * kPadded, lane);
 		}
-	} else {
-		for (int i = lane; i < kWarpElems; i += 32)
-			sin[pidx(i)] = (seg + i < n) ? in[seg + i] : (InT)0;
 	}
 	__syncwarp();
+	bool agg_published = false;  // the current tile's aggregate is out
 
-	// ---- per-thread sequential scan of 16 consecutive elements ----------
-	Acc x[kItems];
-	Acc run = 0;
-#pragma unroll
-	for (int j = 0; j < kItems; ++j) {
-		Acc v = (Acc)(OutT)sin[pidx(lane * kItems + j)];
-		x[j] = run;  // exclusive within the thread
-		run += v;
-	}
-	// Warp inclusive scan of thread totals.
-	Acc inc = run;
-#pragma unroll
-	for (int d = 1; d < 32; d <<= 1) {
-		Acc t = shfl_up(inc, d);
-		if (lane >= d) inc += t;
-	}
-	const Acc lane_excl = inc - run;
-	if (lane == 31) s_warp_tot[warp] = inc;
-	__syncthreads();
+	for (;;) {
+		if (tid == 0) s_next = atomicAdd(ts.counter, 1u);
+		const size_t wseg = (size_t)tile * kTile + (size_t)warp * kWarpElems;
 
-	// ---- tile aggregate, publication and lookback (warp 0) --------------
-	if (warp == 0) {
-		Acc wt = lane < kWarps ? s_warp_tot[lane] : (Acc)0;
-		Acc winc = wt;
+		// ---- lane run sums and their warp scans, per block --------------
+		Acc lane_excl[kBlocks], block_tot[kBlocks];
 #pragma unroll
-		for (int d = 1; d < kWarps; d <<= 1) {
-			Acc t = shfl_up(winc, d);
-			if (lane >= d) winc += t;
-		}
-		const Acc aggregate = __shfl_sync(0xffffffffu, winc, kWarps - 1);
-		if (lane < kWarps) s_warp_tot[lane] = winc - wt;  // warp exclusive
-		const bool do_publish = (long long)tile != debug_skip_tile;
-		constexpr int PT = Slots<Acc>::kPerTile;
-		Acc excl = 0;
-		if (tile == 0) {
-			// A scan continuing an earlier one starts from its carry.
-			if (carry_in) excl = *reinterpret_cast<const Acc *>(carry_in);
-			if (lane == 0 && do_publish)
-				publish<Acc>(ts.words + Slots<Acc>::kWords, excl + aggregate);
-		} else {
-			if (lane == 0 && do_publish) publish<Acc>(ts.words + (size_t)tile * PT, aggregate);
-			excl = lb::lookback_warp<Acc>(ts.words, tile, dev_status);
-			if (lane == 0 && do_publish)
-				publish<Acc>(ts.words + (size_t)tile * PT + Slots<Acc>::kWords, excl + aggregate);
+		for (int b = 0; b < kBlocks; ++b) {
+			const InT *sin = s_in + b * kPadded;
+			Acc run = 0;
+#pragma unroll
+			for (int j = 0; j < kItems; ++j) run += (Acc)(OutT)sin[pidx(lane * kItems + j)];
+			Acc inc = run;
+#pragma unroll
+			for (int d = 1; d < 32; d <<= 1) {
+				Acc t = shfl_up(inc, d);
+				if (lane >= d) inc += t;
+			}
+			lane_excl[b] = inc - run;
+			block_tot[b] = __shfl_sync(0xffffffffu, inc, 31);
 		}
 		if (lane == 0) {
-			s_excl = excl;
-			if (carry_out && (size_t)(tile + 1) * kTile >= n)
-				*reinterpret_cast<Acc *>(carry_out) = excl + aggregate;
+			Acc wsum = 0;
+#pragma unroll
+			for (int b = 0; b < kBlocks; ++b) wsum += block_tot[b];
+			s_warp_tot[warp] = wsum;
 		}
-	}
-	__syncthreads();
+		__syncthreads();
+		const uint32_t next = s_next;
+		const bool have_next = next < num_tiles;
+		const bool next_full = have_next && full_tile(next);
+		const size_t nseg = (size_t)next * kTile + (size_t)warp * kWarpElems;
 
-	// ---- outputs through padded smem, coalesced stores -------------------
-	const Acc base = s_excl + s_warp_tot[warp] + lane_excl;
-	OutT *sout = reinterpret_cast<OutT *>(s_buf[warp]);
+		// ---- prefetch of the next tile (all warps) ----------------------
+		BlockRegs<InT> r;
+		if (next_full) issue_loads<InT>(r, in, nseg, lane);
+		const bool next_publish = next_full && (long long)next != debug_skip_tile;
+
+		// ---- tile aggregate, publication and lookback (warp 0) ----------
+		if (warp == 0) {
+			Acc wt = lane < kWarps ? s_warp_tot[lane] : (Acc)0;
+			Acc winc = wt;
 #pragma unroll
-	for (int j = 0; j < kItems; ++j) sout[pidx(lane * kItems + j)] = (OutT)(base + x[j]);
-	__syncwarp();
-	if (full && vec_ok) {
-		constexpr int EPC = 16 / sizeof(OutT);
-		constexpr int CHUNKS = kWarpElems / EPC;
-		uint4 *dst = reinterpret_cast<uint4 *>(out + seg);
-#pragma unroll
-		for (int c = lane; c < CHUNKS; c += 32) {
-			uint4 v;
-			OutT *e = reinterpret_cast<OutT *>(&v);
-#pragma unroll
-			for (int k = 0; k < EPC; ++k) e[k] = sout[pidx(c * EPC + k)];
-			dev::st_stream_v4(dst + c, v);
+			for (int d = 1; d < kWarps; d <<= 1) {
+				Acc t = shfl_up(winc, d);
+				if (lane >= d) winc += t;
+			}
+			const Acc aggregate = __shfl_sync(0xffffffffu, winc, kWarps - 1);
+			if (lane < kWarps) s_warp_tot[lane] = winc - wt;  // warp exclusive
+			const bool do_publish = (long long)tile != debug_skip_tile;
+			constexpr int PT = Slots<Acc>::kPerTile;
+			Acc excl = 0;
+			if (tile == 0) {
+				// A scan continuing an earlier one starts from its carry.
+				if (carry_in) excl = *reinterpret_cast<const Acc *>(carry_in);
+				if (lane == 0 && do_publish)
+					publish<Acc>(ts.words + Slots<Acc>::kWords, excl + aggregate);
+			} else {
+				if (lane == 0 && do_publish && !agg_published)
+					publish<Acc>(ts.words + (size_t)tile * PT, aggregate);
+				excl = lb::lookback_warp<Acc>(ts.words, tile, dev_status);
+				if (lane == 0 && do_publish)
+					publish<Acc>(ts.words + (size_t)tile * PT + Slots<Acc>::kWords,
+						excl + aggregate);
+			}
+			if (lane == 0) {
+				s_excl = excl;
+				if (carry_out && (size_t)(tile + 1) * kTile >= n)
+					*reinterpret_cast<Acc *>(carry_out) = excl + aggregate;
+			}
 		}
-	} else {
-		for (int i = lane; i < kWarpElems; i += 32)
-			if (seg + i < n) out[seg + i] = sout[pidx(i)];
+		// The next tile's sum from the prefetched registers.
+		if (next_full) {
+			constexpr int EPC = BlockRegs<InT>::kEpc;
+			Acc part = 0;
+#pragma unroll
+			for (int b = 0; b < kBlocks; ++b)
+#pragma unroll
+				for (int k = 0; k < BlockRegs<InT>::kPerLane; ++k) {
+					const InT *e = reinterpret_cast<const InT *>(&r.v[b][k]);
+#pragma unroll
+					for (int q = 0; q < EPC; ++q) part += (Acc)(OutT)e[q];
+				}
+			part = warp_sum<Acc>(part);
+			if (lane == 0) s_next_tot[warp] = part;
+		}
+		__syncthreads();
+		if (next_publish && tid == 0) {
+			Acc agg = 0;
+#pragma unroll
+			for (int w = 0; w < kWarps; ++w) agg += s_next_tot[w];
+			publish<Acc>(ts.words + (size_t)next * Slots<Acc>::kPerTile, agg);
+		}
+
+		// ---- outputs per block: second read, staged, coalesced stores ----
+		Acc base = s_excl + s_warp_tot[warp];
+#pragma unroll
+		for (int b = 0; b < kBlocks; ++b) {
+			const InT *sin = s_in + b * kPadded;
+			Acc run = base + lane_excl[b];
+#pragma unroll
+			for (int j = 0; j < kItems; ++j) {
+				const int q = pidx(lane * kItems + j);
+				const Acc v = (Acc)(OutT)sin[q];
+				s_out[q] = (OutT)run;
+				run += v;
+			}
+			base += block_tot[b];
+			__syncwarp();
+			const size_t seg = wseg + (size_t)b * kBlock;
+			if (seg + kBlock <= n && vec_ok) {
+				constexpr int EPC = 16 / sizeof(OutT);
+				constexpr int CHUNKS = kBlock / EPC;
+				uint4 *dst = reinterpret_cast<uint4 *>(out + seg);
+#pragma unroll
+				for (int c = lane; c < CHUNKS; c += 32) {
+					uint4 v;
+					OutT *e = reinterpret_cast<OutT *>(&v);
+#pragma unroll
+					for (int k = 0; k < EPC; ++k) e[k] = s_out[pidx(c * EPC + k)];
+					dev::st_stream_v4(dst + c, v);
+				}
+			} else {
+				for (int i = lane; i < kBlock; i += 32)
+					if (seg + i < n) out[seg + i] = s_out[pidx(i)];
+			}
+			__syncwarp();
+		}
+		if (!have_next) break;
+
+		// ---- the next tile into shared memory ---------------------------
+		if (next_full) {
+			store_loads<InT>(r, s_in, lane);
+		} else {
+#pragma unroll
+			for (int b = 0; b < kBlocks; ++b)
+				load_block_scalar<InT>(in, n, nseg + (size_t)b * kBlock, s_in + b * kPadded, lane);
+		}
+		__syncwarp();
+		agg_published = next_full;
+		tile = next;
 	}
+}
+
+// Per device and type pair, once: opts the kernel into its dynamic shared
+// memory (more than 48 KB for most pairs) and records its resident CTAs
+// per SM. Later calls (possibly while a graph is being captured) only read
+// the cached count.
+template <typename InT, typename OutT>
+cudaError_t scan_prepare(int *per_sm) {
+	static std::atomic<int> cached[64];
+	static std::mutex mu;
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess) return e;
+	if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+	int v = cached[dev].load(std::memory_order_acquire);
+	if (v == 0) {
+		std::lock_guard<std::mutex> lk(mu);
+		v = cached[dev].load(std::memory_order_relaxed);
+		if (v == 0) {
+			e = cudaFuncSetAttribute(scan_lookback<InT, OutT>,
+				cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scan_smem<InT, OutT>());
+			if (e == cudaSuccess)
+				e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, scan_lookback<InT, OutT>,
+					kThreads, scan_smem<InT, OutT>());
+			if (e != cudaSuccess) return e;
+			if (v < 1) v = 1;
+			cached[dev].store(v, std::memory_order_release);
+		}
+	}
+	*per_sm = v;
+	return cudaSuccess;
+}
+
+// Persistent grid: one CTA per resident slot, at most one per tile.
+inline unsigned scan_grid(size_t tiles, int per_sm, int sm_count) {
+	const size_t g = std::min<size_t>(tiles, (size_t)per_sm * (size_t)sm_count);
+	return (unsigned)std::max<size_t>(g, 1);
 }
 
 template <typename InT, typename OutT>
@@ -189,9 +374,12 @@ cudaError_t launch_scan(const void *in, void *out, size_t n, CCLContext *ctx,
 	ts.counter = (uint32_t *)(tmp + status_bytes);
 	cudaError_t e = cudaMemsetAsync(tmp, 0, bytes, s);
 	bool vec_ok = ((uintptr_t)in % 16 == 0) && ((uintptr_t)out % 16 == 0);
+	int per_sm = 1;
+	if (e == cudaSuccess) e = scan_prepare<InT, OutT>(&per_sm);
 	if (e == cudaSuccess) {
 		KernelTimer t("scan_lookback", s, (double)n * (sizeof(InT) + sizeof(OutT)));
-		scan_lookback<InT, OutT><<<(unsigned)tiles, kThreads, 0, s>>>(
+		scan_lookback<InT, OutT><<<scan_grid(tiles, per_sm, ctx->sm_count), kThreads,
+			scan_smem<InT, OutT>(), s>>>(
 			(const InT *)in, (OutT *)out, n, ts, ctx->d_status, vec_ok,
 			debug_skip_tile, carry_in, carry_out);
 		t.stop();
@@ -265,14 +453,14 @@ extern "C" void clo_gb300_debug_scan_withhold(long long tile) {
 // Same kernel as above; its tile statuses and tile counter live in the
 // file-scope device array below instead of a pool temporary. The array is
 // part of the library's device image: every GPU that loads the library
-// holds it (2 MiB + 16 B) until the process exits. Host code cannot use
+// holds it (1 MiB + 16 B) until the process exits. Host code cannot use
 // the array's name as a device address (on the host it names a stand-in),
 // so the device address is looked up once per device with
 // cudaGetSymbolAddress and cached.
 // ---------------------------------------------------------------------
 
-// Largest no-allocation scan: 2^16 tiles of 4096 elements = 2^28 elements.
-#define CLO_NOALLOC_MAX_TILES (1u << 16)
+// Largest no-allocation scan: 2^15 tiles of 8192 elements = 2^28 elements.
+#define CLO_NOALLOC_MAX_TILES (1u << 15)
 // Four status words per tile (64-bit sums) and one word for the counter.
 #define CLO_NOALLOC_WORDS (CLO_NOALLOC_MAX_TILES * 4u + 2u)
 
@@ -282,6 +470,7 @@ namespace clo {
 namespace {
 
 constexpr size_t kNoAllocMaxElems = (size_t)CLO_NOALLOC_MAX_TILES * kTile;
+static_assert(kNoAllocMaxElems == ((size_t)1 << 28), "no-allocation scan limit");
 
 std::mutex g_noalloc_mu;
 uint64_t *g_noalloc_addr[64] = {};
@@ -312,7 +501,7 @@ uint64_t *noalloc_scratch(int ordinal, GError **err) {
 
 template <typename InT, typename OutT>
 cudaError_t launch_scan_noalloc(const void *in, void *out, size_t n,
-	uint64_t *scratch, int *dev_status, cudaStream_t s) {
+	uint64_t *scratch, int *dev_status, int sm_count, cudaStream_t s) {
 	using Acc = typename std::conditional<(sizeof(OutT) <= 4), uint32_t,
 		uint64_t>::type;
 	const size_t tiles = (n + kTile - 1) / kTile;
@@ -326,7 +515,11 @@ cudaError_t launch_scan_noalloc(const void *in, void *out, size_t n,
 	if (e == cudaSuccess) e = cudaMemsetAsync(ts.counter, 0, sizeof(uint64_t), s);
 	if (e != cudaSuccess) return e;
 	bool vec_ok = ((uintptr_t)in % 16 == 0) && ((uintptr_t)out % 16 == 0);
-	scan_lookback<InT, OutT><<<(unsigned)tiles, kThreads, 0, s>>>(
+	int per_sm = 1;
+	e = scan_prepare<InT, OutT>(&per_sm);
+	if (e != cudaSuccess) return e;
+	scan_lookback<InT, OutT><<<scan_grid(tiles, per_sm, sm_count), kThreads,
+		scan_smem<InT, OutT>(), s>>>(
 		(const InT *)in, (OutT *)out, n, ts, dev_status, vec_ok, -1, nullptr, nullptr);
 	count_launches(1);
 	return cudaGetLastError();
@@ -334,12 +527,12 @@ cudaError_t launch_scan_noalloc(const void *in, void *out, size_t n,
 
 template <typename InT>
 cudaError_t noalloc_out(const void *in, void *out, size_t n, int out_bytes,
-	uint64_t *scratch, int *st, cudaStream_t s) {
+	uint64_t *scratch, int *st, int sms, cudaStream_t s) {
 	switch (out_bytes) {
-	case 1: return launch_scan_noalloc<InT, uint8_t>(in, out, n, scratch, st, s);
-	case 2: return launch_scan_noalloc<InT, uint16_t>(in, out, n, scratch, st, s);
-	case 4: return launch_scan_noalloc<InT, uint32_t>(in, out, n, scratch, st, s);
-	default: return launch_scan_noalloc<InT, uint64_t>(in, out, n, scratch, st, s);
+	case 1: return launch_scan_noalloc<InT, uint8_t>(in, out, n, scratch, st, sms, s);
+	case 2: return launch_scan_noalloc<InT, uint16_t>(in, out, n, scratch, st, sms, s);
+	case 4: return launch_scan_noalloc<InT, uint32_t>(in, out, n, scratch, st, sms, s);
+	default: return launch_scan_noalloc<InT, uint64_t>(in, out, n, scratch, st, sms, s);
 	}
 }
 
@@ -377,17 +570,18 @@ extern "C" cl_bool clo_scan_blelloch_noalloc(CCLQueue *cq, CloType elem_type,
 	cudaSetDevice(cq->ctx->ordinal);
 	const int ob = (int)clo_type_sizeof(sum_type);
 	int *st = cq->ctx->d_status;
+	const int sms = cq->ctx->sm_count;
 	cudaStream_t s = cq->stream;
 	cudaError_t e;
 	switch (elem_type) {
-	case CLO_CHAR: e = noalloc_out<int8_t>(d_in, d_out, numel, ob, scratch, st, s); break;
-	case CLO_UCHAR: e = noalloc_out<uint8_t>(d_in, d_out, numel, ob, scratch, st, s); break;
-	case CLO_SHORT: e = noalloc_out<int16_t>(d_in, d_out, numel, ob, scratch, st, s); break;
-	case CLO_USHORT: e = noalloc_out<uint16_t>(d_in, d_out, numel, ob, scratch, st, s); break;
-	case CLO_INT: e = noalloc_out<int32_t>(d_in, d_out, numel, ob, scratch, st, s); break;
-	case CLO_UINT: e = noalloc_out<uint32_t>(d_in, d_out, numel, ob, scratch, st, s); break;
-	case CLO_LONG: e = noalloc_out<int64_t>(d_in, d_out, numel, ob, scratch, st, s); break;
-	default: e = noalloc_out<uint64_t>(d_in, d_out, numel, ob, scratch, st, s); break;
+	case CLO_CHAR: e = noalloc_out<int8_t>(d_in, d_out, numel, ob, scratch, st, sms, s); break;
+	case CLO_UCHAR: e = noalloc_out<uint8_t>(d_in, d_out, numel, ob, scratch, st, sms, s); break;
+	case CLO_SHORT: e = noalloc_out<int16_t>(d_in, d_out, numel, ob, scratch, st, sms, s); break;
+	case CLO_USHORT: e = noalloc_out<uint16_t>(d_in, d_out, numel, ob, scratch, st, sms, s); break;
+	case CLO_INT: e = noalloc_out<int32_t>(d_in, d_out, numel, ob, scratch, st, sms, s); break;
+	case CLO_UINT: e = noalloc_out<uint32_t>(d_in, d_out, numel, ob, scratch, st, sms, s); break;
+	case CLO_LONG: e = noalloc_out<int64_t>(d_in, d_out, numel, ob, scratch, st, sms, s); break;
+	default: e = noalloc_out<uint64_t>(d_in, d_out, numel, ob, scratch, st, sms, s); break;
 	}
 	return cuda_ok(e, err, "clo_scan_blelloch_noalloc") ? CL_TRUE : CL_FALSE;
 }

@@ -9,7 +9,7 @@
  * src/cl_ops/rng/clo_rng.in.h:97-111). cf4ocl2 itself is a third-party
  * OpenCL wrapper and is not part of this library; what is declared here is
  * the subset of its API that the reference's library code, tests
- * (src/tests/test_rng.c) and benchmarks (src/benchmarks/*.c) call, with the
+ * (src/tests/test_rng.c) and benchmarks (src/benchmarks/clo_*_bench.c) call, with the
  * same names and argument meanings, mapped onto CUDA:
  *
  *   CCLContext  one CUDA device (primary context) + a stream-ordered

@@ -76,7 +76,7 @@ int clo_gb300_timing_get(const char *kernel, double *total_ms,
  * an allocation that may synchronise the device. The caller passes the
  * device input and output pointers; the scan's own scratch (its tile
  * statuses) is a file-scope device array of this library, sized for at
- * most 2^28 elements (2 MiB, held on every GPU that loads the library
+ * most 2^28 elements (1 MiB, held on every GPU that loads the library
  * until the process exits). Larger numel is rejected with CLO_ERROR_ARGS.
  *
  * The first call on a device looks the array's device address up

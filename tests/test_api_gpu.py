@@ -130,10 +130,11 @@ def test_wrapper_memcheck_after_objects(clops):
 
 
 def test_lookback_watchdog_reports_and_context_survives(clops, ctx, queue):
-    """A tile that never publishes its status: the successor's bounded wait
-    runs out (about a second), the kernel still ends, the error is reported
-    as CLO_ERROR_LIBRARY and the context keeps working."""
-    a = np.ones(3 * 4096, dtype=np.uint32)
+    """A tile that never publishes its status: the successors' bounded waits
+    run out (about a second), the kernel still ends, the error is reported
+    as CLO_ERROR_LIBRARY and the context keeps working. 2^18 elements span
+    several tiles whatever the tile size."""
+    a = np.ones(1 << 18, dtype=np.uint32)
     sc = clops.Scanner(ctx, 5, 5)
     bi = clops.Buffer.from_array(ctx, queue, a)
     bo = clops.Buffer(ctx, a.nbytes)
