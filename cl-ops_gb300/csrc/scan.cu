@@ -46,9 +46,15 @@ constexpr int kBlock = 32 * kItems;              // 512 elements
 constexpr int kBlocks = 2;                       // blocks per warp
 constexpr int kWarpElems = kBlocks * kBlock;     // 1024
 constexpr int kTile = kWarps * kWarpElems;       // 8192
-constexpr int kPadded = kBlock + kBlock / 32;    // padded block in shared memory
-
-__device__ __forceinline__ int pidx(int i) { return i + (i >> 5); }
+// A block in shared memory is padded by one element per 128 bytes
+// (per 32 elements of 4 bytes or fewer, per 16 of 8 bytes), so both the
+// lanes' 16-element runs and the 16-byte vector columns are conflict-free.
+template <typename T>
+__host__ __device__ constexpr int pad_shift() { return sizeof(T) == 8 ? 4 : 5; }
+template <typename T>
+__host__ __device__ constexpr int padded() { return kBlock + (kBlock >> pad_shift<T>()); }
+template <typename T>
+__device__ __forceinline__ int pidx(int i) { return i + (i >> pad_shift<T>()); }
 
 using lb::Slots;
 using lb::TileStatus;
@@ -65,7 +71,7 @@ __device__ __forceinline__ Acc shfl_up(Acc v, int d) {
 // staging block.
 template <typename InT, typename OutT>
 constexpr size_t scan_smem() {
-	return (size_t)kWarps * kPadded * (kBlocks * sizeof(InT) + sizeof(OutT));
+	return (size_t)kWarps * (kBlocks * padded<InT>() * sizeof(InT) + padded<OutT>() * sizeof(OutT));
 }
 
 // Resident CTAs per SM (228 KB per SM, 1 KB reserved per CTA), at most 4,
@@ -82,7 +88,7 @@ template <typename InT>
 __device__ __forceinline__ void load_block_scalar(const InT *__restrict__ in, size_t n,
 	size_t seg, InT *sin, int lane) {
 	for (int i = lane; i < kBlock; i += 32)
-		sin[pidx(i)] = (seg + i < n) ? in[seg + i] : (InT)0;
+		sin[pidx<InT>(i)] = (seg + i < n) ? in[seg + i] : (InT)0;
 }
 
 template <typename InT>
@@ -111,13 +117,13 @@ __device__ __forceinline__ void store_loads(const BlockRegs<InT> &r, InT *s_in, 
 	constexpr int EPC = BlockRegs<InT>::kEpc;
 #pragma unroll
 	for (int b = 0; b < kBlocks; ++b) {
-		InT *sin = s_in + b * kPadded;
+		InT *sin = s_in + b * padded<InT>();
 #pragma unroll
 		for (int k = 0; k < BlockRegs<InT>::kPerLane; ++k) {
 			const int c = lane + 32 * k;
 			const InT *e = reinterpret_cast<const InT *>(&r.v[b][k]);
 #pragma unroll
-			for (int q = 0; q < EPC; ++q) sin[pidx(c * EPC + q)] = e[q];
+			for (int q = 0; q < EPC; ++q) sin[pidx<InT>(c * EPC + q)] = e[q];
 		}
 	}
 }
@@ -148,9 +154,9 @@ scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, size_t n,
 
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const uint32_t num_tiles = (uint32_t)((n + kTile - 1) / kTile);
-	InT *s_in = reinterpret_cast<InT *>(s_dyn + (size_t)warp * kPadded *
-		(kBlocks * sizeof(InT) + sizeof(OutT)));
-	OutT *s_out = reinterpret_cast<OutT *>(s_in + kBlocks * kPadded);
+	InT *s_in = reinterpret_cast<InT *>(s_dyn + (size_t)warp *
+		(kBlocks * padded<InT>() * sizeof(InT) + padded<OutT>() * sizeof(OutT)));
+	OutT *s_out = reinterpret_cast<OutT *>(s_in + kBlocks * padded<InT>());
 	auto full_tile = [&](uint32_t t) {
 		return vec_ok && (size_t)(t + 1) * kTile <= n;
 	};
@@ -167,7 +173,7 @@ scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, size_t n,
 		} else {
 #pragma unroll
 			for (int b = 0; b < kBlocks; ++b)
-				load_block_scalar<InT>(in, n, wseg + (size_t)b * kBlock, s_in + b * kPadded, lane);
+				load_block_scalar<InT>(in, n, wseg + (size_t)b * kBlock, s_in + b * padded<InT>(), lane);
 		}
 	}
 	__syncwarp();
@@ -181,10 +187,10 @@ scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, size_t n,
 		Acc lane_excl[kBlocks], block_tot[kBlocks];
 #pragma unroll
 		for (int b = 0; b < kBlocks; ++b) {
-			const InT *sin = s_in + b * kPadded;
+			const InT *sin = s_in + b * padded<InT>();
 			Acc run = 0;
 #pragma unroll
-			for (int j = 0; j < kItems; ++j) run += (Acc)(OutT)sin[pidx(lane * kItems + j)];
+			for (int j = 0; j < kItems; ++j) run += (Acc)(OutT)sin[pidx<InT>(lane * kItems + j)];
 			Acc inc = run;
 #pragma unroll
 			for (int d = 1; d < 32; d <<= 1) {
@@ -271,13 +277,13 @@ scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, size_t n,
 		Acc base = s_excl + s_warp_tot[warp];
 #pragma unroll
 		for (int b = 0; b < kBlocks; ++b) {
-			const InT *sin = s_in + b * kPadded;
+			const InT *sin = s_in + b * padded<InT>();
 			Acc run = base + lane_excl[b];
 #pragma unroll
 			for (int j = 0; j < kItems; ++j) {
-				const int q = pidx(lane * kItems + j);
-				const Acc v = (Acc)(OutT)sin[q];
-				s_out[q] = (OutT)run;
+				const int q = lane * kItems + j;
+				const Acc v = (Acc)(OutT)sin[pidx<InT>(q)];
+				s_out[pidx<OutT>(q)] = (OutT)run;
 				run += v;
 			}
 			base += block_tot[b];
@@ -292,12 +298,12 @@ scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, size_t n,
 					uint4 v;
 					OutT *e = reinterpret_cast<OutT *>(&v);
 #pragma unroll
-					for (int k = 0; k < EPC; ++k) e[k] = s_out[pidx(c * EPC + k)];
+					for (int k = 0; k < EPC; ++k) e[k] = s_out[pidx<OutT>(c * EPC + k)];
 					dev::st_stream_v4(dst + c, v);
 				}
 			} else {
 				for (int i = lane; i < kBlock; i += 32)
-					if (seg + i < n) out[seg + i] = s_out[pidx(i)];
+					if (seg + i < n) out[seg + i] = s_out[pidx<OutT>(i)];
 			}
 			__syncwarp();
 		}
@@ -309,7 +315,7 @@ scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, size_t n,
 		} else {
 #pragma unroll
 			for (int b = 0; b < kBlocks; ++b)
-				load_block_scalar<InT>(in, n, nseg + (size_t)b * kBlock, s_in + b * kPadded, lane);
+				load_block_scalar<InT>(in, n, nseg + (size_t)b * kBlock, s_in + b * padded<InT>(), lane);
 		}
 		__syncwarp();
 		agg_published = next_full;

@@ -172,6 +172,26 @@ def test_satradix_2pow28_u32_sorted_permutation(clops, ctx, queue):
 
 
 @pytest.mark.slow
+def test_satradix_more_chunks_than_resident_ctas(clops, ctx, queue):
+    """5 x 2^27 + 777 keys: more than 2^20 keys per chunk at one chunk per
+    resident CTA, so the pass runs extra chunks in a second wave (each
+    waiting only on chunks claimed before it) and the upsweep grid is
+    sized by its per-thread key cap."""
+    n = 5 * (1 << 27) + 777
+    a = keys_u32(46, n)
+    s = clops.Sorter(ctx, "satradix", 5)
+    b = clops.Buffer.from_array(ctx, queue, a)
+    clops.wait(s.sort_device(queue, b, n))
+    got = b.read(queue, np.uint32, n)
+    assert np.all(got[1:] >= got[:-1])
+    assert int(got.astype(np.uint64).sum()) == int(a.astype(np.uint64).sum())
+    np.testing.assert_array_equal(np.bincount(got >> 16, minlength=1 << 16),
+                                  np.bincount(a >> 16, minlength=1 << 16))
+    b.destroy()
+    s.destroy()
+
+
+@pytest.mark.slow
 def test_satradix_kv_2pow27_stable_permutation(clops, ctx, queue):
     n = 1 << 27
     k = keys_u64(43, n) & np.uint64(0xFFFF0000000000FF)  # many duplicates
