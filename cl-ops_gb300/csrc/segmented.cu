@@ -835,9 +835,15 @@ constexpr int kSWarps = kSThreads / 32;
 constexpr int kSItems = 16;
 constexpr int kSWarpElems = 32 * kSItems;
 constexpr int kSTile = kSWarps * kSWarpElems;
-constexpr int kSPadded = kSWarpElems + kSWarpElems / 32;
-
-__device__ __forceinline__ int pidx(int i) { return i + (i >> 5); }
+// A warp's elements in shared memory are padded by one element per 128
+// bytes (per 32 elements of 4 bytes or fewer, per 16 of 8 bytes), so the
+// lanes' 16-element runs and the 16-byte vector columns are conflict-free.
+template <typename T>
+__host__ __device__ constexpr int spad_shift() { return sizeof(T) == 8 ? 4 : 5; }
+template <typename T>
+__host__ __device__ constexpr int spadded() { return kSWarpElems + (kSWarpElems >> spad_shift<T>()); }
+template <typename T>
+__device__ __forceinline__ int pidx(int i) { return i + (i >> spad_shift<T>()); }
 
 // Head bitmap: bit i set when a segment starts at element i (and holds
 // elements).
@@ -862,10 +868,12 @@ seg_scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, uint64_t n
 	const uint32_t *__restrict__ heads, const uint64_t *off, uint32_t S,
 	lb::TileStatus ts, int *dev_status, bool vec_ok) {
 	using Acc = typename std::conditional<(sizeof(OutT) <= 4), uint32_t, uint64_t>::type;
-	constexpr int ESZ = sizeof(InT) > sizeof(OutT) ? sizeof(InT) : sizeof(OutT);
 	constexpr int PT = lb::Slots<Acc>::kPerTile;
 	constexpr int KW = lb::Slots<Acc>::kWords;
-	__shared__ __align__(16) unsigned char s_buf[kSWarps][kSPadded * ESZ];
+	// Inputs, then (once they are in registers) outputs, in one buffer.
+	constexpr int kBufBytes = spadded<InT>() * (int)sizeof(InT) > spadded<OutT>() * (int)sizeof(OutT)
+		? spadded<InT>() * (int)sizeof(InT) : spadded<OutT>() * (int)sizeof(OutT);
+	__shared__ __align__(16) unsigned char s_buf[kSWarps][kBufBytes];
 	__shared__ Acc s_wsum[kSWarps];
 	__shared__ uint32_t s_wflag[kSWarps];
 	__shared__ Acc s_excl;
@@ -894,11 +902,11 @@ seg_scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, uint64_t n
 			uint4 v = dev::ld_stream_v4(src + c);
 			const InT *e = reinterpret_cast<const InT *>(&v);
 #pragma unroll
-			for (int k = 0; k < EPC; ++k) sin[pidx(c * EPC + k)] = e[k];
+			for (int k = 0; k < EPC; ++k) sin[pidx<InT>(c * EPC + k)] = e[k];
 		}
 	} else {
 		for (int i = lane; i < kSWarpElems; i += 32)
-			sin[pidx(i)] = (seg + i < n) ? in[seg + i] : (InT)0;
+			sin[pidx<InT>(i)] = (seg + i < n) ? in[seg + i] : (InT)0;
 	}
 	// This thread's 16 elements start at a multiple of 16: their head bits
 	// are one half of one bitmap word.
@@ -910,7 +918,7 @@ seg_scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, uint64_t n
 	Acc run = 0;
 #pragma unroll
 	for (int j = 0; j < kSItems; ++j) {
-		const Acc v = (Acc)(OutT)sin[pidx(lane * kSItems + j)];
+		const Acc v = (Acc)(OutT)sin[pidx<InT>(lane * kSItems + j)];
 		if ((hb >> j) & 1u) run = 0;
 		x[j] = run;
 		run += v;
@@ -987,7 +995,7 @@ seg_scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, uint64_t n
 	OutT *sout = reinterpret_cast<OutT *>(s_buf[warp]);
 #pragma unroll
 	for (int j = 0; j < kSItems; ++j)
-		sout[pidx(lane * kSItems + j)] = (OutT)(x[j] + (j < fh ? tcarry : (Acc)0));
+		sout[pidx<OutT>(lane * kSItems + j)] = (OutT)(x[j] + (j < fh ? tcarry : (Acc)0));
 	__syncwarp();
 	if (full && vec_ok && seg >= lo && seg + kSWarpElems <= hi) {
 		constexpr int EPC = 16 / sizeof(OutT);
@@ -998,13 +1006,13 @@ seg_scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, uint64_t n
 			uint4 v;
 			OutT *e = reinterpret_cast<OutT *>(&v);
 #pragma unroll
-			for (int k = 0; k < EPC; ++k) e[k] = sout[pidx(c * EPC + k)];
+			for (int k = 0; k < EPC; ++k) e[k] = sout[pidx<OutT>(c * EPC + k)];
 			dev::st_stream_v4(dst + c, v);
 		}
 	} else {
 		for (int i = lane; i < kSWarpElems; i += 32) {
 			const uint64_t g = seg + i;
-			if (g < n && g >= lo && g < hi) out[g] = sout[pidx(i)];
+			if (g < n && g >= lo && g < hi) out[g] = sout[pidx<OutT>(i)];
 		}
 	}
 }
