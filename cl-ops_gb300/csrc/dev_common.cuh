@@ -104,5 +104,23 @@ __device__ __forceinline__ uint32_t warp_rank_digit(uint32_t *match, uint32_t *h
 	return start + below;
 }
 
+// Stable rank of a key within its half-warp unit (16 lanes) for one round:
+// w is the unit's word for the key's digit (next position << 16 | peer
+// mask). Lanes OR in their bit and read the word back; the lowest peer
+// stores the advanced position with the mask cleared. Returns the key's
+// position.
+__device__ __forceinline__ uint32_t unit_rank_digit(uint32_t *w, uint32_t l16,
+	uint32_t lt16) {
+	atomicOr(w, 1u << l16);
+	__syncwarp();
+	const uint32_t v = *w;
+	__syncwarp();
+	const uint32_t peers = v & 0xFFFFu;
+	const uint32_t below = __popc(peers & lt16);
+	if (below == 0) *w = (v & 0xFFFF0000u) + ((uint32_t)__popc(peers) << 16);
+	__syncwarp();
+	return (v >> 16) + below;
+}
+
 }  // namespace dev
 }  // namespace clo

@@ -269,25 +269,6 @@ __device__ __forceinline__ void chunk_load_vals(V (&v)[ChunkCfg<K, THREADS>::kKp
 	}
 }
 
-// Stable rank of a key within its half-warp unit for one round: w is the
-// unit's word for the key's digit (next position << 16 | peer mask). Lanes
-// OR in their bit and read the word back; the lowest peer stores the
-// advanced position with the mask cleared. Returns the key's position.
-__device__ __forceinline__ uint32_t unit_rank_digit(uint32_t *w, uint32_t l16,
-	uint32_t lt16) {
-	atomicOr(w, 1u << l16);
-	__syncwarp();
-	const uint32_t v = *w;
-	__syncwarp();
-	const uint32_t peers = v & 0xFFFFu;
-	const uint32_t below = __popc(peers & lt16);
-	if (below == 0) *w = (v & 0xFFFF0000u) + ((uint32_t)__popc(peers) << 16);
-	__syncwarp();
-	return (v >> 16) + below;
-}
-
-// Shared memory of the pass: the ranking words, the unit counts, five
-// 256-entry tables, and the key (and value) stage of one tile.
 template <typename K, typename V, bool HAS_V, int THREADS>
 constexpr size_t chunked_smem() {
 	using Cfg = ChunkCfg<K, THREADS>;
@@ -516,7 +497,7 @@ radix_pass_chunked(const K *__restrict__ kin, K *__restrict__ kout,
 		V *sv = reinterpret_cast<V *>(s_stage + (size_t)TILE * sizeof(K));
 #pragma unroll
 		for (int j = 0; j < KPT; ++j) {
-			const uint32_t pos = unit_rank_digit(my_rank + digit_of(k[j], shift), l16, lt16);
+			const uint32_t pos = dev::unit_rank_digit(my_rank + digit_of(k[j], shift), l16, lt16);
 			if (pos < (uint32_t)TILE) {
 				sk[pos] = k[j];
 				if (HAS_V) sv[pos] = v[j];
