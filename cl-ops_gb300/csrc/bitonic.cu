@@ -33,6 +33,8 @@
 #include <climits>
 
 #include "clo_internal.h"
+#include <type_traits>
+
 #include "dev_common.cuh"
 #include "timing.h"
 
@@ -204,6 +206,205 @@ abitonic_tile_finish(T *data, int t, int stage, int maxg) {
 	tile_store(g, s, tile_n);
 }
 
+// ------------------------------------ register-phase tiles (<= 4 bytes)
+// Tiles of 2^14 elements, 512 threads, 32 elements per thread held in
+// registers. In layout L(B0) register m of thread tid holds tile element
+//   ((tid >> B0) << (B0 + 5)) | (m << B0) | (tid & (2^B0 - 1)),
+// so the steps on index bits B0 .. B0 + 4 are compare-exchanges between a
+// thread's own registers. A stage's steps (bits top .. 0) run in up to
+// three such phases -- bits 13..9 in L(9), 8..5 in L(4), 4..0 in L(0) --
+// joined by transposes through the padded shared tile (each layout puts a
+// warp's 32 accesses in 32 banks). Per tile pass this is two shared
+// stores and two loads per element instead of one of each per four steps.
+// The steps and their order are those of the network, so the result is
+// the same as the shared-memory rounds' (and the reference's).
+constexpr int kRLog = 14, kRE = 5, kRThreads = 512, kRN = 1 << kRE;
+
+template <int B0>
+__device__ __forceinline__ uint32_t lidx(uint32_t tid, uint32_t m) {
+	return ((tid >> B0) << (B0 + kRE)) | (m << B0) | (tid & ((1u << B0) - 1u));
+}
+
+// Compare-exchange with a direction fixed at compile time: for integers a
+// min/max pair (swap iff a > b ascending, iff a <= b descending: the same
+// values either way), otherwise the network's own compare.
+template <bool DESC, typename T>
+__device__ __forceinline__ void cx_s(T &a, T &b) {
+	if constexpr (std::is_integral<T>::value) {
+		const T lo = a < b ? a : b, hi = a < b ? b : a;
+		a = DESC ? hi : lo;
+		b = DESC ? lo : hi;
+	} else {
+		cmpxchg(a, b, DESC);
+	}
+}
+
+// Steps on bits HI .. LO (within B0 .. B0 + 4) in layout L(B0); dir(a, b, m)
+// compare-exchanges registers m and m | stride.
+template <int B0, int HI, int LO, typename T, typename Dir>
+__device__ __forceinline__ void rphase(T (&r)[kRN], Dir dir) {
+#pragma unroll
+	for (int b = HI; b >= LO; --b) {
+		const int sb = 1 << (b - B0);
+#pragma unroll
+		for (int m = 0; m < kRN; ++m)
+			if (!(m & sb)) dir(r[m], r[m | sb], m);
+	}
+}
+
+// Padded shared-memory slot of element (tid, m) of L(B0), split as a
+// per-thread base plus a per-register constant: the register bits never
+// carry into the padding term, so
+//   spad(lidx(tid, m)) = spad(lidx(tid, 0)) + (m << B0) + ((m << B0) >> 5).
+template <int B0>
+__device__ __forceinline__ uint32_t lbase(uint32_t tid) {
+	return spad(lidx<B0>(tid, 0));
+}
+template <int B0>
+__host__ __device__ constexpr uint32_t loff(int m) {
+	return ((uint32_t)m << B0) + (((uint32_t)m << B0) >> 5);
+}
+
+template <int FROM, int TO, typename T>
+__device__ __forceinline__ void rtranspose(T (&r)[kRN], T *s, uint32_t tid) {
+	__syncthreads();
+	T *sf = s + lbase<FROM>(tid);
+#pragma unroll
+	for (int m = 0; m < kRN; ++m) sf[loff<FROM>(m)] = r[m];
+	__syncthreads();
+	const T *st = s + lbase<TO>(tid);
+#pragma unroll
+	for (int m = 0; m < kRN; ++m) r[m] = st[loff<TO>(m)];
+}
+
+// One phase of stage S (< kRLog) in layout L(B0): the direction of a pair
+// is bit S of its lower element's tile index, which is a register bit
+// (fixed per register) or a thread bit (fixed per thread).
+template <int S, int B0, int HI, int LO, typename T>
+__device__ __forceinline__ void sort_phase(T (&r)[kRN], uint32_t tid) {
+	if constexpr (S >= B0 && S < B0 + kRE) {
+		rphase<B0, HI, LO>(r, [](T &a, T &b, int m) {
+			if ((m >> (S - B0)) & 1) cx_s<true>(a, b);
+			else cx_s<false>(a, b);
+		});
+	} else {
+		const bool d = (tid >> (S < B0 ? S : S - kRE)) & 1u;
+		rphase<B0, HI, LO>(r, [d](T &a, T &b, int) { cmpxchg(a, b, d); });
+	}
+}
+
+// Stage S (< kRLog) of the tile sort; the registers are in L(0) before and
+// after.
+template <int S, typename T>
+__device__ __forceinline__ void sort_stage(T (&r)[kRN], T *s, uint32_t tid) {
+	constexpr int top = S - 1;
+	if constexpr (top >= 9) {
+		rtranspose<0, 9>(r, s, tid);
+		sort_phase<S, 9, top, 9>(r, tid);
+		rtranspose<9, 4>(r, s, tid);
+		sort_phase<S, 4, 8, 5>(r, tid);
+		rtranspose<4, 0>(r, s, tid);
+		sort_phase<S, 0, 4, 0>(r, tid);
+	} else if constexpr (top >= 5) {
+		rtranspose<0, 4>(r, s, tid);
+		sort_phase<S, 4, top, 5>(r, tid);
+		rtranspose<4, 0>(r, s, tid);
+		sort_phase<S, 0, 4, 0>(r, tid);
+	} else {
+		sort_phase<S, 0, top, 0>(r, tid);
+	}
+}
+
+template <int S, typename T>
+__device__ __forceinline__ void sort_stages(T (&r)[kRN], T *s, uint32_t tid) {
+	sort_stage<S>(r, s, tid);
+	if constexpr (S + 1 < kRLog) sort_stages<S + 1>(r, s, tid);
+}
+
+// All 14 steps of a stage with one direction for the whole tile, starting
+// in L(9) and ending in L(0).
+template <bool D, typename T>
+__device__ __forceinline__ void full_stage_uniform(T (&r)[kRN], T *s, uint32_t tid) {
+	auto dir = [](T &a, T &b, int) { cx_s<D>(a, b); };
+	rphase<9, 13, 9>(r, dir);
+	rtranspose<9, 4>(r, s, tid);
+	rphase<4, 8, 5>(r, dir);
+	rtranspose<4, 0>(r, s, tid);
+	rphase<0, 4, 0>(r, dir);
+}
+
+template <typename T>
+__device__ __forceinline__ void rload_l0(T (&r)[kRN], const T *g, T *s, uint32_t tid) {
+	if constexpr (sizeof(T) == 4) {
+		const uint4 *src = reinterpret_cast<const uint4 *>(g + ((size_t)tid << kRE));
+#pragma unroll
+		for (int q = 0; q < kRN / 4; ++q) {
+			const uint4 v = src[q];
+			r[4 * q + 0] = __builtin_bit_cast(T, v.x);
+			r[4 * q + 1] = __builtin_bit_cast(T, v.y);
+			r[4 * q + 2] = __builtin_bit_cast(T, v.z);
+			r[4 * q + 3] = __builtin_bit_cast(T, v.w);
+		}
+	} else {
+#pragma unroll
+		for (int m = 0; m < kRN; ++m) r[m] = g[lidx<9>(tid, m)];
+		rtranspose<9, 0>(r, s, tid);
+	}
+}
+
+template <typename T>
+__device__ __forceinline__ void rstore_l0(T *g, T (&r)[kRN], T *s, uint32_t tid) {
+	if constexpr (sizeof(T) == 4) {
+		uint4 *dst = reinterpret_cast<uint4 *>(g + ((size_t)tid << kRE));
+#pragma unroll
+		for (int q = 0; q < kRN / 4; ++q)
+			dst[q] = make_uint4(__builtin_bit_cast(uint32_t, r[4 * q + 0]),
+				__builtin_bit_cast(uint32_t, r[4 * q + 1]),
+				__builtin_bit_cast(uint32_t, r[4 * q + 2]),
+				__builtin_bit_cast(uint32_t, r[4 * q + 3]));
+	} else {
+		rtranspose<0, 9>(r, s, tid);
+#pragma unroll
+		for (int m = 0; m < kRN; ++m) g[lidx<9>(tid, m)] = r[m];
+	}
+}
+
+// Stages 1..14 of every tile of 2^14 elements.
+template <typename T>
+__global__ void __launch_bounds__(kRThreads, 2)
+abitonic_tile_sort_r(T *data) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	T *s = reinterpret_cast<T *>(smem_raw);
+	const uint32_t tid = threadIdx.x;
+	const size_t tile_base = (size_t)blockIdx.x << kRLog;
+	T *g = data + tile_base;
+	T r[kRN];
+	rload_l0(r, g, s, tid);
+	sort_stages<1>(r, s, tid);
+	// Stage 14: one direction for the tile (bit 14 of its global index).
+	rtranspose<0, 9>(r, s, tid);
+	if ((tile_base >> kRLog) & 1) full_stage_uniform<true>(r, s, tid);
+	else full_stage_uniform<false>(r, s, tid);
+	rstore_l0(g, r, s, tid);
+}
+
+// Steps 14..1 of `stage` (> 14) for every tile.
+template <typename T>
+__global__ void __launch_bounds__(kRThreads, 2)
+abitonic_tile_finish_r(T *data, int stage) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	T *s = reinterpret_cast<T *>(smem_raw);
+	const uint32_t tid = threadIdx.x;
+	const size_t tile_base = (size_t)blockIdx.x << kRLog;
+	T *g = data + tile_base;
+	T r[kRN];
+#pragma unroll
+	for (int m = 0; m < kRN; ++m) r[m] = g[lidx<9>(tid, m)];
+	if ((tile_base >> stage) & 1) full_stage_uniform<true>(r, s, tid);
+	else full_stage_uniform<false>(r, s, tid);
+	rstore_l0(g, r, s, tid);
+}
+
 template <typename T>
 __global__ void fill_value(T *p, size_t n, T v) {
 	size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -260,9 +461,26 @@ cudaError_t run_abitonic(T *d, size_t N, int max_ps, int max_sfs,
 	if (e != cudaSuccess) return e;
 	const size_t tiles = N >> t;
 	const double pass_bytes = 2.0 * (double)N * sizeof(T);
+	// Register-phase tile kernels for full 2^14 tiles of up to 4-byte types
+	// with the default grouping.
+	bool rtiles = false;
+	if constexpr (sizeof(T) <= 4) {
+		rtiles = t == kRLog && maxg == 4;
+		if (rtiles) {
+			e = cudaFuncSetAttribute(abitonic_tile_sort_r<T>,
+				cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+			if (e == cudaSuccess)
+				e = cudaFuncSetAttribute(abitonic_tile_finish_r<T>,
+					cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+			if (e != cudaSuccess) return e;
+		}
+	}
 	{
 		KernelTimer tm("abitonic_tile_sort", s, pass_bytes);
-		abitonic_tile_sort<T><<<(unsigned)tiles, threads, smem, s>>>(d, t, maxg);
+		if constexpr (sizeof(T) <= 4) {
+			if (rtiles) abitonic_tile_sort_r<T><<<(unsigned)tiles, kRThreads, smem, s>>>(d);
+		}
+		if (!rtiles) abitonic_tile_sort<T><<<(unsigned)tiles, threads, smem, s>>>(d, t, maxg);
 		tm.stop();
 	}
 	launches++;
@@ -285,7 +503,10 @@ cudaError_t run_abitonic(T *d, size_t N, int max_ps, int max_sfs,
 			j -= g;
 		}
 		KernelTimer tf("abitonic_tile_finish", s, pass_bytes);
-		abitonic_tile_finish<T><<<(unsigned)tiles, threads, smem, s>>>(d, t, stage, maxg);
+		if constexpr (sizeof(T) <= 4) {
+			if (rtiles) abitonic_tile_finish_r<T><<<(unsigned)tiles, kRThreads, smem, s>>>(d, stage);
+		}
+		if (!rtiles) abitonic_tile_finish<T><<<(unsigned)tiles, threads, smem, s>>>(d, t, stage, maxg);
 		tf.stop();
 		launches++;
 		e = cudaGetLastError();
