@@ -487,7 +487,11 @@ cudaError_t run_abitonic(T *d, size_t N, int max_ps, int max_sfs,
 	for (int stage = t + 1; stage <= logN && e == cudaSuccess; ++stage) {
 		int j = stage;
 		while (j > t) {
-			int g = std::min(gmaxg, j - t);
+			// Balanced groups (6 steps as 3 + 3, not 5 + 1): a pass of few
+			// steps per thread is the slowest per byte.
+			const int rem = j - t;
+			const int npass = (rem + gmaxg - 1) / gmaxg;
+			int g = (rem + npass - 1) / npass;
 			size_t groups = N >> g;
 			unsigned blocks = (unsigned)((groups + 255) / 256);
 			KernelTimer tm("abitonic_global_steps", s, pass_bytes);
