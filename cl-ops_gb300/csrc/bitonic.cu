@@ -465,7 +465,8 @@ cudaError_t run_abitonic(T *d, size_t N, int max_ps, int max_sfs,
 	// with the default grouping.
 	bool rtiles = false;
 	if constexpr (sizeof(T) <= 4) {
-		rtiles = t == kRLog && maxg == 4;
+		// (16-byte vector accesses need an aligned array.)
+		rtiles = t == kRLog && maxg == 4 && ((uintptr_t)d % 16) == 0;
 		if (rtiles) {
 			e = cudaFuncSetAttribute(abitonic_tile_sort_r<T>,
 				cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
