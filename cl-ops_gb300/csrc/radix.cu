@@ -89,6 +89,20 @@ radix_upsweep(const K *__restrict__ keys, size_t n, uint32_t *__restrict__ hist,
 		if (COLS) atomicAdd(base + p * kPosWords + (d >> 1) * 32, 1u << ((d & 1) << 4));
 		else atomicAdd(base + p * kPosWords + d, 1u);
 	};
+	// 32-bit keys at shift 0 with four positions: the four column rows
+	// (d >> 1) and half selectors (d & 1) come out of two word-wide masks,
+	// then one byte extract, one address add and the atomic per position.
+	auto count4 = [&](uint32_t key) {
+		const uint32_t rows = (key >> 1) & 0x7F7F7F7Fu;
+		const uint32_t halves = (key & 0x01010101u) << 4;  // 0 or 16 per byte
+#pragma unroll
+		for (int p = 0; p < 4; ++p) {
+			const uint32_t row = __byte_perm(rows, 0, 0x4440 + p);
+			const uint32_t sh = __byte_perm(halves, 0, 0x4440 + p);
+			atomicAdd(base + p * kPosWords + row * 32, 1u << sh);
+		}
+	};
+	constexpr bool kFast4 = COLS && PASSES == 4 && sizeof(K) == 4;
 	constexpr int PER = 16 / sizeof(K);  // keys per 16-byte load
 	const bool aligned = ((uintptr_t)keys % 16) == 0;
 	const size_t nvec = aligned ? n / PER : 0;
@@ -102,10 +116,15 @@ radix_upsweep(const K *__restrict__ keys, size_t n, uint32_t *__restrict__ hist,
 #pragma unroll
 		for (int u = 0; u < kUpsweepInFlight; ++u) {
 			const K *e = reinterpret_cast<const K *>(&v[u]);
+			if (kFast4 && base_shift == 0) {
 #pragma unroll
-			for (int p = 0; p < PASSES; ++p)
+				for (int q = 0; q < PER; ++q) count4((uint32_t)e[q]);
+			} else {
 #pragma unroll
-				for (int q = 0; q < PER; ++q) count(p, e[q]);
+				for (int p = 0; p < PASSES; ++p)
+#pragma unroll
+					for (int q = 0; q < PER; ++q) count(p, e[q]);
+			}
 		}
 	}
 	for (; i < nvec; i += stride) {
