@@ -27,12 +27,14 @@
 // over the whole buffer with a bitmap of segment heads; sums restart at
 // every head, a tile holding a head publishes its inclusive prefix at once.
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <type_traits>
 
 #include "clo_internal.h"
 #include "dev_common.cuh"
 #include "scan_status.cuh"
+#include "scan_tile.cuh"
 #include "timing.h"
 
 namespace clo {
@@ -868,21 +870,6 @@ cudaError_t seg_sort_typed(K *keys, uint64_t n_cap, const uint64_t *off, uint32_
 }
 
 // ------------------------------------------------------------ segmented scan
-constexpr int kSThreads = 256;
-constexpr int kSWarps = kSThreads / 32;
-constexpr int kSItems = 16;
-constexpr int kSWarpElems = 32 * kSItems;
-constexpr int kSTile = kSWarps * kSWarpElems;
-// A warp's elements in shared memory are padded by one element per 128
-// bytes (per 32 elements of 4 bytes or fewer, per 16 of 8 bytes), so the
-// lanes' 16-element runs and the 16-byte vector columns are conflict-free.
-template <typename T>
-__host__ __device__ constexpr int spad_shift() { return sizeof(T) == 8 ? 4 : 5; }
-template <typename T>
-__host__ __device__ constexpr int spadded() { return kSWarpElems + (kSWarpElems >> spad_shift<T>()); }
-template <typename T>
-__device__ __forceinline__ int pidx(int i) { return i + (i >> spad_shift<T>()); }
-
 // Head bitmap: bit i set when a segment starts at element i (and holds
 // elements).
 __global__ void __launch_bounds__(256) seg_heads(const uint64_t *off, uint32_t S,
@@ -899,183 +886,315 @@ __global__ void __launch_bounds__(256) seg_heads(const uint64_t *off, uint32_t S
 // Segmented exclusive scan: out[i] = sum of in[j] for j from the start of
 // i's segment to i - 1, for i in [off[0], off[S]); nothing else is written.
 // The combine of (head seen, sum) pairs is the usual segmented one: a
-// later head discards what came before it.
+// later head discards what came before it. Same tile layout and pipeline
+// as the plain scan (csrc/scan_tile.cuh): persistent CTAs take 8192-element
+// tiles in order; while warp 0 looks back, every warp prefetches the next
+// tile and its 32 head words, finds its last head (max-reduction) and sums
+// the elements from there on, so the next tile's (head seen, sum) is
+// published before this tile's outputs -- as an inclusive prefix at once
+// when it holds a head. A tile whose first element is a head needs no
+// carry and does not look back.
 template <typename InT, typename OutT>
-__global__ void __launch_bounds__(kSThreads, 4)
+__global__ void __launch_bounds__(scantile::kThreads, (scantile::scan_min_blocks<InT, OutT>()))
 seg_scan_lookback(const InT *__restrict__ in, OutT *__restrict__ out, uint64_t n,
 	const uint32_t *__restrict__ heads, const uint64_t *off, uint32_t S,
 	lb::TileStatus ts, int *dev_status, bool vec_ok) {
+	using namespace scantile;
 	using Acc = typename std::conditional<(sizeof(OutT) <= 4), uint32_t, uint64_t>::type;
 	constexpr int PT = lb::Slots<Acc>::kPerTile;
 	constexpr int KW = lb::Slots<Acc>::kWords;
-	// Inputs, then (once they are in registers) outputs, in one buffer.
-	constexpr int kBufBytes = spadded<InT>() * (int)sizeof(InT) > spadded<OutT>() * (int)sizeof(OutT)
-		? spadded<InT>() * (int)sizeof(InT) : spadded<OutT>() * (int)sizeof(OutT);
-	__shared__ __align__(16) unsigned char s_buf[kSWarps][kBufBytes];
-	__shared__ Acc s_wsum[kSWarps];
-	__shared__ uint32_t s_wflag[kSWarps];
+	extern __shared__ __align__(16) unsigned char s_dyn[];
+	__shared__ Acc s_wsum[kWarps], s_nsum[kWarps];
+	__shared__ uint32_t s_wflag[kWarps], s_nflag[kWarps];
 	__shared__ Acc s_excl;
-	__shared__ uint32_t s_tile;
+	__shared__ uint32_t s_tile, s_next;
 	__shared__ uint64_t s_lo, s_hi;
 
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const uint32_t num_tiles = (uint32_t)((n + kTile - 1) / kTile);
+	InT *s_in = reinterpret_cast<InT *>(s_dyn + (size_t)warp *
+		(kBlocks * padded<InT>() * sizeof(InT) + padded<OutT>() * sizeof(OutT)));
+	OutT *s_out = reinterpret_cast<OutT *>(s_in + kBlocks * padded<InT>());
+	auto full_tile = [&](uint32_t t) { return vec_ok && (uint64_t)(t + 1) * kTile <= n; };
 	if (tid == 0) {
 		s_tile = atomicAdd(ts.counter, 1u);
 		s_lo = off[0];
 		s_hi = off[S];
 	}
 	__syncthreads();
-	const uint32_t tile = s_tile;
+	uint32_t tile = s_tile;
 	const uint64_t lo = s_lo, hi = s_hi;
-	const uint64_t seg = (uint64_t)tile * kSTile + (uint64_t)warp * kSWarpElems;
-	const bool full = seg + kSWarpElems <= n;
-
-	InT *sin = reinterpret_cast<InT *>(s_buf[warp]);
-	if (full && vec_ok) {
-		constexpr int EPC = 16 / sizeof(InT);
-		constexpr int CHUNKS = kSWarpElems / EPC;
-		const uint4 *src = reinterpret_cast<const uint4 *>(in + seg);
+	if (tile >= num_tiles) return;
+	{
+		const uint64_t wseg = (uint64_t)tile * kTile + (uint64_t)warp * kWarpElems;
+		if (full_tile(tile)) {
+			BlockRegs<InT> r;
+			issue_loads<InT>(r, in, wseg, lane);
+			store_loads<InT>(r, s_in, lane);
+		} else {
 #pragma unroll
-		for (int c = lane; c < CHUNKS; c += 32) {
-			uint4 v = dev::ld_stream_v4(src + c);
-			const InT *e = reinterpret_cast<const InT *>(&v);
-#pragma unroll
-			for (int k = 0; k < EPC; ++k) sin[pidx<InT>(c * EPC + k)] = e[k];
+			for (int b = 0; b < kBlocks; ++b)
+				load_block_scalar<InT>(in, n, wseg + (uint64_t)b * kBlock, s_in + b * padded<InT>(), lane);
 		}
-	} else {
-		for (int i = lane; i < kSWarpElems; i += 32)
-			sin[pidx<InT>(i)] = (seg + i < n) ? in[seg + i] : (InT)0;
 	}
-	// This thread's 16 elements start at a multiple of 16: their head bits
-	// are one half of one bitmap word.
-	const uint64_t e0 = seg + (uint64_t)lane * kSItems;
-	const uint32_t hb = e0 < n ? (heads[e0 >> 5] >> (uint32_t)(e0 & 31)) & 0xffffu : 0u;
 	__syncwarp();
+	bool published = false;  // the current tile's status is already out
 
-	Acc x[kSItems];
-	Acc run = 0;
+	for (;;) {
+		if (tid == 0) s_next = atomicAdd(ts.counter, 1u);
+		const uint64_t wseg = (uint64_t)tile * kTile + (uint64_t)warp * kWarpElems;
+
+		// ---- per block: head bits, lane runs, warp segmented scan -------
+		uint32_t hb[kBlocks], fex[kBlocks], bf[kBlocks];
+		Acc ex[kBlocks], bs[kBlocks];
 #pragma unroll
-	for (int j = 0; j < kSItems; ++j) {
-		const Acc v = (Acc)(OutT)sin[pidx<InT>(lane * kSItems + j)];
-		if ((hb >> j) & 1u) run = 0;
-		x[j] = run;
-		run += v;
-	}
-	// Warp inclusive segmented scan of (has head, sum since last head).
-	Acc inc = run;
-	uint32_t finc = hb != 0;
+		for (int b = 0; b < kBlocks; ++b) {
+			const InT *sin = s_in + b * padded<InT>();
+			// 16 elements starting at a multiple of 16: one half of one word.
+			const uint64_t e0 = wseg + (uint64_t)b * kBlock + (uint64_t)lane * kItems;
+			hb[b] = e0 < n ? (heads[e0 >> 5] >> (uint32_t)(e0 & 31)) & 0xffffu : 0u;
+			Acc run = 0;
 #pragma unroll
-	for (int d = 1; d < 32; d <<= 1) {
-		const Acc t = __shfl_up_sync(0xffffffffu, inc, d);
-		const uint32_t tf = __shfl_up_sync(0xffffffffu, finc, d);
-		if (lane >= d) {
-			if (!finc) inc += t;
-			finc |= tf;
+			for (int j = 0; j < kItems; ++j) {
+				const Acc v = (Acc)(OutT)sin[pidx<InT>(lane * kItems + j)];
+				if ((hb[b] >> j) & 1u) run = 0;
+				run += v;
+			}
+			Acc inc = run;
+			uint32_t finc = hb[b] != 0;
+#pragma unroll
+			for (int d = 1; d < 32; d <<= 1) {
+				const Acc t = __shfl_up_sync(0xffffffffu, inc, d);
+				const uint32_t tf = __shfl_up_sync(0xffffffffu, finc, d);
+				if (lane >= d) {
+					if (!finc) inc += t;
+					finc |= tf;
+				}
+			}
+			ex[b] = __shfl_up_sync(0xffffffffu, inc, 1);
+			fex[b] = __shfl_up_sync(0xffffffffu, finc, 1);
+			if (lane == 0) {
+				ex[b] = 0;
+				fex[b] = 0;
+			}
+			bs[b] = __shfl_sync(0xffffffffu, inc, 31);
+			bf[b] = __shfl_sync(0xffffffffu, finc, 31);
 		}
-	}
-	Acc ex = __shfl_up_sync(0xffffffffu, inc, 1);
-	uint32_t fex = __shfl_up_sync(0xffffffffu, finc, 1);
-	if (lane == 0) {
-		ex = 0;
-		fex = 0;
-	}
-	if (lane == 31) {
-		s_wsum[warp] = inc;
-		s_wflag[warp] = finc;
-	}
-	__syncthreads();
-
-	if (warp == 0) {
-		const Acc wt = lane < kSWarps ? s_wsum[lane] : (Acc)0;
-		const uint32_t wf = lane < kSWarps ? s_wflag[lane] : 0u;
-		Acc winc = wt;
-		uint32_t wfinc = wf;
+		if (lane == 0) {
+			Acc ws = 0;
+			uint32_t wf = 0;
 #pragma unroll
-		for (int d = 1; d < kSWarps; d <<= 1) {
-			const Acc t = __shfl_up_sync(0xffffffffu, winc, d);
-			const uint32_t tf = __shfl_up_sync(0xffffffffu, wfinc, d);
-			if (lane >= d) {
-				if (!wfinc) winc += t;
-				wfinc |= tf;
+			for (int b = 0; b < kBlocks; ++b) {
+				ws = bf[b] ? bs[b] : ws + bs[b];
+				wf |= bf[b];
+			}
+			s_wsum[warp] = ws;
+			s_wflag[warp] = wf;
+		}
+		__syncthreads();
+		const uint32_t next = s_next;
+		const bool have_next = next < num_tiles;
+		const bool next_full = have_next && full_tile(next);
+		const uint64_t nseg = (uint64_t)next * kTile + (uint64_t)warp * kWarpElems;
+
+		// ---- prefetch of the next tile and its head words ----------------
+		BlockRegs<InT> r;
+		uint32_t nhw = 0;
+		if (next_full) {
+			issue_loads<InT>(r, in, nseg, lane);
+			nhw = heads[(nseg >> 5) + lane];
+		}
+
+		// ---- tile status, lookback (warp 0) ------------------------------
+		if (warp == 0) {
+			const Acc wt = lane < kWarps ? s_wsum[lane] : (Acc)0;
+			const uint32_t wf = lane < kWarps ? s_wflag[lane] : 0u;
+			Acc winc = wt;
+			uint32_t wfinc = wf;
+#pragma unroll
+			for (int d = 1; d < kWarps; d <<= 1) {
+				const Acc t = __shfl_up_sync(0xffffffffu, winc, d);
+				const uint32_t tf = __shfl_up_sync(0xffffffffu, wfinc, d);
+				if (lane >= d) {
+					if (!wfinc) winc += t;
+					wfinc |= tf;
+				}
+			}
+			const Acc agg = __shfl_sync(0xffffffffu, winc, kWarps - 1);
+			const uint32_t agg_f = __shfl_sync(0xffffffffu, wfinc, kWarps - 1);
+			Acc wex = __shfl_up_sync(0xffffffffu, winc, 1);
+			uint32_t wfex = __shfl_up_sync(0xffffffffu, wfinc, 1);
+			if (lane == 0) {
+				wex = 0;
+				wfex = 0;
+			}
+			uint64_t *tw = ts.words + (size_t)tile * PT;
+			// A tile holding a head knows its inclusive prefix at once.
+			if (lane == 0 && !published) {
+				if (agg_f || tile == 0) lb::publish<Acc>(tw + KW, agg);
+				else lb::publish<Acc>(tw, agg);
+			}
+			// The carry from earlier tiles matters only when the tile's
+			// first element is not a head.
+			const uint32_t first_head = __shfl_sync(0xffffffffu, hb[0], 0) & 1u;
+			Acc excl = 0;
+			if (tile > 0 && !first_head) excl = lb::lookback_warp<Acc>(ts.words, tile, dev_status);
+			if (lane == 0 && !agg_f && tile > 0) lb::publish<Acc>(tw + KW, excl + agg);
+			if (lane < kWarps) {
+				s_wsum[lane] = wex;
+				s_wflag[lane] = wfex;
+			}
+			if (lane == 0) s_excl = excl;
+		}
+		// ---- the next tile's (head seen, sum since its last head) --------
+		if (next_full) {
+			// Last head in the warp's 1024 elements, +1 (0: none).
+			const uint32_t mine = nhw ? (uint32_t)lane * 32u + 32u - (uint32_t)__clz(nhw) : 0u;
+			const uint32_t last1 = __reduce_max_sync(0xffffffffu, mine);
+			constexpr int EPC = BlockRegs<InT>::kEpc;
+			Acc part = 0;
+#pragma unroll
+			for (int b = 0; b < kBlocks; ++b)
+#pragma unroll
+				for (int k = 0; k < BlockRegs<InT>::kPerLane; ++k) {
+					const InT *e = reinterpret_cast<const InT *>(&r.v[b][k]);
+					const uint32_t i0 = (uint32_t)(b * kBlock + (lane + 32 * k) * EPC);
+#pragma unroll
+					for (int q = 0; q < EPC; ++q)
+						if (i0 + q + 1 >= last1) part += (Acc)(OutT)e[q];
+				}
+			part = lb::warp_sum<Acc>(part);
+			if (lane == 0) {
+				s_nsum[warp] = part;
+				s_nflag[warp] = last1 != 0;
 			}
 		}
-		const Acc agg = __shfl_sync(0xffffffffu, winc, kSWarps - 1);
-		const uint32_t agg_f = __shfl_sync(0xffffffffu, wfinc, kSWarps - 1);
-		Acc wex = __shfl_up_sync(0xffffffffu, winc, 1);
-		uint32_t wfex = __shfl_up_sync(0xffffffffu, wfinc, 1);
-		if (lane == 0) {
-			wex = 0;
-			wfex = 0;
+		__syncthreads();
+		if (next_full && tid == 0) {
+			Acc ns = 0;
+			uint32_t nf = 0;
+#pragma unroll
+			for (int w = 0; w < kWarps; ++w) {
+				ns = s_nflag[w] ? s_nsum[w] : ns + s_nsum[w];
+				nf |= s_nflag[w];
+			}
+			uint64_t *nw = ts.words + (size_t)next * PT;
+			if (nf) lb::publish<Acc>(nw + KW, ns);
+			else lb::publish<Acc>(nw, ns);
 		}
-		// A tile holding a head knows its inclusive prefix at once.
-		uint64_t *tw = ts.words + (size_t)tile * PT;
-		if (lane == 0) {
-			if (agg_f || tile == 0) lb::publish<Acc>(tw + KW, agg);
-			else lb::publish<Acc>(tw, agg);
-		}
-		// The carry from earlier tiles matters only when the tile's first
-		// element is not a head.
-		const uint32_t first_head = __shfl_sync(0xffffffffu, hb, 0) & 1u;
-		Acc excl = 0;
-		if (tile > 0 && !first_head) excl = lb::lookback_warp<Acc>(ts.words, tile, dev_status);
-		if (lane == 0 && !agg_f && tile > 0) lb::publish<Acc>(tw + KW, excl + agg);
-		if (lane < kSWarps) {
-			s_wsum[lane] = wex;
-			s_wflag[lane] = wfex;
-		}
-		if (lane == 0) s_excl = excl;
-	}
-	__syncthreads();
 
-	const Acc wcarry = s_wsum[warp] + (s_wflag[warp] ? (Acc)0 : s_excl);
-	const Acc tcarry = ex + (fex ? (Acc)0 : wcarry);
-	const int fh = hb ? __ffs(hb) - 1 : kSItems;
-	OutT *sout = reinterpret_cast<OutT *>(s_buf[warp]);
+		// ---- outputs per block: second read, staged, coalesced stores ----
+		Acc carry = s_wsum[warp] + (s_wflag[warp] ? (Acc)0 : s_excl);
 #pragma unroll
-	for (int j = 0; j < kSItems; ++j)
-		sout[pidx<OutT>(lane * kSItems + j)] = (OutT)(x[j] + (j < fh ? tcarry : (Acc)0));
-	__syncwarp();
-	if (full && vec_ok && seg >= lo && seg + kSWarpElems <= hi) {
-		constexpr int EPC = 16 / sizeof(OutT);
-		constexpr int CHUNKS = kSWarpElems / EPC;
-		uint4 *dst = reinterpret_cast<uint4 *>(out + seg);
+		for (int b = 0; b < kBlocks; ++b) {
+			const InT *sin = s_in + b * padded<InT>();
+			Acc run = ex[b] + (fex[b] ? (Acc)0 : carry);
 #pragma unroll
-		for (int c = lane; c < CHUNKS; c += 32) {
-			uint4 v;
-			OutT *e = reinterpret_cast<OutT *>(&v);
+			for (int j = 0; j < kItems; ++j) {
+				const int q = lane * kItems + j;
+				const Acc v = (Acc)(OutT)sin[pidx<InT>(q)];
+				if ((hb[b] >> j) & 1u) run = 0;
+				s_out[pidx<OutT>(q)] = (OutT)run;
+				run += v;
+			}
+			carry = bf[b] ? bs[b] : bs[b] + carry;
+			__syncwarp();
+			const uint64_t seg = wseg + (uint64_t)b * kBlock;
+			if (vec_ok && seg >= lo && seg + kBlock <= hi && seg + kBlock <= n) {
+				constexpr int EPC = 16 / sizeof(OutT);
+				constexpr int CHUNKS = kBlock / EPC;
+				uint4 *dst = reinterpret_cast<uint4 *>(out + seg);
 #pragma unroll
-			for (int k = 0; k < EPC; ++k) e[k] = sout[pidx<OutT>(c * EPC + k)];
-			dev::st_stream_v4(dst + c, v);
+				for (int c = lane; c < CHUNKS; c += 32) {
+					uint4 v;
+					OutT *e = reinterpret_cast<OutT *>(&v);
+#pragma unroll
+					for (int k = 0; k < EPC; ++k) e[k] = s_out[pidx<OutT>(c * EPC + k)];
+					dev::st_stream_v4(dst + c, v);
+				}
+			} else {
+				for (int i = lane; i < kBlock; i += 32) {
+					const uint64_t g = seg + i;
+					if (g < n && g >= lo && g < hi) out[g] = s_out[pidx<OutT>(i)];
+				}
+			}
+			__syncwarp();
 		}
-	} else {
-		for (int i = lane; i < kSWarpElems; i += 32) {
-			const uint64_t g = seg + i;
-			if (g < n && g >= lo && g < hi) out[g] = sout[pidx<OutT>(i)];
+		if (!have_next) break;
+
+		// ---- the next tile into shared memory ----------------------------
+		if (next_full) {
+			store_loads<InT>(r, s_in, lane);
+		} else {
+#pragma unroll
+			for (int b = 0; b < kBlocks; ++b)
+				load_block_scalar<InT>(in, n, nseg + (uint64_t)b * kBlock, s_in + b * padded<InT>(), lane);
+		}
+		__syncwarp();
+		published = next_full;
+		tile = next;
+	}
+}
+
+// Per device and type pair, once: the kernel's dynamic shared memory and
+// its resident CTAs per SM (later calls, possibly during a graph capture,
+// only read the cache).
+template <typename InT, typename OutT>
+cudaError_t seg_scan_prepare(int *per_sm) {
+	static std::atomic<int> cached[64];
+	static std::mutex mu;
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess) return e;
+	if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+	int v = cached[dev].load(std::memory_order_acquire);
+	if (v == 0) {
+		std::lock_guard<std::mutex> lk(mu);
+		v = cached[dev].load(std::memory_order_relaxed);
+		if (v == 0) {
+			constexpr size_t smem = scantile::scan_smem<InT, OutT>();
+			e = cudaFuncSetAttribute(seg_scan_lookback<InT, OutT>,
+				cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+			if (e == cudaSuccess)
+				e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, seg_scan_lookback<InT, OutT>,
+					scantile::kThreads, smem);
+			if (e != cudaSuccess) return e;
+			if (v < 1) v = 1;
+			cached[dev].store(v, std::memory_order_release);
 		}
 	}
+	*per_sm = v;
+	return cudaSuccess;
 }
 
 template <typename InT, typename OutT>
 cudaError_t launch_seg_scan(const void *in, void *out, uint64_t n_cap,
 	const uint64_t *off, uint32_t S, CCLContext *ctx, cudaStream_t s, GError **err) {
 	using Acc = typename std::conditional<(sizeof(OutT) <= 4), uint32_t, uint64_t>::type;
-	const uint64_t tiles = (n_cap + kSTile - 1) / kSTile;
+	const uint64_t tiles = (n_cap + scantile::kTile - 1) / scantile::kTile;
 	if (tiles >= (1ull << 31)) {
 		set_error(err, CLO_ERROR_ARGS, "Segmented scan buffer of %llu elements is too large",
 			(unsigned long long)n_cap);
 		return cudaErrorInvalidValue;
 	}
+	// One bitmap word per 32 elements, plus one word of slack.
 	const size_t words = (size_t)((n_cap + 31) / 32) + 1;
 	const size_t bm_bytes = (words * 4 + 15) / 16 * 16;
 	const size_t st_bytes = (size_t)tiles * lb::Slots<Acc>::kPerTile * 8;
 	const size_t total = bm_bytes + st_bytes + 16;
+	int per_sm = 1;
+	cudaError_t e = seg_scan_prepare<InT, OutT>(&per_sm);
+	if (e != cudaSuccess) {
+		cuda_ok(e, err, "segmented scan");
+		return e;
+	}
 	char *tmp = (char *)tmp_alloc(ctx, total, s, err);
 	if (!tmp) return cudaErrorMemoryAllocation;
 	uint32_t *bits = (uint32_t *)tmp;
 	lb::TileStatus ts;
 	ts.words = (uint64_t *)(tmp + bm_bytes);
 	ts.counter = (uint32_t *)(tmp + bm_bytes + st_bytes);
-	cudaError_t e = cudaMemsetAsync(tmp, 0, total, s);
+	e = cudaMemsetAsync(tmp, 0, total, s);
 	if (e == cudaSuccess) {
 		const uint32_t grid = (uint32_t)std::min<uint64_t>(((uint64_t)S + 255) / 256,
 			(uint64_t)ctx->sm_count * 8);
@@ -1085,8 +1204,10 @@ cudaError_t launch_seg_scan(const void *in, void *out, uint64_t n_cap,
 	}
 	const bool vec_ok = ((uintptr_t)in % 16 == 0) && ((uintptr_t)out % 16 == 0);
 	if (e == cudaSuccess) {
+		const unsigned grid = (unsigned)std::max<uint64_t>(1,
+			std::min<uint64_t>(tiles, (uint64_t)per_sm * ctx->sm_count));
 		KernelTimer t("seg_scan_lookback", s, (double)n_cap * (sizeof(InT) + sizeof(OutT)));
-		seg_scan_lookback<InT, OutT><<<(unsigned)tiles, kSThreads, 0, s>>>(
+		seg_scan_lookback<InT, OutT><<<grid, scantile::kThreads, scantile::scan_smem<InT, OutT>(), s>>>(
 			(const InT *)in, (OutT *)out, n_cap, bits, off, S, ts, ctx->d_status, vec_ok);
 		t.stop();
 		e = cudaGetLastError();

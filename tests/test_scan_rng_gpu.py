@@ -37,11 +37,24 @@ def test_scan_types(clops, ctx, queue, code, dt, ocode, odt):
                                   oracle.scan(a, code, odt))
 
 
-@pytest.mark.parametrize("n", [0, 1, 2, 511, 512, 513, 4095, 4096, 4097, 131072, 1000003])
+@pytest.mark.parametrize("n", [0, 1, 2, 511, 512, 513, 4095, 4096, 4097, 8191, 8192, 8193,
+                               16385, 131072, 1000003, 5000011])
 def test_scan_sizes_uint_to_ulong(clops, ctx, queue, n):
     a = (splitmix64(45, n) >> np.uint64(56)).astype(np.uint32)  # values in [0, 255]
     np.testing.assert_array_equal(_scan(clops, ctx, queue, a, 5, 7, np.uint64),
                                   oracle.scan(a, 5, np.uint64))
+
+
+@pytest.mark.parametrize("code,dt,ocode,odt", [(1, np.uint8, 1, np.uint8), (0, np.int8, 4, np.int32),
+                                               (3, np.uint16, 7, np.uint64), (4, np.int32, 4, np.int32),
+                                               (7, np.uint64, 7, np.uint64), (6, np.int64, 2, np.int16)])
+def test_scan_many_tiles_per_cta(clops, ctx, queue, code, dt, ocode, odt):
+    # More tiles than resident CTAs: CTAs take second and later tiles, whose
+    # loads are prefetched and aggregates published during the lookback.
+    n = (1 << 22) + 3
+    a = keys_of_type(77 + code, n, dt)
+    np.testing.assert_array_equal(_scan(clops, ctx, queue, a, code, ocode, odt),
+                                  oracle.scan(a, code, odt))
 
 
 def test_scan_host_data_and_unaligned_views(clops, ctx, queue):
