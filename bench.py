@@ -500,9 +500,12 @@ def run_suite(clops, ctx, q, args, only=None):
     def serve():
         """Open-loop serving: Poisson arrivals at 20k requests/s (seed 49),
         60 % sort / 30 % scan / 10 % random fill, n log-uniform in
-        [2^10, 2^26], uint / ulong 50/50, 120 GB admission budget; host
-        data in page-locked pools (requests read and write slices of them).
-        Against the same requests served by serial plain host-data calls."""
+        [2^10, 2^26], uint / ulong 50/50, 120 GB admission budget. Primary:
+        device-resident buffers (requests read slices of a 4 GiB device pool
+        and write their own slices of a 48 GiB device output ring), against
+        the same requests as serial plain device-data calls. Secondary: the
+        same requests on host buffers (page-locked pools), against serial
+        plain host-data calls."""
         dur = args.serve_seconds
         rate = 20000.0
         u = splitmix64(49, 1 << 22)
@@ -518,95 +521,173 @@ def run_suite(clops, ctx, q, args, only=None):
         wide = (u[3::8][:count] & np.uint64(1)).astype(bool)
         pos_in = u[4::8][:count]
         pos_out = u[5::8][:count]
-        pool_bytes = 4 << 30
-        hin = clops.lib.clo_host_alloc(pool_bytes, None)
-        hout = clops.lib.clo_host_alloc(pool_bytes, None)
-        pin = np.ctypeslib.as_array((clops.C.c_uint8 * pool_bytes).from_address(hin))
-        block = splitmix64(149, 1 << 26).view(np.uint8)  # 512 MiB, repeated
-        for o in range(0, pool_bytes, block.size):
-            pin[o:o + block.size] = block
-        reqs = []
-        elems = 0.0
+        # (op, type / generator, sum type, n or states, draws, in bytes, out bytes)
+        specs, elems = [], 0.0
         for i in range(count):
             n = int(nreq[i])
             if kind[i] < 6:
                 code, eb = (clops.CLO_ULONG, 8) if wide[i] else (clops.CLO_UINT, 4)
-                ib, ob, op, sc_code, st, dr = eb, eb, clops.SERVE_SORT, 0, n, 0
+                specs.append((clops.SERVE_SORT, code, 0, n, 0, n * eb, n * eb))
+                elems += n
             elif kind[i] < 9:
                 code, eb = (clops.CLO_ULONG, 8) if wide[i] else (clops.CLO_UINT, 4)
-                ib, ob, op, sc_code, st, dr = eb, 8, clops.SERVE_SCAN, clops.CLO_ULONG, n, 0
-            else:
-                g = i % 5
-                st, dr = max(1, n // 16), 16
-                ib, ob = clops.RNG_SEED_SIZE[clops.RNG_NAMES[g]], 4 * dr
-                code, op, sc_code = g, clops.SERVE_RNG_FILL, 0
-            span_in, span_out = st * ib, st * ob
-            a = hin + int(pos_in[i] % np.uint64((pool_bytes - span_in) // 16)) * 16
-            b = hout + int(pos_out[i] % np.uint64((pool_bytes - span_out) // 16)) * 16
-            if op == clops.SERVE_RNG_FILL:
-                reqs.append(clops.Server.request(op, 0, 0, st, dr, code, inp=a, out=b))
-                elems += st * dr
-            else:
-                reqs.append(clops.Server.request(op, code, sc_code, n, inp=a, out=b))
+                specs.append((clops.SERVE_SCAN, code, clops.CLO_ULONG, n, 0, n * eb, n * 8))
                 elems += n
-        srv = clops.Server(ctx, 120 << 30, streams=4)
-        # warm-up: a few requests of each kind
-        for r in reqs[:64]:
-            srv.submit(r)
-        srv.drain()
-        srv.reset_stats()
-        srv.replay(reqs, list(arrivals))
-        srv.drain()
-        st_ = srv.stats()
-        srv.destroy()
-        # Serial plain calls on the first requests (about 2 s of work).
+            else:
+                g, st, dr = i % 5, max(1, n // 16), 16
+                specs.append((clops.SERVE_RNG_FILL, g, 0, st, dr,
+                              st * clops.RNG_SEED_SIZE[clops.RNG_NAMES[g]], st * dr * 4))
+                elems += st * dr
+        block = splitmix64(149, 1 << 26).view(np.uint8)  # 512 MiB of random bytes
+
+        def make(pool_in, pool_bytes, out_addr, device):
+            reqs = []
+            for i, (op, code, sc, n, dr, span_in, span_out) in enumerate(specs):
+                a = pool_in + int(pos_in[i] % np.uint64((pool_bytes - span_in) // 16)) * 16
+                bo = out_addr(i, span_out)
+                if op == clops.SERVE_RNG_FILL:
+                    reqs.append(clops.Server.request(op, 0, 0, n, dr, code, inp=a, out=bo,
+                                                     device=device))
+                else:
+                    reqs.append(clops.Server.request(op, code, sc, n, inp=a, out=bo,
+                                                     device=device))
+            return reqs
+
+        def served(reqs):
+            srv = clops.Server(ctx, 120 << 30, streams=4)
+            for r in reqs[:64]:  # warm-up: a few requests of each kind
+                srv.submit(r)
+            srv.drain()
+            srv.reset_stats()
+            srv.replay(reqs, list(arrivals))
+            srv.drain()
+            st_ = srv.stats()
+            srv.destroy()
+            return st_
+
         sorters = {clops.CLO_UINT: clops.Sorter(ctx, "satradix", clops.CLO_UINT),
                    clops.CLO_ULONG: clops.Sorter(ctx, "satradix", clops.CLO_ULONG)}
         scanners = {clops.CLO_UINT: clops.Scanner(ctx, clops.CLO_UINT, clops.CLO_ULONG),
                     clops.CLO_ULONG: clops.Scanner(ctx, clops.CLO_ULONG, clops.CLO_ULONG)}
-        done_el, t0 = 0.0, time.perf_counter()
-        for r in reqs:
-            if r.op == clops.SERVE_SORT:
-                clops.call(clops.lib.clo_sort_with_host_data, sorters[r.type].h, q.h, None,
-                           r.in_, r.out, r.n, 0)
-                done_el += r.n
-            elif r.op == clops.SERVE_SCAN:
-                clops.call(clops.lib.clo_scan_with_host_data, scanners[r.type].h, q.h, None,
-                           r.in_, r.out, r.n, 0)
-                done_el += r.n
-            else:
-                name = clops.RNG_NAMES[r.rng]
-                seeds = np.ctypeslib.as_array((clops.C.c_uint8 * (r.n * clops.RNG_SEED_SIZE[name]))
-                                              .from_address(r.in_))
-                rng = clops.Rng(ctx, q, name, clops.CLO_RNG_SEED_EXT_HOST, r.n, seeds=seeds)
-                ob_ = clops.Buffer(ctx, r.n * r.draws * 4)
-                clops.wait(rng.fill(q, ob_, r.draws))
-                clops.call(clops.lib.ccl_buffer_enqueue_read, ob_.h, q.h, 1, 0,
-                           r.n * r.draws * 4, r.out, None)
-                ob_.destroy()
-                rng.destroy()
-                done_el += r.n * r.draws
-            if time.perf_counter() - t0 > 2.0:
-                break
-        serial = done_el / (time.perf_counter() - t0)
+
+        class Wrapped:
+            def __init__(self, addr, nbytes):
+                self.h = clops.call(clops.lib.ccl_buffer_new_wrap, ctx.h, clops.C.c_void_p(addr),
+                                    nbytes)
+
+            def destroy(self):
+                clops.lib.ccl_buffer_destroy(self.h)
+
+        def serial_device(reqs):
+            """The requests one at a time as plain device-data calls (about
+            2 s of work)."""
+            done_el, t0 = 0.0, time.perf_counter()
+            for r, sp in zip(reqs, specs):
+                bi, bo_ = Wrapped(r.in_, max(sp[5], 1)), Wrapped(r.out, max(sp[6], 1))
+                if r.op == clops.SERVE_SORT:
+                    clops.wait(clops.call(clops.lib.clo_sort_with_device_data, sorters[r.type].h,
+                                          q.h, None, bi.h, bo_.h, r.n, 0))
+                    done_el += r.n
+                elif r.op == clops.SERVE_SCAN:
+                    clops.wait(clops.call(clops.lib.clo_scan_with_device_data, scanners[r.type].h,
+                                          q.h, None, bi.h, bo_.h, r.n, 0))
+                    done_el += r.n
+                else:
+                    rng = clops.Rng(ctx, q, clops.RNG_NAMES[r.rng], clops.CLO_RNG_SEED_EXT_DEV,
+                                    r.n, seeds=bi)
+                    clops.wait(rng.fill(q, bo_, r.draws))
+                    rng.destroy()
+                    done_el += r.n * r.draws
+                bi.destroy()
+                bo_.destroy()
+                if time.perf_counter() - t0 > 2.0:
+                    break
+            return done_el / (time.perf_counter() - t0)
+
+        def serial_host(reqs):
+            """The requests one at a time as plain host-data calls (about 2 s
+            of work)."""
+            done_el, t0 = 0.0, time.perf_counter()
+            for r in reqs:
+                if r.op == clops.SERVE_SORT:
+                    clops.call(clops.lib.clo_sort_with_host_data, sorters[r.type].h, q.h, None,
+                               r.in_, r.out, r.n, 0)
+                    done_el += r.n
+                elif r.op == clops.SERVE_SCAN:
+                    clops.call(clops.lib.clo_scan_with_host_data, scanners[r.type].h, q.h, None,
+                               r.in_, r.out, r.n, 0)
+                    done_el += r.n
+                else:
+                    name = clops.RNG_NAMES[r.rng]
+                    seeds = np.ctypeslib.as_array(
+                        (clops.C.c_uint8 * (r.n * clops.RNG_SEED_SIZE[name])).from_address(r.in_))
+                    rng = clops.Rng(ctx, q, name, clops.CLO_RNG_SEED_EXT_HOST, r.n, seeds=seeds)
+                    ob_ = clops.Buffer(ctx, r.n * r.draws * 4)
+                    clops.wait(rng.fill(q, ob_, r.draws))
+                    clops.call(clops.lib.ccl_buffer_enqueue_read, ob_.h, q.h, 1, 0,
+                               r.n * r.draws * 4, r.out, None)
+                    ob_.destroy()
+                    rng.destroy()
+                    done_el += r.n * r.draws
+                if time.perf_counter() - t0 > 2.0:
+                    break
+            return done_el / (time.perf_counter() - t0)
+
+        def report(st_, serial, buffers):
+            agg = st_["elements"] / st_["span_s"] if st_["span_s"] else 0.0
+            return {
+                "buffers": buffers, "open_loop_s": dur, "offered_req_per_s": rate,
+                "requests": count, "offered_Gelem_per_s": round(elems / dur / 1e9, 2),
+                "submitted": st_["submitted"], "admitted": st_["admitted"],
+                "completed": st_["completed"], "rejected": st_["rejected"],
+                "batches": st_["batches"], "max_queued": st_["max_queued"],
+                "peak_budget_GB": round(st_["peak_bytes"] / 1e9, 2),
+                "budget_GB": 120 * 1.073741824,
+                "p50_ms": round(st_["p50_ms"], 2), "p99_ms": round(st_["p99_ms"], 2),
+                "mean_ms": round(st_["mean_ms"], 2), "span_s": round(st_["span_s"], 3),
+                "aggregate_Gelem_per_s": round(agg / 1e9, 3),
+                "serial_plain_Gelem_per_s": round(serial / 1e9, 3),
+                "speedup_vs_serial_plain": round(agg / serial, 2) if serial else None}
+
+        # Device-resident buffers.
+        dpool = 4 << 30
+        din = clops.Buffer(ctx, dpool)
+        for o in range(0, dpool, block.size):
+            clops.call(clops.lib.ccl_buffer_enqueue_write, din.h, q.h, 1, o, block.size,
+                       clops.np_ptr(block), None)
+        ring = 48 << 30
+        dout = clops.Buffer(ctx, ring)
+        cursor = [0]
+
+        def ring_slot(i, span):
+            span = (span + 255) // 256 * 256
+            if cursor[0] + span > ring:
+                cursor[0] = 0
+            at = dout.ptr + cursor[0]
+            cursor[0] += span
+            return at
+        dreqs = make(din.ptr, dpool, ring_slot, True)
+        dev_res = report(served(dreqs), serial_device(dreqs), "device-resident")
+        din.destroy()
+        dout.destroy()
+
+        # Host buffers (page-locked pools; outputs at random slices).
+        pool_bytes = 4 << 30
+        hin = clops.lib.clo_host_alloc(pool_bytes, None)
+        hout = clops.lib.clo_host_alloc(pool_bytes, None)
+        pin = np.ctypeslib.as_array((clops.C.c_uint8 * pool_bytes).from_address(hin))
+        for o in range(0, pool_bytes, block.size):
+            pin[o:o + block.size] = block
+        hreqs = make(hin, pool_bytes, lambda i, span: hout + int(
+            pos_out[i] % np.uint64((pool_bytes - span) // 16)) * 16, False)
+        host_res = report(served(hreqs), serial_host(hreqs), "host (page-locked)")
         for x in list(sorters.values()) + list(scanners.values()):
             x.destroy()
         del pin
         clops.lib.clo_host_free(hin)
         clops.lib.clo_host_free(hout)
-        agg = st_["elements"] / st_["span_s"] if st_["span_s"] else 0.0
-        res["serve_poisson_20k"] = {
-            "open_loop_s": dur, "offered_req_per_s": rate, "requests": count,
-            "offered_Gelem_per_s": round(elems / dur / 1e9, 2),
-            "submitted": st_["submitted"], "admitted": st_["admitted"],
-            "completed": st_["completed"], "rejected": st_["rejected"],
-            "batches": st_["batches"], "max_queued": st_["max_queued"],
-            "peak_budget_GB": round(st_["peak_bytes"] / 1e9, 2), "budget_GB": 120 * 1.073741824,
-            "p50_ms": round(st_["p50_ms"], 2), "p99_ms": round(st_["p99_ms"], 2),
-            "mean_ms": round(st_["mean_ms"], 2), "span_s": round(st_["span_s"], 3),
-            "aggregate_Gelem_per_s": round(agg / 1e9, 3),
-            "serial_plain_Gelem_per_s": round(serial / 1e9, 3),
-            "speedup_vs_serial_plain": round(agg / serial, 2) if serial else None}
+        res["serve_poisson_20k"] = dev_res
+        res["serve_poisson_20k_host_buffers"] = host_res
 
     def c1_c3():
         """C1: 2^20 uint32 keys with the reference's radix=16 option

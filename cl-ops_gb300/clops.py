@@ -58,7 +58,7 @@ class ServeRequest(C.Structure):
     """CloServeRequest (include/clo_serve.h)."""
     _fields_ = [("op", C.c_int), ("type", C.c_int), ("sum_type", C.c_int),
                 ("n", C.c_size_t), ("draws", C.c_size_t), ("rng", C.c_int),
-                ("in_", C.c_void_p), ("out", C.c_void_p)]
+                ("in_", C.c_void_p), ("out", C.c_void_p), ("device_data", C.c_uint32)]
 
 
 class ServeStats(C.Structure):
@@ -511,13 +511,16 @@ class Server:
         self.h = call(lib.clo_serve_new, ctx.h, budget_bytes, streams)
 
     @staticmethod
-    def request(op, type_=0, sum_type=0, n=0, draws=0, rng=0, inp=None, out=None):
-        """inp / out: numpy arrays or raw addresses."""
+    def request(op, type_=0, sum_type=0, n=0, draws=0, rng=0, inp=None, out=None,
+                device=False):
+        """inp / out: numpy arrays or raw addresses (host memory), or, with
+        device=True, device addresses on the server's GPU (Buffer.ptr)."""
         def addr(x):
             if x is None:
                 return None
             return x.ctypes.data if isinstance(x, np.ndarray) else int(x)
-        return ServeRequest(op, type_, sum_type, n, draws, rng, addr(inp), addr(out))
+        return ServeRequest(op, type_, sum_type, n, draws, rng, addr(inp), addr(out),
+                            1 if device else 0)
 
     def submit(self, req):
         return call(lib.clo_serve_submit, self.h, C.byref(req))

@@ -179,6 +179,15 @@ cudaError_t seg_scan(const void *in, void *out, uint64_t n_cap, const uint64_t *
 
 // Host check of segment offsets (non-decreasing, within numel, segments
 // shorter than 2^30): CLO_ERROR_ARGS otherwise.
+// Copies k device segments into one buffer and back: segment i holds
+// off[i + 1] - off[i] elements of elem_bytes bytes at srcs[i] (gather) or
+// dsts[i] (scatter), and at element off[i] of the contiguous buffer. srcs,
+// dsts and off are device arrays.
+cudaError_t seg_gather(void *dst, const void *const *srcs, const uint64_t *off, uint32_t k,
+	uint64_t total, int elem_bytes, int sm_count, cudaStream_t s);
+cudaError_t seg_scatter(void *const *dsts, const void *src, const uint64_t *off, uint32_t k,
+	uint64_t total, int elem_bytes, int sm_count, cudaStream_t s);
+
 bool check_offsets(const uint64_t *off, size_t S, size_t numel, GError **err);
 
 // Generator ids (index into clo_rng_infos).

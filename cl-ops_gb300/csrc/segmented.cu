@@ -1231,6 +1231,60 @@ cudaError_t seg_scan_out(const void *in, void *out, uint64_t n_cap, const uint64
 	return cudaErrorInvalidValue;
 }
 
+// ------------------------------------------------ gather / scatter
+// Thread t of the grid handles 16 consecutive elements of the contiguous
+// buffer: one binary search for the segment of the first, then forward.
+constexpr int kGatherRun = 16;
+
+__device__ __forceinline__ uint32_t segment_of(const uint64_t *off, uint32_t k, uint64_t g) {
+	// Largest i with off[i] <= g (off[0] = 0 <= g < off[k]).
+	uint32_t lo = 0, hi = k;
+	while (hi - lo > 1) {
+		const uint32_t mid = (lo + hi) >> 1;
+		if (off[mid] <= g) lo = mid;
+		else hi = mid;
+	}
+	return lo;
+}
+
+template <typename T, bool GATHER>
+__global__ void __launch_bounds__(256) seg_move(T *flat, T *const *ptrs, const uint64_t *off,
+	uint32_t k, uint64_t total) {
+	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * kGatherRun;
+	for (uint64_t g0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) * kGatherRun;
+		 g0 < total; g0 += stride) {
+		uint32_t i = segment_of(off, k, g0);
+		uint64_t next = off[i + 1];
+#pragma unroll 4
+		for (int e = 0; e < kGatherRun; ++e) {
+			const uint64_t g = g0 + e;
+			if (g >= total) break;
+			while (next <= g) next = off[++i + 1];
+			T *p = ptrs[i] + (g - off[i]);
+			if (GATHER) flat[g] = *p;
+			else *p = flat[g];
+		}
+	}
+}
+
+template <bool GATHER>
+cudaError_t seg_move_launch(void *flat, void *const *ptrs, const uint64_t *off, uint32_t k,
+	uint64_t total, int eb, int sm_count, cudaStream_t s) {
+	if (total == 0 || k == 0) return cudaSuccess;
+	const uint64_t threads = (total + kGatherRun - 1) / kGatherRun;
+	const unsigned grid = (unsigned)std::max<uint64_t>(1,
+		std::min<uint64_t>((threads + 255) / 256, (uint64_t)sm_count * 16));
+	switch (eb) {
+	case 1: seg_move<uint8_t, GATHER><<<grid, 256, 0, s>>>((uint8_t *)flat, (uint8_t *const *)ptrs, off, k, total); break;
+	case 2: seg_move<uint16_t, GATHER><<<grid, 256, 0, s>>>((uint16_t *)flat, (uint16_t *const *)ptrs, off, k, total); break;
+	case 4: seg_move<uint32_t, GATHER><<<grid, 256, 0, s>>>((uint32_t *)flat, (uint32_t *const *)ptrs, off, k, total); break;
+	case 8: seg_move<uint64_t, GATHER><<<grid, 256, 0, s>>>((uint64_t *)flat, (uint64_t *const *)ptrs, off, k, total); break;
+	default: return cudaErrorInvalidValue;
+	}
+	count_launches(1);
+	return cudaGetLastError();
+}
+
 }  // namespace
 
 int seg_sort_num_variants() { return kNumVariants; }
@@ -1275,6 +1329,19 @@ cudaError_t seg_scan(const void *in, void *out, uint64_t n_cap, const uint64_t *
 	}
 	set_error(err, CLO_ERROR_ARGS, "Unsupported scan element type %d", (int)in_type);
 	return cudaErrorInvalidValue;
+}
+
+
+cudaError_t seg_gather(void *dst, const void *const *srcs, const uint64_t *off, uint32_t k,
+	uint64_t total, int elem_bytes, int sm_count, cudaStream_t s) {
+	return seg_move_launch<true>(dst, const_cast<void *const *>(srcs), off, k, total,
+		elem_bytes, sm_count, s);
+}
+
+cudaError_t seg_scatter(void *const *dsts, const void *src, const uint64_t *off, uint32_t k,
+	uint64_t total, int elem_bytes, int sm_count, cudaStream_t s) {
+	return seg_move_launch<false>(const_cast<void *>(src), dsts, off, k, total, elem_bytes,
+		sm_count, s);
 }
 
 }  // namespace clo

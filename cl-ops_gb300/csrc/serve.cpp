@@ -68,9 +68,14 @@ struct Batch {
 	std::vector<Item *> items;
 	size_t bytes = 0;
 	cudaEvent_t ev = nullptr;
-	uint64_t *h_off = nullptr;  // pinned offsets of a segmented call
+	// Pinned: kMaxBatch + 1 offsets of a segmented call, then (device-
+	// resident batches) kMaxBatch input and kMaxBatch output pointers.
+	uint64_t *h_off = nullptr;
 	bool failed = false;
 };
+
+// Pinned words per batch buffer (offsets, input and output pointers).
+constexpr size_t kPinnedWords = 3 * kMaxBatch + 1;
 
 struct Lane {
 	cudaStream_t stream = nullptr;
@@ -113,25 +118,46 @@ size_t elem_bytes(CloType t) { return clo_type_sizeof(t); }
 void launch_batch(clo_server *srv, Batch *b, Lane *lane) {
 	cudaStream_t s = lane->stream;
 	const CloServeRequest &r0 = b->items[0]->r;
+	const bool dev_data = r0.device_data != CL_FALSE;
+	const cudaMemcpyKind h2d = dev_data ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+	const cudaMemcpyKind d2h = dev_data ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
 	GError *err = nullptr;
 	cudaError_t e = cudaSuccess;
 	const size_t k = b->items.size();
 	size_t total = 0;
 	for (Item *it : b->items) total += it->r.n;
 	if (r0.op == CLO_SERVE_RNG_FILL) {
+		// The states are copied (the request's input is only read); the
+		// draws go straight to a device-resident output.
 		const size_t ss = clo_rng_infos[r0.rng].seed_size;
-		char *dev = (char *)clo::tmp_alloc(srv->ctx, r0.n * ss + r0.n * r0.draws * 4 + 256, s, &err);
+		const size_t draw_bytes = dev_data ? 0 : r0.n * r0.draws * 4;
+		char *dev = (char *)clo::tmp_alloc(srv->ctx, r0.n * ss + draw_bytes + 256, s, &err);
 		if (!dev) {
 			b->failed = true;
 		} else {
 			char *states = dev;
-			uint32_t *out = (uint32_t *)(dev + (r0.n * ss + 255) / 256 * 256);
-			e = cudaMemcpyAsync(states, r0.in, r0.n * ss, cudaMemcpyHostToDevice, s);
+			uint32_t *out = dev_data ? (uint32_t *)r0.out
+				: (uint32_t *)(dev + (r0.n * ss + 255) / 256 * 256);
+			e = cudaMemcpyAsync(states, r0.in, r0.n * ss, h2d, s);
 			if (e == cudaSuccess)
 				e = clo::rng_fill(states, r0.n, r0.rng, out, r0.draws, 32, 0, s);
-			if (e == cudaSuccess)
-				e = cudaMemcpyAsync(r0.out, out, r0.n * r0.draws * 4, cudaMemcpyDeviceToHost, s);
+			if (e == cudaSuccess && !dev_data)
+				e = cudaMemcpyAsync(r0.out, out, r0.n * r0.draws * 4, d2h, s);
 			clo::tmp_free(dev, s);
+		}
+	} else if (dev_data && k == 1) {
+		// One device-resident request: the plain kernels on its buffers
+		// (a sort copies its input to the output and sorts there).
+		const size_t ib = elem_bytes(r0.type);
+		const size_t ob = r0.op == CLO_SERVE_SCAN ? elem_bytes(r0.sum_type) : ib;
+		if (r0.n && r0.op == CLO_SERVE_SORT) {
+			if (r0.out != r0.in)
+				e = cudaMemcpyAsync(r0.out, r0.in, r0.n * ib, cudaMemcpyDeviceToDevice, s);
+			if (e == cudaSuccess)
+				e = clo::radix_sort(r0.out, nullptr, r0.n, (int)ib, 0, (int)(8 * ib), srv->ctx,
+					s, false, &err);
+		} else if (r0.n) {
+			e = clo::scan_exclusive(r0.in, r0.out, r0.n, r0.type, (int)ob, srv->ctx, s, &err);
 		}
 	} else {
 		const size_t ib = elem_bytes(r0.type);
@@ -139,9 +165,17 @@ void launch_batch(clo_server *srv, Batch *b, Lane *lane) {
 		uint64_t *h_off = b->h_off;
 		h_off[0] = 0;
 		for (size_t i = 0; i < k; ++i) h_off[i + 1] = h_off[i] + b->items[i]->r.n;
-		// Device layout: [offsets][inputs][outputs (scan)], 256-byte aligned.
-		const size_t off_bytes = (k + 1) * 8;
-		const size_t in_at = (off_bytes + 255) / 256 * 256;
+		// Device-resident batches also pass the requests' pointers.
+		uint64_t *h_in = h_off + k + 1, *h_out = h_in + k;
+		if (dev_data)
+			for (size_t i = 0; i < k; ++i) {
+				h_in[i] = (uint64_t)(uintptr_t)b->items[i]->r.in;
+				h_out[i] = (uint64_t)(uintptr_t)b->items[i]->r.out;
+			}
+		// Device layout: [offsets (+ pointers)][inputs][outputs (scan)],
+		// 256-byte aligned.
+		const size_t meta_bytes = (dev_data ? 3 * k + 1 : k + 1) * 8;
+		const size_t in_at = (meta_bytes + 255) / 256 * 256;
 		const size_t out_at = r0.op == CLO_SERVE_SCAN ? (in_at + total * ib + 255) / 256 * 256
 			: in_at;
 		const size_t bytes = out_at + total * ob + 16;
@@ -152,12 +186,17 @@ void launch_batch(clo_server *srv, Batch *b, Lane *lane) {
 			uint64_t *d_off = (uint64_t *)dev;
 			char *din = dev + in_at;
 			char *dout = dev + out_at;
-			e = cudaMemcpyAsync(d_off, h_off, off_bytes, cudaMemcpyHostToDevice, s);
-			for (size_t i = 0; i < k && e == cudaSuccess; ++i) {
-				const CloServeRequest &r = b->items[i]->r;
-				if (r.n)
-					e = cudaMemcpyAsync(din + h_off[i] * ib, r.in, r.n * ib,
-						cudaMemcpyHostToDevice, s);
+			e = cudaMemcpyAsync(d_off, h_off, meta_bytes, cudaMemcpyHostToDevice, s);
+			if (dev_data) {
+				if (e == cudaSuccess)
+					e = clo::seg_gather(din, (const void *const *)(d_off + k + 1), d_off,
+						(uint32_t)k, total, (int)ib, srv->ctx->sm_count, s);
+			} else {
+				for (size_t i = 0; i < k && e == cudaSuccess; ++i) {
+					const CloServeRequest &r = b->items[i]->r;
+					if (r.n)
+						e = cudaMemcpyAsync(din + h_off[i] * ib, r.in, r.n * ib, h2d, s);
+				}
 			}
 			if (e == cudaSuccess && total > 0) {
 				// A request alone takes the plain kernels (the chunked
@@ -176,11 +215,16 @@ void launch_batch(clo_server *srv, Batch *b, Lane *lane) {
 					e = clo::seg_scan(din, dout, total, d_off, k, r0.type, (int)ob,
 						srv->ctx, s, &err);
 			}
-			for (size_t i = 0; i < k && e == cudaSuccess; ++i) {
-				const CloServeRequest &r = b->items[i]->r;
-				if (r.n)
-					e = cudaMemcpyAsync(r.out, dout + h_off[i] * ob, r.n * ob,
-						cudaMemcpyDeviceToHost, s);
+			if (dev_data) {
+				if (e == cudaSuccess)
+					e = clo::seg_scatter((void *const *)(d_off + 2 * k + 1), dout, d_off,
+						(uint32_t)k, total, (int)ob, srv->ctx->sm_count, s);
+			} else {
+				for (size_t i = 0; i < k && e == cudaSuccess; ++i) {
+					const CloServeRequest &r = b->items[i]->r;
+					if (r.n)
+						e = cudaMemcpyAsync(r.out, dout + h_off[i] * ob, r.n * ob, d2h, s);
+				}
 			}
 			clo::tmp_free(dev, s);
 		}
@@ -288,7 +332,7 @@ void sched_loop(clo_server *srv) {
 			if (b->items[0]->r.op != CLO_SERVE_RNG_FILL) {
 				if (srv->pinned_free.empty()) {
 					uint64_t *p = nullptr;
-					if (cudaMallocHost(&p, (kMaxBatch + 1) * 8) != cudaSuccess) {
+					if (cudaMallocHost(&p, kPinnedWords * 8) != cudaSuccess) {
 						cudaGetLastError();
 						p = nullptr;
 					}
@@ -351,6 +395,7 @@ size_t clo_serve_select(const CloServeRequest *pending, size_t npending,
 	for (size_t i = 1; i < npending && k < max_batch; ++i) {
 		const CloServeRequest &r = pending[i];
 		if (r.op != h.op || r.type != h.type || r.n > small_n) continue;
+		if ((r.device_data != CL_FALSE) != (h.device_data != CL_FALSE)) continue;
 		if (h.op == CLO_SERVE_SCAN && r.sum_type != h.sum_type) continue;
 		const size_t f = clo_serve_footprint(&r);
 		if (f == 0 || elems + r.n > batch_elems || need + f > free_bytes) continue;

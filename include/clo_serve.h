@@ -2,8 +2,11 @@
  * cl_ops on GB300 -- serving layer (no counterpart in the reference).
  *
  * A server owns one GPU context and runs sort, scan and random-fill
- * requests whose data live in host memory (page-locked memory from
- * clo_host_alloc keeps the copies asynchronous). Requests are admitted in
+ * requests whose data live either in host memory (page-locked memory from
+ * clo_host_alloc keeps the copies asynchronous) or in device memory of the
+ * server's GPU (device-resident buffers: no host copies; small requests of
+ * a batch are gathered into one buffer and scattered back by kernels).
+ * Requests are admitted in
  * arrival order while their device footprint fits in the server's byte
  * budget; small requests of the same kind (sort or scan, same types) that
  * wait together are batched into one segmented call, which gives each of
@@ -35,9 +38,12 @@ typedef struct clo_serve_request {
 	size_t n;          /* SORT / SCAN: elements; RNG_FILL: generator states */
 	size_t draws;      /* RNG_FILL: draws per state */
 	int rng;           /* RNG_FILL: generator, index into clo_rng_infos */
-	const void *in;    /* host input: the elements, or the states' raw bytes */
-	void *out;         /* host output: n elements / n sums / draws * n uint32
+	const void *in;    /* input: the elements, or the states' raw bytes */
+	void *out;         /* output: n elements / n sums / draws * n uint32
 	                    * (draw-major, as clo_rng_fill) */
+	cl_bool device_data;  /* CL_TRUE: in and out are device pointers on the
+	                       * server's GPU (device-resident buffers; `in` is
+	                       * only read); CL_FALSE: host memory */
 } CloServeRequest;
 
 typedef struct clo_serve_stats {
@@ -94,8 +100,9 @@ void clo_serve_destroy(CloServer *srv);
  * to `chosen` (at most max_batch) and returns how many: none when the
  * oldest does not fit; else the oldest, plus -- when it is a small sort or
  * scan (n <= small_n) -- later waiting requests of the same op and types
- * that are small too, while their elements total at most batch_elems and
- * their footprints fit. */
+ * that are small too (and whose data live in the same kind of memory),
+ * while their elements total at most batch_elems and their footprints
+ * fit. */
 size_t clo_serve_footprint(const CloServeRequest *req);
 size_t clo_serve_select(const CloServeRequest *pending, size_t npending,
 	size_t free_bytes, size_t small_n, size_t batch_elems, size_t max_batch,

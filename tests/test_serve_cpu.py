@@ -13,8 +13,9 @@ def lib(clops):
     return clops
 
 
-def req(clops, op, n, type_=UINT, sum_type=ULONG, draws=0, rng=0):
-    return clops.Server.request(op, type_, sum_type, n, draws, rng, inp=16, out=16)
+def req(clops, op, n, type_=UINT, sum_type=ULONG, draws=0, rng=0, device=False):
+    return clops.Server.request(op, type_, sum_type, n, draws, rng, inp=16, out=16,
+                                device=device)
 
 
 def select(clops, reqs, free, small_n=1 << 20, batch_elems=1 << 26, max_batch=64):
@@ -64,3 +65,13 @@ def test_batch_limits(lib):
     one = fp(lib, reqs[0])
     assert len(select(lib, reqs, 2 * one + one // 2)) == 2
     assert select(lib, [req(lib, RNG, 100, draws=2, rng=1)] * 3, 1 << 40) == [0]
+
+
+def test_device_and_host_requests_batch_apart(lib):
+    reqs = [req(lib, SORT, 100), req(lib, SORT, 100, device=True), req(lib, SORT, 100),
+            req(lib, SORT, 100, device=True)]
+    assert select(lib, reqs, 1 << 40) == [0, 2]
+    assert select(lib, reqs[1:], 1 << 40) == [0, 2]
+    # the same footprint either way (the device-resident form is charged
+    # as much as the host one)
+    assert fp(lib, reqs[0]) == fp(lib, reqs[1])

@@ -108,3 +108,61 @@ def test_serve_open_loop_replay_latency(clops, ctx):
         np.testing.assert_array_equal(dst, exp)
     assert all(t > 0 for t in tickets)
     srv.destroy()
+
+
+def to_device(clops, ctx, q, reqs):
+    """The same requests with device-resident buffers: (request, expected,
+    input buffer, output buffer, output dtype, count, input array)."""
+    out = []
+    for r, exp, dst, a in reqs:
+        bi = clops.Buffer.from_array(ctx, q, a)
+        bo = clops.Buffer(ctx, max(dst.nbytes, 1))
+        rd = clops.Server.request(r.op, r.type, r.sum_type, r.n, r.draws, r.rng,
+                                  inp=bi.ptr, out=bo.ptr, device=True)
+        out.append((rd, exp, bi, bo, dst.dtype, dst.size, a))
+    return out
+
+
+def test_serve_device_resident_mix_matches_oracle_and_alone(clops, ctx, queue):
+    reqs = to_device(clops, ctx, queue, make_requests(clops, 200, seed=72))
+    srv = clops.Server(ctx, 8 << 30, streams=4)
+    tickets = [srv.submit(r[0]) for r in reqs]
+    for t in tickets:
+        srv.wait(t)
+    srv.drain()
+    st = srv.stats()
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    assert st["batches"] < len(reqs)          # small requests were batched
+    mixed = []
+    for rd, exp, bi, bo, dt, cnt, a in reqs:
+        got = bo.read(queue, dt, cnt)
+        np.testing.assert_array_equal(got, exp)
+        np.testing.assert_array_equal(bi.read(queue, a.dtype, a.size), a)  # input only read
+        mixed.append(got)
+    for (rd, _, _, bo, dt, cnt, _), m in zip(reqs, mixed):
+        bo.write(queue, np.zeros(cnt, dt))
+        srv.wait(srv.submit(rd))
+        np.testing.assert_array_equal(bo.read(queue, dt, cnt), m)
+    srv.destroy()
+    for r in reqs:
+        r[2].destroy()
+        r[3].destroy()
+
+
+def test_serve_host_and_device_requests_together(clops, ctx, queue):
+    host = make_requests(clops, 60, seed=73, max_log2=14)
+    dev = to_device(clops, ctx, queue, make_requests(clops, 60, seed=74, max_log2=14))
+    srv = clops.Server(ctx, 2 << 30, streams=3)
+    order = []
+    for h, d in zip(host, dev):
+        order.append(srv.submit(h[0]))
+        order.append(srv.submit(d[0]))
+    srv.drain()
+    assert srv.stats()["completed"] == 120 and srv.stats()["failed"] == 0
+    for _, exp, dst, _ in host:
+        np.testing.assert_array_equal(dst, exp)
+    for rd, exp, bi, bo, dt, cnt, _ in dev:
+        np.testing.assert_array_equal(bo.read(queue, dt, cnt), exp)
+        bi.destroy()
+        bo.destroy()
+    srv.destroy()
