@@ -194,7 +194,9 @@ struct CtaCfg {
 // a block scan of the digit totals, stable ranks through shared-memory OR
 // peer masks, and a pass through shared memory back to index order.
 // Elements past the segment end are all-ones keys: they rank last in every
-// digit, so they stay behind the segment and are never written.
+// digit, so they stay behind the segment and are never written. Warps whose
+// keys all lie past the end take no part in the passes (their counts stay
+// zero), so a segment pays only for the warps it fills.
 template <typename K, int THREADS, int KPT>
 __global__ void __launch_bounds__(THREADS) seg_sort_cta(K *keys, const uint64_t *off,
 	const uint32_t *list, const uint32_t *count, int passes) {
@@ -221,6 +223,9 @@ __global__ void __launch_bounds__(THREADS) seg_sort_cta(K *keys, const uint64_t 
 		const uint32_t s = list[li];
 		const uint64_t base = off[s];
 		const uint32_t len = (uint32_t)(off[s + 1] - base);
+		// Warps holding part of the segment, and the keys they hold.
+		const bool active = wb < len;
+		const uint32_t held = std::min<uint32_t>(TILE, (len + KPT * 32 - 1) / (KPT * 32) * (KPT * 32));
 		K k[KPT];
 #pragma unroll
 		for (int j = 0; j < KPT; ++j) {
@@ -231,8 +236,10 @@ __global__ void __launch_bounds__(THREADS) seg_sort_cta(K *keys, const uint64_t 
 			const int shift = p * kRadixBits;
 			for (int i = lane; i < kRadix; i += 32) my_hist[i] = 0;
 			__syncwarp();
+			if (active) {
 #pragma unroll
-			for (int j = 0; j < KPT; ++j) atomicAdd(my_hist + digit_of(k[j], shift), 1u);
+				for (int j = 0; j < KPT; ++j) atomicAdd(my_hist + digit_of(k[j], shift), 1u);
+			}
 			__syncthreads();
 			// Digit totals (DPT consecutive digits per thread), the scan of
 			// the threads' sums within each warp, and whether one digit holds
@@ -249,7 +256,7 @@ __global__ void __launch_bounds__(THREADS) seg_sort_cta(K *keys, const uint64_t 
 					for (int w = 0; w < W; ++w) c += s_hist[w * kRadix + d];
 					tot[q] = c;
 					tsum += c;
-					triv = triv || c == (d == kRadix - 1 ? (uint32_t)TILE : len);
+					triv = triv || c == (d == kRadix - 1 ? held : len);
 				}
 				tinc = tsum;
 #pragma unroll
@@ -277,14 +284,18 @@ __global__ void __launch_bounds__(THREADS) seg_sort_cta(K *keys, const uint64_t 
 				}
 			}
 			__syncthreads();
+			if (active) {
 #pragma unroll
-			for (int j = 0; j < KPT; ++j) {
-				sk[dev::warp_rank_digit(my_match, my_hist, digit_of(k[j], shift), lane, lt)] =
-					k[j];
+				for (int j = 0; j < KPT; ++j) {
+					sk[dev::warp_rank_digit(my_match, my_hist, digit_of(k[j], shift), lane, lt)] =
+						k[j];
+				}
 			}
 			__syncthreads();
+			if (active) {
 #pragma unroll
-			for (int j = 0; j < KPT; ++j) k[j] = sk[wb + j * 32 + lane];
+				for (int j = 0; j < KPT; ++j) k[j] = sk[wb + j * 32 + lane];
+			}
 		}
 #pragma unroll
 		for (int j = 0; j < KPT; ++j) {
