@@ -307,12 +307,16 @@ __global__ void __launch_bounds__(THREADS) seg_sort_cta(K *keys, const uint64_t 
 }
 
 // ------------------------------------------------------ large segments
-// Tile -> segment map, and clearing of what the passes accumulate into:
-// the segment's digit histograms and the first pass's tile statuses.
+// Tile -> segment map and per-tile descriptors (segment start and end,
+// tile index within the segment, large-segment rank: what a pass needs to
+// start a tile, in one round trip), and clearing of what the passes
+// accumulate into: the segment's digit histograms and the first pass's
+// tile statuses.
 template <int TILE>
 __global__ void __launch_bounds__(256) seg_tiles(const uint64_t *off,
 	const uint64_t *tstart, const uint32_t *list, const uint32_t *count,
-	uint32_t *tile_seg, uint32_t *seg_hist, int passes, uint32_t *status0) {
+	uint32_t *tile_seg, ulonglong2 *tile_span, uint2 *tile_x, uint32_t *seg_hist,
+	int passes, uint32_t *status0) {
 	const uint32_t lane = threadIdx.x & 31u;
 	const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -323,7 +327,12 @@ __global__ void __launch_bounds__(256) seg_tiles(const uint64_t *off,
 		const uint32_t first = (uint32_t)(ts >> 32), lr = (uint32_t)ts;
 		const uint64_t len = off[s + 1] - off[s];
 		const uint32_t ntiles = (uint32_t)((len + TILE - 1) / TILE);
-		for (uint32_t t = lane; t < ntiles; t += 32) tile_seg[first + t] = s;
+		const ulonglong2 span = make_ulonglong2(off[s], off[s + 1]);
+		for (uint32_t t = lane; t < ntiles; t += 32) {
+			tile_seg[first + t] = s;
+			tile_span[first + t] = span;
+			tile_x[first + t] = make_uint2(t, lr);
+		}
 		uint4 *h = reinterpret_cast<uint4 *>(seg_hist + (size_t)lr * passes * kRadix);
 		for (uint32_t q = lane; q < (uint32_t)passes * (kRadix / 4); q += 32)
 			h[q] = make_uint4(0, 0, 0, 0);
@@ -375,6 +384,8 @@ struct SegPassArgs {
 	const uint64_t *off;
 	const uint64_t *tstart;
 	const uint32_t *tile_seg;
+	const ulonglong2 *tile_span;  // segment [start, end) of each tile
+	const uint2 *tile_x;          // (tile index within the segment, rank)
 	const uint32_t *seg_hist;  // + pass * 256; stride passes * 256 per segment
 	uint32_t hist_stride;
 	uint32_t *status;
@@ -459,22 +470,24 @@ seg_pass(const K *__restrict__ kin, K *__restrict__ kout, SegPassArgs a) {
 #pragma unroll
 	for (int i = 0; i < GROWS; ++i) s_cnt[seg_row(grp * GROWS + i) + pd] = 0;
 	const uint32_t T = (uint32_t)(a.tstart[a.S] >> 32);
+	// Thread 0 takes the next tile and its descriptor (one round trip after
+	// the claim); after the first tile this overlaps the write-out.
+	auto claim = [&]() {
+		const uint32_t t = atomicAdd(a.counter, 1u);
+		s_misc[0] = t;
+		if (t < T) {
+			const ulonglong2 span = a.tile_span[t];
+			const uint2 x = a.tile_x[t];
+			s_misc[1] = x.x;   // tile index within the segment
+			s_misc[2] = x.y;   // large-segment rank
+			s_seg[0] = span.x;
+			s_seg[1] = span.y;
+		}
+	};
+	if (tid == 0) claim();
+	__syncthreads();
 
 	for (;;) {
-		if (tid == 0) {
-			const uint32_t t = atomicAdd(a.counter, 1u);
-			s_misc[0] = t;
-			if (t < T) {
-				const uint32_t s = a.tile_seg[t];
-				const uint64_t ts = a.tstart[s];
-				const uint32_t first = (uint32_t)(ts >> 32);
-				s_misc[1] = t - first;       // tile index within the segment
-				s_misc[2] = (uint32_t)ts;    // large-segment rank
-				s_seg[0] = a.off[s];
-				s_seg[1] = a.off[s + 1];
-			}
-		}
-		__syncthreads();
 		const uint32_t tile = s_misc[0];
 		if (tile >= T) break;
 		const uint32_t ti = s_misc[1];
@@ -595,6 +608,7 @@ seg_pass(const K *__restrict__ kin, K *__restrict__ kout, SegPassArgs a) {
 			if (pos < (uint32_t)TILE) sk[pos] = k[j];
 		}
 		__syncthreads();
+		if (tid == 0) claim();
 #pragma unroll
 		for (int i = 0; i < KPT; ++i) {
 			const int q = i * kLThreads + tid;
@@ -748,14 +762,16 @@ cudaError_t seg_sort_typed(K *keys, uint64_t n_cap, const uint64_t *off, uint32_
 	const uint64_t L_bound = std::min<uint64_t>(S, n_cap / (max_b + 1));
 	const uint64_t T_bound = n_cap / LTILE + L_bound + 1;
 	// Scratch: [counts 16][lists 4S][tinfo S+1][tstart S+1] then, with large
-	// segments possible, [tile_seg T][seg_hist L*passes*256][status 2*T*256]
-	// [alt keys n_cap].
+	// segments possible, [tile_seg T][tile_span T][tile_x T]
+	// [seg_hist L*passes*256][status 2*T*256][alt keys n_cap].
 	size_t off_cnt = 0;
 	size_t off_lists = 64;
 	size_t off_tinfo = (off_lists + 4 * (size_t)S * 4 + 15) / 16 * 16;
 	size_t off_tstart = off_tinfo + ((size_t)S + 1) * 8;
 	size_t off_tseg = (off_tstart + ((size_t)S + 1) * 8 + 255) / 256 * 256;
-	size_t off_hist = (off_tseg + T_bound * 4 + 255) / 256 * 256;
+	size_t off_tspan = (off_tseg + T_bound * 4 + 255) / 256 * 256;
+	size_t off_tx = off_tspan + T_bound * 16;
+	size_t off_hist = (off_tx + T_bound * 8 + 255) / 256 * 256;
 	size_t off_st0 = (off_hist + L_bound * passes * kRadix * 4 + 255) / 256 * 256;
 	size_t off_st1 = off_st0 + T_bound * kRadix * 4;
 	size_t off_alt = (off_st1 + T_bound * kRadix * 4 + 255) / 256 * 256;
@@ -767,6 +783,8 @@ cudaError_t seg_sort_typed(K *keys, uint64_t n_cap, const uint64_t *off, uint32_
 	uint64_t *tinfo = (uint64_t *)(tmp + off_tinfo);
 	uint64_t *tstart = (uint64_t *)(tmp + off_tstart);
 	uint32_t *tile_seg = (uint32_t *)(tmp + off_tseg);
+	ulonglong2 *tile_span = (ulonglong2 *)(tmp + off_tspan);
+	uint2 *tile_x = (uint2 *)(tmp + off_tx);
 	uint32_t *seg_hist = (uint32_t *)(tmp + off_hist);
 	uint32_t *st[2] = {(uint32_t *)(tmp + off_st0), (uint32_t *)(tmp + off_st1)};
 	K *alt = alt_ext ? alt_ext : (K *)(tmp + off_alt);
@@ -813,7 +831,7 @@ cudaError_t seg_sort_typed(K *keys, uint64_t n_cap, const uint64_t *off, uint32_
 			const uint32_t grid = (uint32_t)std::min<uint64_t>((L_bound + 7) / 8,
 				(uint64_t)ctx->sm_count * 8);
 			seg_tiles<LTILE><<<grid, 256, 0, s>>>(off, tstart, list3, counts + 3, tile_seg,
-				seg_hist, passes, st[0]);
+				tile_span, tile_x, seg_hist, passes, st[0]);
 			launches++;
 			e = cudaGetLastError();
 		}
@@ -842,6 +860,8 @@ cudaError_t seg_sort_typed(K *keys, uint64_t n_cap, const uint64_t *off, uint32_
 			pa.off = off;
 			pa.tstart = tstart;
 			pa.tile_seg = tile_seg;
+			pa.tile_span = tile_span;
+			pa.tile_x = tile_x;
 			pa.seg_hist = seg_hist + (size_t)p * kRadix;
 			pa.hist_stride = (uint32_t)(passes * kRadix);
 			pa.status = st[p & 1];
