@@ -628,7 +628,9 @@ cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
 	}
 	std::vector<int> active;
 	if (e == cudaSuccess) {
-		if (allow_skip && n >= (1u << 16)) {
+		// Below 2^22 keys the readback's host round trip (the GPU idles
+		// while the host decides) costs about what a skipped pass saves.
+		if (allow_skip && n >= ((size_t)1 << 22)) {
 			std::vector<uint32_t> h((size_t)passes * kRadix);
 			e = cudaMemcpyAsync(h.data(), hist, h.size() * 4, cudaMemcpyDeviceToHost, s);
 			if (e == cudaSuccess) e = cudaStreamSynchronize(s);
