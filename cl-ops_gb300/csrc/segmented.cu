@@ -1263,9 +1263,11 @@ cudaError_t seg_scan_out(const void *in, void *out, uint64_t n_cap, const uint64
 }
 
 // ------------------------------------------------ gather / scatter
-// Thread t of the grid handles 16 consecutive elements of the contiguous
-// buffer: one binary search for the segment of the first, then forward.
-constexpr int kGatherRun = 16;
+// Each warp moves 512 consecutive elements of the contiguous buffer, lane l
+// taking elements l, l + 32, ... (coalesced on both sides within a run):
+// one binary search for the segment of the lane's first element, then
+// forward.
+constexpr int kGatherRun = 16;  // elements per lane per warp chunk
 
 __device__ __forceinline__ uint32_t segment_of(const uint64_t *off, uint32_t k, uint64_t g) {
 	// Largest i with off[i] <= g (off[0] = 0 <= g < off[k]).
@@ -1281,17 +1283,29 @@ __device__ __forceinline__ uint32_t segment_of(const uint64_t *off, uint32_t k, 
 template <typename T, bool GATHER>
 __global__ void __launch_bounds__(256) seg_move(T *flat, T *const *ptrs, const uint64_t *off,
 	uint32_t k, uint64_t total) {
-	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * kGatherRun;
-	for (uint64_t g0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) * kGatherRun;
-		 g0 < total; g0 += stride) {
+	constexpr uint64_t kChunk = 32 * kGatherRun;
+	const uint32_t lane = threadIdx.x & 31u;
+	const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+	for (uint64_t c = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+		 c * kChunk < total; c += warps) {
+		const uint64_t g0 = c * kChunk + lane;
+		if (g0 >= total) continue;
 		uint32_t i = segment_of(off, k, g0);
-		uint64_t next = off[i + 1];
+		uint64_t start = off[i], next = off[i + 1];
+		T *base = ptrs[i];
 #pragma unroll 4
 		for (int e = 0; e < kGatherRun; ++e) {
-			const uint64_t g = g0 + e;
+			const uint64_t g = g0 + (uint64_t)e * 32;
 			if (g >= total) break;
-			while (next <= g) next = off[++i + 1];
-			T *p = ptrs[i] + (g - off[i]);
+			if (next <= g) {
+				do {
+					++i;
+					next = off[i + 1];
+				} while (next <= g);
+				start = off[i];
+				base = ptrs[i];
+			}
+			T *p = base + (g - start);
 			if (GATHER) flat[g] = *p;
 			else *p = flat[g];
 		}
@@ -1302,9 +1316,9 @@ template <bool GATHER>
 cudaError_t seg_move_launch(void *flat, void *const *ptrs, const uint64_t *off, uint32_t k,
 	uint64_t total, int eb, int sm_count, cudaStream_t s) {
 	if (total == 0 || k == 0) return cudaSuccess;
-	const uint64_t threads = (total + kGatherRun - 1) / kGatherRun;
+	const uint64_t warps = (total + 32 * kGatherRun - 1) / (32 * kGatherRun);
 	const unsigned grid = (unsigned)std::max<uint64_t>(1,
-		std::min<uint64_t>((threads + 255) / 256, (uint64_t)sm_count * 16));
+		std::min<uint64_t>((warps + 7) / 8, (uint64_t)sm_count * 16));
 	switch (eb) {
 	case 1: seg_move<uint8_t, GATHER><<<grid, 256, 0, s>>>((uint8_t *)flat, (uint8_t *const *)ptrs, off, k, total); break;
 	case 2: seg_move<uint16_t, GATHER><<<grid, 256, 0, s>>>((uint16_t *)flat, (uint16_t *const *)ptrs, off, k, total); break;
