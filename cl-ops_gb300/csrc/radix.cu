@@ -64,7 +64,7 @@ __device__ __forceinline__ uint32_t digit_of(K k, int shift) {
 constexpr int kUpsweepThreads = 256;
 constexpr size_t kUpsweepKeysPerThread = 4096;
 constexpr int kUpsweepColumnPasses = 4;  // most positions counted in columns
-constexpr int kUpsweepInFlight = 4;
+constexpr int kUpsweepInFlight = 8;
 
 template <int PASSES>
 constexpr size_t upsweep_smem() {
