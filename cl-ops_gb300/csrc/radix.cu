@@ -55,8 +55,8 @@ __device__ __forceinline__ uint32_t digit_of(K k, int shift) {
 // positions count into lane columns: the (d & 1) 16-bit half of word
 // (d >> 1) * 32 + lane per position, shared by the CTA's warps through
 // atomics, so a warp's 32 increments hit 32 different banks; more positions
-// count into one 256-bin row per warp and position. Each thread keeps four
-// 16-byte loads in flight.
+// count into one 256-bin row per warp and position. Each thread keeps
+// kUpsweepInFlight 16-byte loads in flight.
 //
 // A column half receives at most kWarps x (keys per thread) increments;
 // the grid is sized so that a thread sees at most kUpsweepKeysPerThread
