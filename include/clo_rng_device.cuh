@@ -73,14 +73,17 @@ CLO_RNG_HD uint32_t clo_rng_step_mwc64x(uint2 *s) {
  * m = 2^31 - 1, with C's truncating signed remainder; output shifted left
  * by one. */
 CLO_RNG_HD uint32_t clo_rng_step_parkmiller(int32_t *s) {
-	int64_t p = (int64_t)(*s) * 16807;
-	// |p| < 2^46; |p| mod (2^31 - 1) by folding (2^31 = 1 modulo 2^31 - 1):
-	// a*2^31 + b = a + b, then at most one subtraction. The sign follows
-	// the dividend, as C's truncating % does.
-	uint64_t u = (uint64_t)(p < 0 ? -p : p);
-	uint64_t q = (u & 0x7FFFFFFFull) + (u >> 31);
-	if (q >= 0x7FFFFFFFull) q -= 0x7FFFFFFFull;
-	int32_t v = p < 0 ? -(int32_t)q : (int32_t)q;
+	// p = s * 16807; |p| = |s| * 16807 < 2^46 as one 32x32->64 product.
+	// |p| mod (2^31 - 1) by folding (2^31 = 1 modulo 2^31 - 1):
+	// a*2^31 + b = a + b, in 32 bits, then at most one subtraction. The
+	// sign follows the dividend (the sign of s), as C's truncating % does.
+	const int32_t x = *s;
+	const uint32_t a = x < 0 ? 0u - (uint32_t)x : (uint32_t)x;
+	const uint64_t w = (uint64_t)a * 16807u;
+	const uint32_t lo = (uint32_t)w, hi = (uint32_t)(w >> 32);
+	uint32_t q = (lo & 0x7FFFFFFFu) + ((hi << 1) | (lo >> 31));
+	if (q >= 0x7FFFFFFFu) q -= 0x7FFFFFFFu;
+	const int32_t v = x < 0 ? -(int32_t)q : (int32_t)q;
 	*s = v;
 	return ((uint32_t)v) << 1;
 }
