@@ -335,7 +335,7 @@ def run_suite(clops, ctx, q, args, only=None):
             x.destroy()
 
     def kv():
-        n = 1 << 27
+        n = 1 << (27 if only is None else min(args.log2n, 27))
         k = keys_u64(43, n)
         v = np.arange(n, dtype=np.uint32)
         kp, vp = clops.Buffer.from_array(ctx, q, k), clops.Buffer.from_array(ctx, q, v)
@@ -347,7 +347,7 @@ def run_suite(clops, ctx, q, args, only=None):
             copy(vp, vb, v.nbytes)
         ms_copy = timed(restore)
         ms = timed(lambda: (restore(), s.sort_kv_device(q, kb, vb, clops.CLO_UINT, n))) - ms_copy
-        res["satradix_kv_2pow27_u64_u32"] = {
+        res[f"satradix_kv_2pow{n.bit_length() - 1}_u64_u32"] = {
             "Gpairs/s": round(n / (ms * 1e-3) / 1e9, 3), "ms": round(ms, 3),
             "model_bytes_per_pair": 200,
             "frac_of_peak": round(200.0 * n / (ms * 1e-3) / 1e9 / peak, 4)}

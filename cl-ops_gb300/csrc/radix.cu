@@ -14,10 +14,11 @@
 //      a. the CTA counts its chunk's digits, publishes the counts and looks
 //         back over the preceding chunks once (decoupled lookback, one
 //         thread per digit, bounded waits) for its digits' global offsets;
-//      b. per tile, keys are loaded warp-striped (a warp's keys are in
-//         index order) and ranked among equal digits of their warp, stably
-//         (lanes in order, rounds in order): peers found through a
-//         shared-memory OR mask, the lowest advancing the warp's counter;
+//      b. per tile, keys are loaded in half-warp units (a unit's keys are
+//         in index order) and ranked among equal digits of their unit,
+//         stably (lanes in order, rounds in order): peers found through a
+//         shared-memory OR mask in the low half of the unit's word for the
+//         digit, whose high half holds the unit's next position;
 //      c. keys (then values) are staged in shared memory in tile-sorted
 //         order and written out so that consecutive threads write
 //         consecutive addresses of a digit's run, each digit's run
@@ -163,7 +164,7 @@ radix_upsweep(const K *__restrict__ keys, size_t n, uint32_t *__restrict__ hist,
 // ----------------------------------------------------------- onesweep pass
 struct PassArgs {
 	const uint32_t *hist;   // 256 bins of this digit position
-	uint32_t *status;       // num_tiles * 256 words used by this pass
+	uint32_t *status;       // chunks * 256 words used by this pass
 	uint32_t *status_next;  // the other buffer, cleared for the next pass
 	uint32_t *tile_counter;
 	int *dev_status;
