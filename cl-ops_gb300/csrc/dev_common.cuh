@@ -7,17 +7,14 @@
 namespace clo {
 namespace dev {
 
-__device__ __forceinline__ uint32_t lane_id() {
-	return threadIdx.x & 31u;
-}
-
 __device__ __forceinline__ uint32_t lanemask_lt() {
 	uint32_t m;
 	asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
 	return m;
 }
 
-// Relaxed/acquire/release accesses at GPU scope for lookback flags.
+// Relaxed accesses at GPU scope for the lookback status words (each word
+// carries its own ready bits, so no ordering beyond the word is needed).
 __device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t *p) {
 	uint32_t v;
 	asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -28,19 +25,11 @@ __device__ __forceinline__ uint64_t ld_relaxed_u64(const uint64_t *p) {
 	asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
 	return v;
 }
-__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p) {
-	uint32_t v;
-	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-	return v;
-}
 __device__ __forceinline__ void st_relaxed_u32(uint32_t *p, uint32_t v) {
 	asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
 }
 __device__ __forceinline__ void st_relaxed_u64(uint64_t *p, uint64_t v) {
 	asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" :: "l"(p), "l"(v) : "memory");
-}
-__device__ __forceinline__ void st_release_u32(uint32_t *p, uint32_t v) {
-	asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
 }
 
 // Streaming (evict-first) 16-byte load/store for data touched once.
