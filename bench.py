@@ -96,6 +96,10 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+# HBM bandwidth of the GB300 specification, the secondary denominator.
+SPEC_HBM_GBS = 8000.0
+
+
 def ncu_traffic(name):
     """DRAM bytes per launch recorded from an ncu capture, if committed."""
     p = ROOT / "profiles" / name
@@ -289,6 +293,13 @@ def run_ours(args):
             "upsweep_avg_ms": round(up_ms / up_n, 4) if up_n else None,
             "whole_sort_model": "36 B/key (4 B upsweep + 4 passes x 8 B)",
             "whole_sort_frac": round((36.0 * n * K / (ms / 1e3) / 1e9) / peak, 4),
+            # The same fractions against the 8 TB/s specification, and the
+            # whole sort against its n x 8 B lower bound (one read and one
+            # write of the keys).
+            "spec_peak": SPEC_HBM_GBS,
+            "frac_of_spec": round(achieved / SPEC_HBM_GBS, 4) if achieved else None,
+            "whole_sort_frac_of_spec": round((36.0 * n * K / (ms / 1e3) / 1e9) / SPEC_HBM_GBS, 4),
+            "lower_bound_8B_per_key_frac": round((8.0 * n * K / (ms / 1e3) / 1e9) / peak, 4),
         },
         "clocks": clk,
     }
