@@ -9,20 +9,21 @@
 // Per sort:
 //   1. radix_upsweep: one read of the keys builds the 256-bin histogram
 //      of every digit position at once.
-//   2. per digit position, radix_pass_chunked (one launch per pass), one
-//      CTA per contiguous chunk of 4096-key tiles (2048 for 64-bit keys):
-//      a. the CTA counts its chunk's digits, publishes the counts and looks
-//         back over the preceding chunks once (decoupled lookback, one
-//         thread per digit, bounded waits) for its digits' global offsets;
-//      b. per tile, keys are loaded in half-warp units (a unit's keys are
-//         in index order) and ranked among equal digits of their unit,
-//         stably (lanes in order, rounds in order): peers found through a
-//         shared-memory OR mask in the low half of the unit's word for the
-//         digit, whose high half holds the unit's next position;
-//      c. keys (then values) are staged in shared memory in tile-sorted
-//         order and written out so that consecutive threads write
-//         consecutive addresses of a digit's run, each digit's run
-//         continuing where the previous tile's ended.
+//   2. per digit position, radix_pass_tiles (one launch per pass), one CTA
+//      per tile (14336 32-bit keys; 5120 pairs of a 64-bit key and a
+//      32-bit value), tiles claimed in order from a counter:
+//      a. keys are loaded in half-warp units (a unit's keys are in index
+//         order), the tile's digit counts are published for the decoupled
+//         lookback before the tile is ranked;
+//      b. keys are ranked among equal digits of their unit, stably (lanes
+//         in order, rounds in order): peers found through a shared-memory
+//         OR mask in the low half of the unit's word for the digit, whose
+//         high half holds the unit's next position; keys (and values) are
+//         staged in shared memory in tile-sorted order;
+//      c. one thread per digit looks back over the preceding tiles
+//         (bounded waits) for the digit's global offset;
+//      d. the staged tile is written out so that consecutive threads write
+//         consecutive addresses of a digit's run.
 // Passes whose digit has a single populated bin are skipped (the order of
 // a stable sort by a constant digit is the identity).
 //
@@ -164,7 +165,7 @@ radix_upsweep(const K *__restrict__ keys, size_t n, uint32_t *__restrict__ hist,
 // ----------------------------------------------------------- onesweep pass
 struct PassArgs {
 	const uint32_t *hist;   // 256 bins of this digit position
-	uint32_t *status;       // chunks * 256 words used by this pass
+	uint32_t *status;       // tiles * 256 words used by this pass
 	uint32_t *status_next;  // the other buffer, cleared for the next pass
 	uint32_t *tile_counter;
 	int *dev_status;
@@ -172,11 +173,13 @@ struct PassArgs {
 	int shift;
 };
 
-// Lookback window: predecessor statuses read per round trip per digit.
-constexpr int kLookWindow = 32;
+// Lookback window: predecessor statuses read per round trip per digit. A
+// tile's nearest inclusive predecessor is a few tiles back; wider windows
+// measured slower.
+constexpr int kLookWindow = 8;
 
-// Threads per CTA of the chunked pass.
-constexpr int kChunkThreads = 256;
+// Threads per CTA of the pass: one per digit in the per-tile scans.
+constexpr int kPassThreads = kRadix;
 
 // Reads the statuses of tiles base, base-1, ..., base-W+1 for one digit
 // (independent loads, one round trip), adds them in order to `excl` up to
@@ -211,336 +214,208 @@ __device__ __forceinline__ bool lookback_window(const uint32_t *status, int digi
 }
 
 
-// ------------------------------------------------------- chunked pass
-// One CTA per contiguous chunk of tiles (chunks claimed in order from an
-// atomic counter). The CTA first counts the digit over its whole chunk
-// with streaming 16-byte loads, publishes the chunk's counts and looks
-// back over the preceding chunks -- one decoupled lookback per CTA and
-// pass instead of one per tile, so no tile ever waits on another CTA --
-// then ranks and scatters its tiles in order, each digit's run continuing
-// where the previous tile's ended. The counting read costs key-size bytes
-// per key on top of the pass's read and write. With 256 threads
-// (4096-key tiles) four CTAs share an SM and hide each other's per-tile
-// latency.
-//
-// Shared-memory work per key is what bounds the pass, so both counting
-// steps and the ranking are built to touch few shared words:
-//  - phase 1 counts into lane columns: digit d of lane l is the (d & 1)
-//    16-bit half of word (d >> 1) * 32 + l, shared by the CTA's warps
-//    through atomics. A warp's 32 increments hit 32 different banks.
-//  - phase 2 ranks in half-warp units (16 lanes, KPT rounds): the unit's
-//    word for digit d holds the unit's next tile position for d in its
-//    upper half and the round's peer mask in its lower half, so a round is
-//    one OR, one read and one store by the lowest peer.
-template <typename K, int THREADS>
-struct ChunkCfg {
-	static_assert(THREADS == kRadix, "one thread per digit in the per-tile scans");
-	static constexpr int kWarps = THREADS / 32;
-	static constexpr int kUnits = 2 * kWarps;          // half-warp ranking units
-	static constexpr int kKpt = sizeof(K) <= 4 ? 16 : 8;
-	static constexpr int kUnitKeys = 16 * kKpt;        // a unit's keys in one tile
-	static constexpr int kTile = THREADS * kKpt;
-	// Largest chunk: a lane-column counter half receives at most kWarps x
-	// (keys per thread) = kWarps x (2^20 / THREADS + 4) < 2^16 increments.
-	static constexpr size_t kMaxChunkKeys = (size_t)1 << 20;
-};
-
-// Chunks (CTAs) of a pass over ctiles tiles: one per resident CTA
-// (per_sm x SMs), more when the chunks would exceed kMaxChunkKeys.
-template <typename K>
-uint32_t chunk_count(size_t ctiles, int sm_count, int per_sm) {
-	using Cfg = ChunkCfg<K, kChunkThreads>;
-	constexpr size_t kMaxTiles = Cfg::kMaxChunkKeys / Cfg::kTile;
-	const size_t c = std::max<size_t>((size_t)std::max(per_sm, 1) * sm_count,
-		(ctiles + kMaxTiles - 1) / kMaxTiles);
-	return (uint32_t)std::max<size_t>(std::min(c, ctiles), 1);
-}
-
 // Ranking and count rows: 256 digits each, 264 words apart, odd rows 8
 // words later, so rows 2w and 2w + 1 (the two units of warp w) hold a digit
 // 16 banks apart and a digit both halves of a warp hold does not conflict.
 constexpr int kRowWords = kRadix + 8;
 __device__ __forceinline__ int row_of(int r) { return r * kRowWords + (r & 1) * 8; }
 
-// Keys of one unit in a tile, round-major: round j of lane l holds key
-// ubase + 16 j + l, so the unit's (round, lane) order is index order.
-template <typename K, int THREADS>
-__device__ __forceinline__ void chunk_load_keys(K (&k)[ChunkCfg<K, THREADS>::kKpt],
-	const K *__restrict__ kin, size_t n, uint32_t tile, int unit, int l16) {
-	using Cfg = ChunkCfg<K, THREADS>;
-	const size_t ubase = (size_t)tile * Cfg::kTile + (size_t)unit * Cfg::kUnitKeys;
-#pragma unroll
-	for (int j = 0; j < Cfg::kKpt; ++j) {
-		size_t idx = ubase + (size_t)j * 16 + l16;
-		k[j] = idx < n ? kin[idx] : (K)~(K)0;
-	}
+// ------------------------------------------------------- onesweep pass
+// One tile per CTA, tiles claimed in order from an atomic counter, so every
+// tile a CTA waits on belongs to a CTA that is already running. Per tile:
+//  1. keys (and values) are loaded in half-warp units: unit u holds the
+//     tile's keys u * 16 KPT .. (u + 1) * 16 KPT - 1, round j of lane l the
+//     key 16 j + l, so a unit's (round, lane) order is index order;
+//  2. the digits are counted into per-unit rows (16-bit halves, units u and
+//     u + 8 sharing a row); the thread of digit d turns them into unit
+//     prefixes and the tile's count of d, and publishes the count as the
+//     tile's lookback status (tile 0: its inclusive prefix) before the
+//     tile is ranked;
+//  3. ranking: the unit's word for digit d holds the unit's next tile
+//     position for d in its upper half and the round's peer mask in its
+//     lower half, so a round is one OR, one read and one store by the
+//     lowest peer (stable: lanes in order, rounds in order); keys and
+//     values are staged in shared memory at their tile-sorted positions;
+//  4. the thread of digit d looks back over the preceding tiles' statuses
+//     (windows of kLookWindow, bounded waits), publishes the inclusive
+//     prefix and sets the digit's output base;
+//  5. the staged tile is written out so that consecutive threads write
+//     consecutive addresses of a digit's run.
+// Consecutive tiles fill consecutive stretches of every digit's output, so
+// output lines complete in L2 while they are hot, and the pass moves one
+// read and one write of each key (and value). Tiles are large (TilesCfg)
+// because each costs one lookback.
+template <typename K, typename V, bool HAS_V, int KPT>
+constexpr size_t tiles_smem() {
+	return ((16 + 8) * kRowWords + 2 * kRadix + 64) * sizeof(uint32_t) +
+		(size_t)kPassThreads * KPT * (sizeof(K) + (HAS_V ? sizeof(V) : 0));
 }
 
-// Values of one unit in a tile, in the keys' layout.
-template <typename K, typename V, int THREADS>
-__device__ __forceinline__ void chunk_load_vals(V (&v)[ChunkCfg<K, THREADS>::kKpt],
-	const V *__restrict__ vin, size_t n, uint32_t tile, int unit, int l16) {
-	using Cfg = ChunkCfg<K, THREADS>;
-	const size_t ubase = (size_t)tile * Cfg::kTile + (size_t)unit * Cfg::kUnitKeys;
-#pragma unroll
-	for (int j = 0; j < Cfg::kKpt; ++j) {
-		size_t idx = ubase + (size_t)j * 16 + l16;
-		v[j] = idx < n ? vin[idx] : (V)0;
-	}
-}
-
-template <typename K, typename V, bool HAS_V, int THREADS>
-constexpr size_t chunked_smem() {
-	using Cfg = ChunkCfg<K, THREADS>;
-	return ((Cfg::kUnits + Cfg::kUnits / 2) * kRowWords + 4 * kRadix + 64) * sizeof(uint32_t) +
-		(size_t)Cfg::kTile * (sizeof(K) + (HAS_V ? sizeof(V) : 0));
-}
-
-// Resident CTAs per SM the pass is compiled for: four for keys only, three
-// with values (keys and values of a tile stay in registers), fewer when
-// the shared memory (228 KB per SM, 1 KB reserved per CTA) allows fewer.
-template <typename K, typename V, bool HAS_V, int THREADS>
-constexpr int chunked_min_blocks() {
-	constexpr int by_smem = (int)((228 * 1024) / (chunked_smem<K, V, HAS_V, THREADS>() + 1024));
-	constexpr int want = HAS_V ? 3 : 4;
-	return by_smem < want ? by_smem : want;
-}
-
-template <typename K, typename V, bool HAS_V, int THREADS>
-__global__ void __launch_bounds__(THREADS, (chunked_min_blocks<K, V, HAS_V, THREADS>()))
-radix_pass_chunked(const K *__restrict__ kin, K *__restrict__ kout,
-	const V *__restrict__ vin, V *__restrict__ vout, PassArgs a,
-	uint32_t num_tiles, uint32_t num_chunks) {
-	using Cfg = ChunkCfg<K, THREADS>;
-	constexpr int KPT = Cfg::kKpt;
-	constexpr int TILE = Cfg::kTile;
-	constexpr int UNITS = Cfg::kUnits;
+template <typename K, typename V, bool HAS_V, int KPT, int MINB>
+__global__ void __launch_bounds__(kPassThreads, MINB)
+radix_pass_tiles(const K *__restrict__ kin, K *__restrict__ kout,
+	const V *__restrict__ vin, V *__restrict__ vout, PassArgs a, uint32_t num_tiles) {
+	constexpr int THREADS = kPassThreads;
+	constexpr int TILE = THREADS * KPT;
+	constexpr int UNITS = 16;
 	constexpr int HALF = UNITS / 2;
-	constexpr int kWin = kLookWindow / 2;
+	constexpr int UKEYS = 16 * KPT;  // a unit's keys
+	static_assert(UKEYS <= 0xFFFF && TILE <= 0xFFFF, "16-bit unit and tile counts");
+	constexpr int kWin = kLookWindow;
 	extern __shared__ __align__(16) unsigned char smem[];
-	// Ranking rows of units and count rows, kRowWords apart (row_of).
 	uint32_t *s_rank = reinterpret_cast<uint32_t *>(smem);   // [UNITS] rows
 	uint32_t *s_cnt = s_rank + UNITS * kRowWords;            // [HALF] rows
 	uint32_t *s_tile_off = s_cnt + HALF * kRowWords;         // [256]
-	uint32_t *s_tile_cnt = s_tile_off + kRadix;              // [256]
-	uint32_t *s_run = s_tile_cnt + kRadix;                   // [256]
-	uint32_t *s_part = s_run + kRadix;                       // [256]
+	uint32_t *s_part = s_tile_off + kRadix;                  // [256]
 	uint32_t *s_misc = s_part + kRadix;                      // [64]
 	unsigned char *s_stage = reinterpret_cast<unsigned char *>(s_misc + 64);
-	// Phase 1 only: [128][32] lane-column counters over s_rank.
-	uint32_t *s_col = s_rank;
-	static_assert(UNITS * kRowWords >= (kRadix / 2) * 32, "column counters fit");
 
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const int unit = 2 * warp + (lane >> 4);
 	const uint32_t l16 = lane & 15;
 	const uint32_t lt16 = (1u << l16) - 1u;
 	uint32_t *my_rank = s_rank + row_of(unit);
-	// Tile counts: units u and u + HALF share row u % HALF (16-bit halves).
 	uint32_t *my_cnt = s_cnt + row_of(unit % HALF);
 	const uint32_t cnt_inc = 1u << ((unit / HALF) * 16);
 	const int shift = a.shift;
-	const int pd = tid;        // the digit this thread scans
-	const int dw = pd >> 5;    // the warp that owns digit pd
+	const int pd = tid;
+	const int dw = pd >> 5;
 
 	if (tid == 0) s_misc[0] = atomicAdd(a.tile_counter, 1u);
-	for (int i = tid; i < (kRadix / 2) * 32; i += THREADS) s_col[i] = 0;
 #pragma unroll
 	for (int i = 0; i < HALF; ++i) s_cnt[row_of(i) + pd] = 0;
 	// Global digit base of this pass: exclusive scan of its histogram.
-	{
-		const uint32_t hv = a.hist[pd];
-		uint32_t inc = hv;
+	const uint32_t hv = a.hist[pd];
+	uint32_t hinc = hv;
 #pragma unroll
-		for (int s = 1; s < 32; s <<= 1) {
-			uint32_t t = __shfl_up_sync(0xffffffffu, inc, s);
-			if (lane >= s) inc += t;
-		}
-		if (lane == 31) s_misc[16 + dw] = inc;
-		s_part[pd] = inc - hv;
+	for (int s = 1; s < 32; s <<= 1) {
+		uint32_t t = __shfl_up_sync(0xffffffffu, hinc, s);
+		if (lane >= s) hinc += t;
 	}
+	if (lane == 31) s_misc[16 + dw] = hinc;
 	__syncthreads();
-	const uint32_t c = s_misc[0];
-	if (c >= num_chunks) return;
-	uint32_t run_init;
-	{
-		uint32_t goff = 0;
+	const uint32_t t = s_misc[0];
+	if (t >= num_tiles) return;
+	uint32_t gbase = hinc - hv;
 #pragma unroll
-		for (int w = 0; w < 8; ++w)
-			if (w < dw) goff += s_misc[16 + w];
-		run_init = s_part[pd] + goff;
-	}
-	const uint32_t t0 = (uint32_t)((uint64_t)c * num_tiles / num_chunks);
-	const uint32_t t1 = (uint32_t)((uint64_t)(c + 1) * num_tiles / num_chunks);
-	const size_t k_lo = (size_t)t0 * TILE;
-	const size_t k_hi = (size_t)t1 * TILE < a.n ? (size_t)t1 * TILE : a.n;
+	for (int w = 0; w < 8; ++w)
+		if (w < dw) gbase += s_misc[16 + w];
 
-	// Phase 1: digit counts of the whole chunk, in lane columns.
-	{
-		constexpr int PER = 16 / sizeof(K);
-		uint32_t *col = s_col + lane;
-		const bool vec = ((uintptr_t)(kin + k_lo) % 16) == 0;
-		const size_t nvec = vec ? (k_hi - k_lo) / PER : 0;
-		const uint4 *src = reinterpret_cast<const uint4 *>(kin + k_lo);
-		constexpr int kIn = 4;  // 16-byte loads in flight per thread
-		size_t i = tid;
-		for (; i + (kIn - 1) * THREADS < nvec; i += kIn * THREADS) {
-			uint4 v[kIn];
-#pragma unroll
-			for (int u = 0; u < kIn; ++u) v[u] = dev::ld_stream_v4(src + i + u * THREADS);
-#pragma unroll
-			for (int u = 0; u < kIn; ++u) {
-				const K *e = reinterpret_cast<const K *>(&v[u]);
-#pragma unroll
-				for (int q = 0; q < PER; ++q) {
-					const uint32_t d = digit_of(e[q], shift);
-					atomicAdd(col + (d >> 1) * 32, 1u << ((d & 1) << 4));
-				}
-			}
-		}
-		for (; i < nvec; i += THREADS) {
-			uint4 v = dev::ld_stream_v4(src + i);
-			const K *e = reinterpret_cast<const K *>(&v);
-#pragma unroll
-			for (int q = 0; q < PER; ++q) {
-				const uint32_t d = digit_of(e[q], shift);
-				atomicAdd(col + (d >> 1) * 32, 1u << ((d & 1) << 4));
-			}
-		}
-		for (size_t i = k_lo + nvec * PER + tid; i < k_hi; i += THREADS) {
-			const uint32_t d = digit_of(kin[i], shift);
-			atomicAdd(col + (d >> 1) * 32, 1u << ((d & 1) << 4));
-		}
-	}
-	__syncthreads();
-	{
-		// Sum digit pd's 32 column halves (rotated start: no bank conflicts).
-		const uint32_t *row = s_col + (pd >> 1) * 32;
-		const int hs = (pd & 1) << 4;
-		uint32_t cnt = 0;
-#pragma unroll 8
-		for (int i = 0; i < 32; ++i) cnt += (row[(i + lane) & 31] >> hs) & 0xFFFFu;
-		uint32_t *st = a.status + (size_t)c * kRadix + pd;
-		if (c == 0) dev::st_relaxed_u32(st, kStPrefix | cnt);
-		else dev::st_relaxed_u32(st, kStAgg | cnt);
-		a.status_next[(size_t)c * kRadix + pd] = 0;
-		uint32_t excl = 0;
-		if (c > 0) {
-			long long base = (long long)c - 1;
-			uint32_t iter = 0;
-			bool done = lookback_window<4>(a.status, pd, base, excl);
-			while (!done && base >= 0) {
-				uint32_t sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + pd);
-				while ((sv & ~kStValue) == 0) {
-					if (++iter >= dev::kSpinLimit) break;
-					dev::backoff(iter);
-					sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + pd);
-				}
-				if ((sv & ~kStValue) == 0) {
-					dev::report_timeout(a.dev_status, DEV_ERR_LOOKBACK_TIMEOUT, (int)c);
-					break;
-				}
-				done = lookback_window<kWin>(a.status, pd, base, excl);
-			}
-			dev::st_relaxed_u32(st, kStPrefix | (excl + cnt));
-		}
-		s_run[pd] = run_init;
-		s_tile_cnt[pd] = excl;  // the first tile's run starts after excl
-	}
-	__syncthreads();
-
-	// Phase 2: tiles of the chunk in order.
+	// Keys (and values) of this thread's unit, round-major (index order).
 	K k[KPT];
 	V v[HAS_V ? KPT : 1];
-	if (t0 < t1) {
-		chunk_load_keys<K, THREADS>(k, kin, a.n, t0, unit, l16);
-		if constexpr (HAS_V) chunk_load_vals<K, V, THREADS>(v, vin, a.n, t0, unit, l16);
+	const size_t ubase = (size_t)t * TILE + (size_t)unit * UKEYS;
+#pragma unroll
+	for (int j = 0; j < KPT; ++j) {
+		const size_t idx = ubase + (size_t)j * 16 + l16;
+		k[j] = idx < a.n ? kin[idx] : (K)~(K)0;
+		if constexpr (HAS_V) v[j] = idx < a.n ? vin[idx] : (V)0;
 	}
-	for (uint32_t t = t0; t < t1; ++t) {
 #pragma unroll
-		for (int j = 0; j < KPT; ++j) atomicAdd(my_cnt + digit_of(k[j], shift), cnt_inc);
-		__syncthreads();
-		// Unit prefixes of digit pd in unit order (rows' low halves are
-		// units 0..HALF-1, high halves units HALF..UNITS-1); the rows are
-		// cleared for the next tile as they are read.
-		uint32_t c2[HALF];
+	for (int j = 0; j < KPT; ++j) atomicAdd(my_cnt + digit_of(k[j], shift), cnt_inc);
+	__syncthreads();
+	// Unit prefixes of digit pd in unit order and the tile's count.
+	uint32_t c2[HALF];
 #pragma unroll
-		for (int i = 0; i < HALF; ++i) {
-			c2[i] = s_cnt[row_of(i) + pd];
-			s_cnt[row_of(i) + pd] = 0;
+	for (int i = 0; i < HALF; ++i) c2[i] = s_cnt[row_of(i) + pd];
+	uint32_t run = 0;
+#pragma unroll
+	for (int i = 0; i < HALF; ++i) {
+		const uint32_t lo = c2[i] & 0xFFFFu;
+		c2[i] = (c2[i] & 0xFFFF0000u) | run;
+		run += lo;
+	}
+#pragma unroll
+	for (int i = 0; i < HALF; ++i) {
+		const uint32_t hi = c2[i] >> 16;
+		c2[i] = (c2[i] & 0xFFFFu) | (run << 16);
+		run += hi;
+	}
+	const uint32_t sum = run;
+	// Publish the tile's count of digit pd (tile 0: its inclusive prefix).
+	uint32_t *st = a.status + (size_t)t * kRadix + pd;
+	dev::st_relaxed_u32(st, (t == 0 ? kStPrefix : kStAgg) | sum);
+	a.status_next[(size_t)t * kRadix + pd] = 0;
+	// Tile offsets of the digits: exclusive scan of the counts.
+	{
+		uint32_t inc = sum;
+#pragma unroll
+		for (int d = 1; d < 32; d <<= 1) {
+			uint32_t tt = __shfl_up_sync(0xffffffffu, inc, d);
+			if (lane >= d) inc += tt;
 		}
-		uint32_t run = 0;
+		if (lane == 31) s_misc[8 + dw] = inc;
+		s_part[pd] = inc - sum;
+	}
+	__syncthreads();
+	uint32_t to = s_part[pd];
 #pragma unroll
-		for (int i = 0; i < HALF; ++i) {
-			const uint32_t lo = c2[i] & 0xFFFFu;
-			c2[i] = (c2[i] & 0xFFFF0000u) | run;
-			run += lo;
+	for (int w = 0; w < 8; ++w)
+		if (w < dw) to += s_misc[8 + w];
+#pragma unroll
+	for (int i = 0; i < HALF; ++i) {
+		s_rank[row_of(i) + pd] = (to + (c2[i] & 0xFFFFu)) << 16;
+		s_rank[row_of(i + HALF) + pd] = (to + (c2[i] >> 16)) << 16;
+	}
+	__syncthreads();
+	K *sk = reinterpret_cast<K *>(s_stage);
+	V *sv = reinterpret_cast<V *>(s_stage + (size_t)TILE * sizeof(K));
+#pragma unroll
+	for (int j = 0; j < KPT; ++j) {
+		const uint32_t pos = dev::unit_rank_digit(my_rank + digit_of(k[j], shift), l16, lt16);
+		if (pos < (uint32_t)TILE) {
+			sk[pos] = k[j];
+			if (HAS_V) sv[pos] = v[j];
 		}
-#pragma unroll
-		for (int i = 0; i < HALF; ++i) {
-			const uint32_t hi = c2[i] >> 16;
-			c2[i] = (c2[i] & 0xFFFFu) | (run << 16);
-			run += hi;
-		}
-		const uint32_t sum = run;
-		// Advance the run by the previous tile's count (or the lookback).
-		s_run[pd] += s_tile_cnt[pd];
-		s_tile_cnt[pd] = sum;
-		{
-			uint32_t inc = sum;
-#pragma unroll
-			for (int d = 1; d < 32; d <<= 1) {
-				uint32_t tt = __shfl_up_sync(0xffffffffu, inc, d);
-				if (lane >= d) inc += tt;
+	}
+	// Lookback over the preceding tiles for digit pd (bounded waits).
+	uint32_t excl = 0;
+	if (t > 0) {
+		long long base = (long long)t - 1;
+		uint32_t iter = 0;
+		bool done = lookback_window<kWin>(a.status, pd, base, excl);
+		while (!done && base >= 0) {
+			uint32_t sw = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + pd);
+			while ((sw & ~kStValue) == 0) {
+				if (++iter >= dev::kSpinLimit) break;
+				dev::backoff(iter);
+				sw = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + pd);
 			}
-			if (lane == 31) s_misc[8 + dw] = inc;
-			s_part[pd] = inc - sum;
-		}
-		__syncthreads();
-		{
-			uint32_t woff = 0;
-#pragma unroll
-			for (int w = 0; w < 8; ++w)
-				if (w < dw) woff += s_misc[8 + w];
-			const uint32_t to = s_part[pd] + woff;
-#pragma unroll
-			for (int i = 0; i < HALF; ++i) {
-				s_rank[row_of(i) + pd] = (to + (c2[i] & 0xFFFFu)) << 16;
-				s_rank[row_of(i + HALF) + pd] = (to + (c2[i] >> 16)) << 16;
+			if ((sw & ~kStValue) == 0) {
+				dev::report_timeout(a.dev_status, DEV_ERR_LOOKBACK_TIMEOUT, (int)t);
+				break;
 			}
-			// Output index of staged position q of digit d is q + G[d]
-			// (modulo 2^32), G[d] = global run start - tile offset.
-			s_tile_off[pd] = s_run[pd] - to;
+			done = lookback_window<kWin>(a.status, pd, base, excl);
 		}
-		__syncthreads();
-		K *sk = reinterpret_cast<K *>(s_stage);
-		V *sv = reinterpret_cast<V *>(s_stage + (size_t)TILE * sizeof(K));
+		dev::st_relaxed_u32(st, kStPrefix | (excl + sum));
+	}
+	// Output index of staged position q of digit d is q + G[d] (mod 2^32).
+	s_tile_off[pd] = gbase + excl - to;
+	__syncthreads();
 #pragma unroll
-		for (int j = 0; j < KPT; ++j) {
-			const uint32_t pos = dev::unit_rank_digit(my_rank + digit_of(k[j], shift), l16, lt16);
-			if (pos < (uint32_t)TILE) {
-				sk[pos] = k[j];
-				if (HAS_V) sv[pos] = v[j];
-			}
-		}
-		__syncthreads();
-		if (t + 1 < t1) {
-			chunk_load_keys<K, THREADS>(k, kin, a.n, t + 1, unit, l16);
-			if constexpr (HAS_V) chunk_load_vals<K, V, THREADS>(v, vin, a.n, t + 1, unit, l16);
-		}
-#pragma unroll
-		for (int i = 0; i < KPT; ++i) {
-			const int q = i * THREADS + tid;
-			const K key = sk[q];
-			const size_t o = (uint32_t)(s_tile_off[digit_of(key, shift)] + (uint32_t)q);
-			if (o < a.n) {
-				kout[o] = key;
-				if (HAS_V) vout[o] = sv[q];
-			}
+	for (int i = 0; i < KPT; ++i) {
+		const int q = i * THREADS + tid;
+		const K key = sk[q];
+		const size_t o = (uint32_t)(s_tile_off[digit_of(key, shift)] + (uint32_t)q);
+		if (o < a.n) {
+			kout[o] = key;
+			if (HAS_V) vout[o] = sv[q];
 		}
 	}
 }
 
+// Tile shape of the pass by the 32-bit register words a key (and value)
+// takes: keys per thread and resident CTAs per SM, each the measured best
+// at 2^27 - 2^28 elements (larger tiles mean fewer lookbacks; the limit is
+// 128 registers a thread without spills). 32-bit keys: 14336-key tiles;
+// 64-bit keys with 32-bit values: 5120 pairs.
+template <typename K, typename V, bool HAS_V>
+struct TilesCfg {
+	static constexpr int kWords = (int)((sizeof(K) + 3) / 4) + (HAS_V ? (int)((sizeof(V) + 3) / 4) : 0);
+	static constexpr int kKpt = kWords == 1 ? 56 : kWords == 2 ? 32 : kWords == 3 ? 20 : 16;
+	static constexpr int kMinBlocks = 2;
+	static constexpr int kTile = kPassThreads * kKpt;
+};
 
 template <typename K, int PASSES>
 void launch_upsweep_p(cudaStream_t s, const K *keys, size_t n, uint32_t *hist,
@@ -585,24 +460,19 @@ cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
 			"satradix: %zu elements exceed the single-sort limit of 2^30 - 1", n);
 		return cudaErrorInvalidValue;
 	}
-	// The chunked pass: tiles of ChunkCfg size, one chunk per CTA.
-	constexpr int CT = kChunkThreads;
-	constexpr int CTILE = ChunkCfg<K, CT>::kTile;
-	const size_t ctiles = (n + CTILE - 1) / CTILE;
-	const size_t smem = chunked_smem<K, V, HAS_V, CT>();
-	auto kern = radix_pass_chunked<K, V, HAS_V, CT>;
+	// One CTA per tile of TilesCfg size.
+	using TC = TilesCfg<K, V, HAS_V>;
+	const size_t ctiles = (n + TC::kTile - 1) / TC::kTile;
+	const size_t smem = tiles_smem<K, V, HAS_V, TC::kKpt>();
+	auto kern = radix_pass_tiles<K, V, HAS_V, TC::kKpt, TC::kMinBlocks>;
 	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
 		(int)smem);
-	int per_sm = 0;
-	if (e == cudaSuccess)
-		e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, CT, smem);
 	if (e != cudaSuccess) {
 		cuda_ok(e, err, "satradix");
 		return e;
 	}
-	const uint32_t chunks = chunk_count<K>(ctiles, ctx->sm_count, per_sm);
-	// Status slots: one per chunk.
-	const size_t status_words = (size_t)chunks * kRadix;
+	// Status slots: one per tile.
+	const size_t status_words = ctiles * kRadix;
 	// Scratch: [hist passes*256][counters 8][status0][status1][alt keys][alt vals]
 	size_t off_hist = 0;
 	size_t off_cnt = off_hist + (size_t)passes * kRadix * 4;
@@ -659,8 +529,8 @@ cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
 			pa.shift = active[q] * kRadixBits;
 			KernelTimer t("satradix_onesweep", s,
 				2.0 * (double)n * (sizeof(K) + (HAS_V ? sizeof(V) : 0)));
-			kern<<<chunks, CT, smem, s>>>(src_k, dst_k, src_v, dst_v, pa,
-				(uint32_t)ctiles, chunks);
+			kern<<<(unsigned)ctiles, kPassThreads, smem, s>>>(src_k, dst_k, src_v, dst_v, pa,
+				(uint32_t)ctiles);
 			t.stop();
 			launches++;
 			e = cudaGetLastError();
@@ -682,27 +552,22 @@ cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
 // Stable partition of n keys by the top 8 of their sort_bits low bits:
 // keys_out receives the keys grouped by that digit, in input order within a
 // digit; counts (host) receives the 256 group sizes. One histogram kernel
-// for the digit, a host readback of its 256 counts, one chunked pass.
+// for the digit, a host readback of its 256 counts, one pass.
 template <typename K>
 cudaError_t msd_partition_typed(const K *keys_in, K *keys_out, size_t n, int sort_bits,
 	uint32_t *counts, CCLContext *ctx, cudaStream_t s, GError **err) {
-	constexpr int CT = kChunkThreads;
-	constexpr int CTILE = ChunkCfg<K, CT>::kTile;
+	using TC = TilesCfg<K, uint32_t, false>;
 	const int shift = sort_bits - kRadixBits;
-	const size_t ctiles = (n + CTILE - 1) / CTILE;
-	const size_t smem = chunked_smem<K, uint32_t, false, CT>();
-	auto kern = radix_pass_chunked<K, uint32_t, false, CT>;
+	const size_t ctiles = (n + TC::kTile - 1) / TC::kTile;
+	const size_t smem = tiles_smem<K, uint32_t, false, TC::kKpt>();
+	auto kern = radix_pass_tiles<K, uint32_t, false, TC::kKpt, TC::kMinBlocks>;
 	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
 		(int)smem);
-	int per_sm = 0;
-	if (e == cudaSuccess)
-		e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, CT, smem);
 	if (e != cudaSuccess) {
 		cuda_ok(e, err, "satradix partition");
 		return e;
 	}
-	const uint32_t chunks = chunk_count<K>(ctiles, ctx->sm_count, per_sm);
-	const size_t status_words = (size_t)chunks * kRadix;
+	const size_t status_words = ctiles * kRadix;
 	const size_t off_cnt = kRadix * 4, off_st0 = off_cnt + 64;
 	const size_t off_st1 = off_st0 + status_words * 4;
 	char *tmp = (char *)tmp_alloc(ctx, off_st1 + status_words * 4, s, err);
@@ -733,8 +598,8 @@ cudaError_t msd_partition_typed(const K *keys_in, K *keys_out, size_t n, int sor
 		pa.shift = shift;
 		if (e == cudaSuccess) {
 			KernelTimer t("satradix_onesweep", s, 2.0 * (double)n * sizeof(K));
-			kern<<<chunks, CT, smem, s>>>(keys_in, keys_out, nullptr, nullptr, pa,
-				(uint32_t)ctiles, chunks);
+			kern<<<(unsigned)ctiles, kPassThreads, smem, s>>>(keys_in, keys_out, nullptr, nullptr,
+				pa, (uint32_t)ctiles);
 			t.stop();
 			e = cudaGetLastError();
 		}

@@ -172,11 +172,10 @@ def test_satradix_2pow28_u32_sorted_permutation(clops, ctx, queue):
 
 
 @pytest.mark.slow
-def test_satradix_more_chunks_than_resident_ctas(clops, ctx, queue):
-    """5 x 2^27 + 777 keys: more than 2^20 keys per chunk at one chunk per
-    resident CTA, so the pass runs extra chunks in a second wave (each
-    waiting only on chunks claimed before it) and the upsweep grid is
-    sized by its per-thread key cap."""
+def test_satradix_5x2pow27_keys_many_tile_waves(clops, ctx, queue):
+    """5 x 2^27 + 777 keys: about 47k tiles with a ragged last one, run in
+    many waves of CTAs (each waiting only on tiles claimed before it), and
+    the upsweep grid sized by its per-thread key cap."""
     n = 5 * (1 << 27) + 777
     a = keys_u32(46, n)
     s = clops.Sorter(ctx, "satradix", 5)
