@@ -44,12 +44,14 @@ constexpr int kRadix = 256;
 constexpr int kRadixBits = 8;
 constexpr uint32_t kMaxSegLen = (1u << 30) - 1u;
 
-// Large-segment pass: 512 threads, 16 (8 for 64-bit keys) keys per thread.
-constexpr int kLThreads = 512;
+// Large-segment pass: 256 threads (one per digit in the per-tile scans),
+// 56 keys per thread (32 for 64-bit keys), 2 CTAs per SM: the plain sort's
+// tile shape, large because each tile costs one lookback.
+constexpr int kLThreads = 256;
 constexpr int kLWarps = kLThreads / 32;
 template <typename K>
 struct LCfg {
-	static constexpr int kKpt = sizeof(K) <= 4 ? 16 : 8;
+	static constexpr int kKpt = sizeof(K) <= 4 ? 56 : 32;
 	static constexpr int kTile = kLThreads * kKpt;
 };
 
@@ -429,31 +431,34 @@ __device__ __forceinline__ bool seg_lookback_window(const uint32_t *status, int 
 // a digit 16 banks apart.
 constexpr int kSegRowWords = kRadix + 8;
 __device__ __forceinline__ int seg_row(int r) { return r * kSegRowWords + (r & 1) * 8; }
-constexpr int kLUnits = 2 * kLWarps;  // 32 half-warp units per tile
+constexpr int kLUnits = 2 * kLWarps;  // 16 half-warp units per tile
+constexpr int kSegLookWindow = 8;     // predecessor statuses per round trip
 
 // One pass over all tiles of all large segments, by persistent CTAs that
-// take tiles in order from a counter. A segment's first tile publishes an
-// inclusive prefix at once, so lookbacks never cross segments. Keys are
-// ranked in half-warp units (dev::unit_rank_digit): the unit's word per
-// digit holds its next tile position (upper 16 bits) and the round's peer
-// mask (lower 16). Unit counts are 16-bit halves of 16 count rows (units u
-// and u + 16 share row u); each half of the CTA scans 8 rows.
+// take tiles in order from a counter (the next tile and its descriptor are
+// claimed during the write-out). Per tile as the plain sort's pass: keys
+// loaded in half-warp units (a unit's (round, lane) order is index order),
+// unit counts in 16-bit halves of 8 count rows (units u and u + 8 share
+// row u), the tile's counts published before it is ranked (a segment's
+// first tile publishes an inclusive prefix at once, so lookbacks stop at
+// the segment's start), ranking with dev::unit_rank_digit (the unit's word
+// per digit holds its next tile position in the upper 16 bits and the
+// round's peer mask in the lower 16), staging, then a lookback in windows
+// of kSegLookWindow and a write-out with one base per digit.
 template <typename K>
 __global__ void __launch_bounds__(kLThreads, 2)
 seg_pass(const K *__restrict__ kin, K *__restrict__ kout, SegPassArgs a) {
 	constexpr int KPT = LCfg<K>::kKpt;
 	constexpr int TILE = LCfg<K>::kTile;
 	constexpr int UKEYS = 16 * KPT;          // a unit's keys in one tile
-	constexpr int CROWS = kLUnits / 2;       // 16 count rows
-	constexpr int GROWS = CROWS / 2;         // rows per thread group
+	constexpr int HALF = kLUnits / 2;        // 8 count rows
+	static_assert(TILE <= 0xFFFF, "16-bit unit and tile counts");
 	extern __shared__ __align__(16) unsigned char smem[];
-	uint32_t *s_rank = reinterpret_cast<uint32_t *>(smem);     // [32] rows
-	uint32_t *s_cnt = s_rank + kLUnits * kSegRowWords;         // [16] rows
-	uint32_t *s_half = s_cnt + CROWS * kSegRowWords;           // [2 groups][2][256]
-	uint32_t *s_tile_off = s_half + 4 * kRadix;                // [256]
-	uint32_t *s_to = s_tile_off + kRadix;                      // [256]
-	uint32_t *s_glob = s_to + kRadix;                          // [256]
-	uint32_t *s_misc = s_glob + kRadix;                        // [64]
+	uint32_t *s_rank = reinterpret_cast<uint32_t *>(smem);     // [16] rows
+	uint32_t *s_cnt = s_rank + kLUnits * kSegRowWords;         // [8] rows
+	uint32_t *s_tile_off = s_cnt + HALF * kSegRowWords;        // [256]
+	uint32_t *s_part = s_tile_off + kRadix;                    // [256]
+	uint32_t *s_misc = s_part + kRadix;                        // [64]
 	uint64_t *s_seg = reinterpret_cast<uint64_t *>(s_misc + 64);  // [2]
 	unsigned char *s_stage = reinterpret_cast<unsigned char *>(s_seg + 2);
 
@@ -462,13 +467,13 @@ seg_pass(const K *__restrict__ kin, K *__restrict__ kout, SegPassArgs a) {
 	const uint32_t l16 = lane & 15;
 	const uint32_t lt16 = (1u << l16) - 1u;
 	uint32_t *my_rank = s_rank + seg_row(unit);
-	uint32_t *my_cnt = s_cnt + seg_row(unit % CROWS);
-	const uint32_t cnt_inc = 1u << ((unit / CROWS) * 16);
-	const int pd = tid & (kRadix - 1), grp = tid >> 8;   // digit, thread group
-	const int dw = (tid >> 5) & 7;                        // warp within the group
+	uint32_t *my_cnt = s_cnt + seg_row(unit % HALF);
+	const uint32_t cnt_inc = 1u << ((unit / HALF) * 16);
+	const int pd = tid;        // the digit this thread scans
+	const int dw = tid >> 5;   // the warp that owns digit pd
 	const int shift = a.shift;
 #pragma unroll
-	for (int i = 0; i < GROWS; ++i) s_cnt[seg_row(grp * GROWS + i) + pd] = 0;
+	for (int i = 0; i < HALF; ++i) s_cnt[seg_row(i) + pd] = 0;
 	const uint32_t T = (uint32_t)(a.tstart[a.S] >> 32);
 	// Thread 0 takes the next tile and its descriptor (one round trip after
 	// the claim); after the first tile this overlaps the write-out.
@@ -493,8 +498,7 @@ seg_pass(const K *__restrict__ kin, K *__restrict__ kout, SegPassArgs a) {
 		const uint32_t ti = s_misc[1];
 		const uint32_t lr = s_misc[2];
 		const uint64_t seg_a = s_seg[0], seg_e = s_seg[1];
-		const uint64_t tile_base = seg_a + (uint64_t)ti * TILE;
-		const uint64_t ubase = tile_base + (uint64_t)unit * UKEYS;
+		const uint64_t ubase = seg_a + (uint64_t)ti * TILE + (uint64_t)unit * UKEYS;
 
 		K k[KPT];
 #pragma unroll
@@ -502,118 +506,105 @@ seg_pass(const K *__restrict__ kin, K *__restrict__ kout, SegPassArgs a) {
 			const uint64_t idx = ubase + (uint64_t)j * 16 + l16;
 			k[j] = idx < seg_e ? kin[idx] : (K)~(K)0;
 		}
+		// Digit base within the segment: exclusive scan of its histogram.
+		const uint32_t hv = a.seg_hist[(size_t)lr * a.hist_stride + pd];
+		uint32_t hinc = hv;
+#pragma unroll
+		for (int d = 1; d < 32; d <<= 1) {
+			const uint32_t t = __shfl_up_sync(0xffffffffu, hinc, d);
+			if (lane >= d) hinc += t;
+		}
+		if (lane == 31) s_misc[16 + dw] = hinc;
 #pragma unroll
 		for (int j = 0; j < KPT; ++j) atomicAdd(my_cnt + digit_of(k[j], shift), cnt_inc);
 		__syncthreads();
-
-		// Unit prefixes within this group's rows (low halves: units
-		// 8 grp .. 8 grp + 7; high halves: units 16 + 8 grp ..), rows
-		// cleared for the next tile as they are read.
-		uint32_t c2[GROWS];
-		uint32_t lo_sum = 0, hi_sum = 0;
+		uint32_t gbase = hinc - hv;
 #pragma unroll
-		for (int i = 0; i < GROWS; ++i) {
-			const int r = seg_row(grp * GROWS + i) + pd;
-			const uint32_t c = s_cnt[r];
-			s_cnt[r] = 0;
-			c2[i] = (lo_sum & 0xFFFFu) | (hi_sum << 16);   // exclusive, per half
-			lo_sum += c & 0xFFFFu;
-			hi_sum += c >> 16;
+		for (int w = 0; w < 8; ++w)
+			if (w < dw) gbase += s_misc[16 + w];
+		// Unit prefixes of digit pd in unit order (low halves: units
+		// 0..7, high halves: units 8..15); rows cleared as they are read.
+		uint32_t c2[HALF];
+#pragma unroll
+		for (int i = 0; i < HALF; ++i) {
+			c2[i] = s_cnt[seg_row(i) + pd];
+			s_cnt[seg_row(i) + pd] = 0;
 		}
-		s_half[(grp * 2 + 0) * kRadix + pd] = lo_sum;
-		s_half[(grp * 2 + 1) * kRadix + pd] = hi_sum;
-		__syncthreads();
-		// Unit order: group 0 low, group 1 low, group 0 high, group 1 high.
-		const uint32_t lo0 = s_half[0 * kRadix + pd], hi0 = s_half[1 * kRadix + pd];
-		const uint32_t lo1 = s_half[2 * kRadix + pd];
-		const uint32_t hi1 = s_half[3 * kRadix + pd];
-		const uint32_t tile_cnt = lo0 + lo1 + hi0 + hi1;
-		const uint32_t base_lo = grp == 0 ? 0u : lo0;
-		const uint32_t base_hi = grp == 0 ? lo0 + lo1 : lo0 + lo1 + hi0;
-		if (grp == 0) {
-			uint32_t *st = a.status + (size_t)tile * kRadix + pd;
-			dev::st_relaxed_u32(st, (ti == 0 ? kStPrefix : kStAgg) | tile_cnt);
-			a.status_next[(size_t)tile * kRadix + pd] = 0;
-			uint32_t inc = tile_cnt;
+		uint32_t run = 0;
+#pragma unroll
+		for (int i = 0; i < HALF; ++i) {
+			const uint32_t lo = c2[i] & 0xFFFFu;
+			c2[i] = (c2[i] & 0xFFFF0000u) | run;
+			run += lo;
+		}
+#pragma unroll
+		for (int i = 0; i < HALF; ++i) {
+			const uint32_t hi = c2[i] >> 16;
+			c2[i] = (c2[i] & 0xFFFFu) | (run << 16);
+			run += hi;
+		}
+		const uint32_t sum = run;
+		uint32_t *st = a.status + (size_t)tile * kRadix + pd;
+		dev::st_relaxed_u32(st, (ti == 0 ? kStPrefix : kStAgg) | sum);
+		a.status_next[(size_t)tile * kRadix + pd] = 0;
+		{
+			uint32_t inc = sum;
 #pragma unroll
 			for (int d = 1; d < 32; d <<= 1) {
 				const uint32_t t = __shfl_up_sync(0xffffffffu, inc, d);
 				if (lane >= d) inc += t;
 			}
 			if (lane == 31) s_misc[8 + dw] = inc;
-			s_tile_off[pd] = inc - tile_cnt;
-		} else {
-			const uint32_t hv = a.seg_hist[(size_t)lr * a.hist_stride + pd];
-			uint32_t inc = hv;
-#pragma unroll
-			for (int s = 1; s < 32; s <<= 1) {
-				const uint32_t t = __shfl_up_sync(0xffffffffu, inc, s);
-				if (lane >= s) inc += t;
-			}
-			if (lane == 31) s_misc[16 + dw] = inc;
-			s_glob[pd] = inc - hv;
+			s_part[pd] = inc - sum;
 		}
 		__syncthreads();
-		uint32_t woff = 0, goff = 0;
+		uint32_t to = s_part[pd];
 #pragma unroll
-		for (int w = 0; w < 8; ++w) {
-			if (w < dw) {
-				woff += s_misc[8 + w];
-				goff += s_misc[16 + w];
-			}
-		}
-		const uint32_t to = s_tile_off[pd] + woff;
+		for (int w = 0; w < 8; ++w)
+			if (w < dw) to += s_misc[8 + w];
 #pragma unroll
-		for (int i = 0; i < GROWS; ++i) {
-			const int r = grp * GROWS + i;
-			s_rank[seg_row(r) + pd] = (to + base_lo + (c2[i] & 0xFFFFu)) << 16;
-			s_rank[seg_row(r + CROWS) + pd] = (to + base_hi + (c2[i] >> 16)) << 16;
-		}
-		uint32_t digit_base = 0;
-		if (grp == 0) {
-			s_to[pd] = to;
-			digit_base = s_glob[pd] + goff;
+		for (int i = 0; i < HALF; ++i) {
+			s_rank[seg_row(i) + pd] = (to + (c2[i] & 0xFFFFu)) << 16;
+			s_rank[seg_row(i + HALF) + pd] = (to + (c2[i] >> 16)) << 16;
 		}
 		__syncthreads();
-
-		if (grp == 0) {
-			uint32_t excl = 0;
-			if (ti > 0) {
-				long long base = (long long)tile - 1;
-				uint32_t iter = 0;
-				bool done = seg_lookback_window<4>(a.status, pd, base, excl);
-				while (!done && base >= 0) {
-					uint32_t sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + pd);
-					while ((sv & ~kStValue) == 0) {
-						if (++iter >= dev::kSpinLimit) break;
-						dev::backoff(iter);
-						sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + pd);
-					}
-					if ((sv & ~kStValue) == 0) {
-						dev::report_timeout(a.dev_status, DEV_ERR_LOOKBACK_TIMEOUT, (int)tile);
-						break;
-					}
-					done = seg_lookback_window<16>(a.status, pd, base, excl);
-				}
-				dev::st_relaxed_u32(a.status + (size_t)tile * kRadix + pd,
-					kStPrefix | (excl + tile_cnt));
-			}
-			s_glob[pd] = digit_base + excl - s_to[pd];
-		}
-
 		K *sk = reinterpret_cast<K *>(s_stage);
 #pragma unroll
 		for (int j = 0; j < KPT; ++j) {
 			const uint32_t pos = dev::unit_rank_digit(my_rank + digit_of(k[j], shift), l16, lt16);
 			if (pos < (uint32_t)TILE) sk[pos] = k[j];
 		}
+		// Lookback over the segment's preceding tiles (bounded waits).
+		uint32_t excl = 0;
+		if (ti > 0) {
+			long long base = (long long)tile - 1;
+			uint32_t iter = 0;
+			bool done = seg_lookback_window<kSegLookWindow>(a.status, pd, base, excl);
+			while (!done && base >= 0) {
+				uint32_t sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + pd);
+				while ((sv & ~kStValue) == 0) {
+					if (++iter >= dev::kSpinLimit) break;
+					dev::backoff(iter);
+					sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + pd);
+				}
+				if ((sv & ~kStValue) == 0) {
+					dev::report_timeout(a.dev_status, DEV_ERR_LOOKBACK_TIMEOUT, (int)tile);
+					break;
+				}
+				done = seg_lookback_window<kSegLookWindow>(a.status, pd, base, excl);
+			}
+			dev::st_relaxed_u32(st, kStPrefix | (excl + sum));
+		}
+		// Output offset (within the segment) of staged position q of digit
+		// d is q + G[d] (modulo 2^32).
+		s_tile_off[pd] = gbase + excl - to;
 		__syncthreads();
 		if (tid == 0) claim();
 #pragma unroll
 		for (int i = 0; i < KPT; ++i) {
 			const int q = i * kLThreads + tid;
 			const K key = sk[q];
-			const uint64_t o = seg_a + (uint32_t)(s_glob[digit_of(key, shift)] + (uint32_t)q);
+			const uint64_t o = seg_a + (uint32_t)(s_tile_off[digit_of(key, shift)] + (uint32_t)q);
 			if (o < seg_e) kout[o] = key;
 		}
 		__syncthreads();
@@ -622,7 +613,7 @@ seg_pass(const K *__restrict__ kin, K *__restrict__ kout, SegPassArgs a) {
 
 template <typename K>
 size_t seg_pass_smem() {
-	return ((size_t)(kLUnits + kLUnits / 2) * kSegRowWords + 7 * kRadix + 64) * sizeof(uint32_t) +
+	return ((size_t)(kLUnits + kLUnits / 2) * kSegRowWords + 3 * kRadix + 64) * sizeof(uint32_t) +
 		2 * sizeof(uint64_t) + (size_t)LCfg<K>::kTile * sizeof(K);
 }
 

@@ -25,9 +25,12 @@ def _seg_sort(clops, ctx, q, code, a, off, options=None, key_type=None, buf_extr
 
 
 # Lengths that hit every class boundary of every variant (32, 512, 1024,
-# 2048, 4096, 8192 and the multi-tile passes), empty and single segments.
+# 2048, 4096, 8192), the large-segment pass's tile edges (14336 keys of up
+# to 32 bits, 8192 of 64 bits; one to three tiles), empty and single
+# segments.
 EDGE_LENS = [0, 1, 2, 31, 32, 33, 0, 511, 512, 513, 1023, 1024, 1025, 2047, 2048, 2049,
-             4095, 4096, 4097, 8191, 8192, 8193, 16384, 16385, 40000, 3, 0, 1]
+             4095, 4096, 4097, 8191, 8192, 8193, 14335, 14336, 14337, 16384, 16385,
+             28672, 28673, 40000, 3, 0, 1]
 
 
 @pytest.mark.parametrize("variant", [0, 1, 2])
