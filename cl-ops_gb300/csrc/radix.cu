@@ -162,7 +162,7 @@ radix_upsweep(const K *__restrict__ keys, size_t n, uint32_t *__restrict__ hist,
 	}
 }
 
-// ----------------------------------------------------------- onesweep pass
+// ------------------------------------------------- pass state and lookback
 struct PassArgs {
 	const uint32_t *hist;   // 256 bins of this digit position
 	uint32_t *status;       // tiles * 256 words used by this pass
@@ -213,7 +213,6 @@ __device__ __forceinline__ bool lookback_window(const uint32_t *status, int digi
 	return done;
 }
 
-
 // Ranking and count rows: 256 digits each, 264 words apart, odd rows 8
 // words later, so rows 2w and 2w + 1 (the two units of warp w) hold a digit
 // 16 banks apart and a digit both halves of a warp hold does not conflict.
@@ -245,6 +244,10 @@ __device__ __forceinline__ int row_of(int r) { return r * kRowWords + (r & 1) * 
 // output lines complete in L2 while they are hot, and the pass moves one
 // read and one write of each key (and value). Tiles are large (TilesCfg)
 // because each costs one lookback.
+//
+// Shared memory: 16 ranking rows and 8 count rows (row_of), the tile
+// offsets and a scan array (256 words each), 64 misc words, the staged
+// tile (keys, then values).
 template <typename K, typename V, bool HAS_V, int KPT>
 constexpr size_t tiles_smem() {
 	return ((16 + 8) * kRowWords + 2 * kRadix + 64) * sizeof(uint32_t) +

@@ -199,8 +199,8 @@ void launch_batch(clo_server *srv, Batch *b, Lane *lane) {
 				}
 			}
 			if (e == cudaSuccess && total > 0) {
-				// A request alone takes the plain kernels (the chunked
-				// onesweep sort, without the host readback of pass skipping);
+				// A request alone takes the plain kernels (the onesweep
+				// sort, without the host readback of pass skipping);
 				// a batch takes one segmented call.
 				if (r0.op == CLO_SERVE_SORT && k == 1)
 					e = clo::radix_sort(din, nullptr, total, (int)ib, 0, (int)(8 * ib),
