@@ -369,9 +369,12 @@ size_t clo_serve_footprint(const CloServeRequest *r) {
 	const size_t slack = 1u << 20;  // tile statuses, offsets, alignment
 	switch (r->op) {
 	case CLO_SERVE_SORT: {
-		// keys + the alternate key buffer of the multi-CTA passes + statuses
+		// keys + the alternate key buffer of the passes + per-tile state:
+		// two 1 KB lookback status slots and 28 B of segment descriptors
+		// for every tile of at least 8192 keys (the smallest tile of a
+		// keys-only pass)
 		const size_t eb = elem_bytes(r->type);
-		return 2 * r->n * eb + r->n / 8 + slack;
+		return 2 * r->n * eb + (r->n + 8191) / 8192 * 2076 + slack;
 	}
 	case CLO_SERVE_SCAN:
 		return r->n * (elem_bytes(r->type) + elem_bytes(r->sum_type)) + r->n / 8 + slack;
