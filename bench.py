@@ -235,7 +235,7 @@ def run_ours(args):
     q.gc()
 
     # ---- end to end: pinned host in/out, blocking host-data call ------------
-    e2e_steps = max(1, min(K, 5))
+    e2e_steps = K
     hin = clops.lib.clo_host_alloc(keys.nbytes, None)
     hout = clops.lib.clo_host_alloc(keys.nbytes, None)
     ain = np.ctypeslib.as_array((clops.C.c_uint32 * n).from_address(hin))
@@ -271,9 +271,7 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "u32",
         "data": "synthetic (splitmix64 seed 42, uniform over [0, 2^32))",
-        "config": {"workload": WORKLOAD, "n": n, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2: a distinct 1 GiB copy per step",
-                   "result_check": "sorted+multiset ok" if ok else "FAILED"},
+        "config": bench_config(n, world, ok),
         "e2e": {"value": round(world * n * e2e_steps / e2e_s / 1e9, 3), "unit": "Gkeys/s",
                 "h2d_bytes_per_step": n * 4, "d2h_bytes_per_step": n * 4,
                 "api": "clo_sort_with_host_data, pinned host buffers"},
@@ -761,48 +759,96 @@ def run_suite(clops, ctx, q, args, only=None):
     return res
 
 
-def cpu_baseline(args):
-    """CPU restatement of the reference algorithm (LSD radix, 4-bit digits
-    as the reference's default radix 16) on a bounded sample, all host
-    threads."""
+def bench_config(n, world, ok):
+    """The headline workload's config, the same in both arms."""
+    return {"workload": WORKLOAD, "n": n, "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2: a distinct 1 GiB copy per step",
+            "result_check": "sorted+multiset ok" if ok else "FAILED"}
+
+
+def cpu_port_sorts(keys, steps, warmup, cores):
+    """The reference's algorithm (LSD radix sort, 4-bit digits as its default
+    radix 16) restated in C, on all host threads: `steps` timed sorts of a
+    fresh copy of `keys` (the copy is made outside the timed part). Returns
+    (total seconds, last output ok)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
-    n = 1 << 24
-    cores = os.cpu_count() or 1
-    keys = keys_u32_chunked(42, n)
-    work = keys.copy()
-    oracle.radix_sort_u32_threaded(work, cores, 4)
-    reps = 3
-    t0 = time.perf_counter()
-    for _ in range(reps):
+    work = np.empty_like(keys)
+    for _ in range(warmup):
         work[:] = keys
         oracle.radix_sort_u32_threaded(work, cores, 4)
-    dt = (time.perf_counter() - t0) / reps
-    return {"value": round(n / dt / 1e9, 4), "unit": "Gkeys/s", "cores": cores, "kind": "port",
-            "sample": "2^24 of the 2^28 uint32 keys (same generator), LSD radix 16, "
-                      f"{reps} timed sorts"}
+    total = 0.0
+    for _ in range(steps):
+        work[:] = keys
+        t0 = time.perf_counter()
+        oracle.radix_sort_u32_threaded(work, cores, 4)
+        total += time.perf_counter() - t0
+    ok = bool(np.all(work[1:] >= work[:-1])) and \
+        int(work.sum(dtype=np.uint64)) == int(keys.sum(dtype=np.uint64))
+    return total, ok
+
+
+def reference_kernels_c1():
+    """The reference's own satradix kernels (its OpenCL C, compiled for the
+    host by oracle/build_ref.py) on 2^20 uint32 keys from seed 42 with radix
+    16, one timed sort. Work-groups run in parallel on all host threads;
+    each work-group's work-items are fibers switched at every barrier, so
+    the time includes that emulation's overhead. Checked against the
+    committed digest of the same run. None where the library is absent."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    try:
+        import ref
+        if not ref.available():
+            return None
+    except Exception:
+        return None
+    import hashlib
+    n = 1 << 20
+    keys = keys_u32_chunked(42, n)
+    t0 = time.perf_counter()
+    out = ref.sort(keys, 5, "satradix", 256)
+    dt = time.perf_counter() - t0
+    want = None
+    kats = json.loads((ROOT / "tests" / "golden" / "reference_kats.json").read_text())["kats"]
+    for k in kats:
+        if k["op"] == "sort" and k["algo"] == "satradix" and k["n"] == n and k["seed"] == 42:
+            want = k["sha256"]
+    got = hashlib.sha256(out.tobytes()).hexdigest()
+    return {"value": round(n / dt / 1e9, 6), "unit": "Gkeys/s", "seconds": round(dt, 2),
+            "cores": int(os.environ.get("CLC_THREADS", os.cpu_count() or 1)),
+            "kind": "reference",
+            "sample": "2^20 uint32 keys, seed 42, radix 16, lws 256: the reference's own "
+                      "satradix kernels through a host OpenCL-C emulation (work-groups on "
+                      "threads, work-items as fibers switched at barriers)",
+            "result_check": "reference digest ok" if got == want else "FAILED"}
+
+
+def cpu_baseline(args):
+    """The reference's algorithm on the host cores, on the full headline
+    workload (3 timed sorts of 2^28 keys), plus the reference's own kernels
+    at 2^20 keys."""
+    n = 1 << args.log2n
+    cores = os.cpu_count() or 1
+    reps = 3
+    total, ok = cpu_port_sorts(keys_u32_chunked(42, n), reps, 1, cores)
+    out = {"value": round(n * reps / total / 1e9, 4), "unit": "Gkeys/s", "cores": cores,
+           "kind": "port",
+           "sample": f"the full workload: {reps} sorts of all 2^{args.log2n} uint32 keys, "
+                     "LSD radix 16, all host threads",
+           "result_check": "sorted+multiset ok" if ok else "FAILED"}
+    rk = reference_kernels_c1() if args.ref_kernels else None
+    if rk is not None:
+        out["reference_kernels"] = rk
+    return out
 
 
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle
-    n = 1 << 24
+    n = 1 << args.log2n
     cores = os.cpu_count() or 1
-    keys = keys_u32_chunked(42, n)
-    work = keys.copy()
-    for _ in range(args.warmup):
-        work[:] = keys
-        oracle.radix_sort_u32_threaded(work, cores, 4)
-    total = 0.0
-    for _ in range(args.steps):
-        work[:] = keys
-        t0 = time.perf_counter()
-        oracle.radix_sort_u32_threaded(work, cores, 4)
-        total += time.perf_counter() - t0
-    ok = bool(np.all(work[1:] >= work[:-1]))
+    total, ok = cpu_port_sorts(keys_u32_chunked(42, n), args.steps, args.warmup, cores)
     val = n * args.steps / total / 1e9
     out = {
         "impl": "reference",
@@ -811,11 +857,10 @@ def run_reference(args):
         "ms_per_step": round(total / args.steps * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic (splitmix64 seed 42, uniform over [0, 2^32))",
-        "config": {"workload": WORKLOAD, "n": 1 << 28, "sample_n": n,
-                   "result_check": "sorted" if ok else "FAILED"},
+        "config": bench_config(n, world, ok),
         "cpu_baseline": {"value": round(val, 4), "unit": "Gkeys/s", "cores": cores, "kind": "port",
-                         "sample": "each step sorts 2^24 of the 2^28 keys with the reference's "
-                                   "LSD radix-16 scheme on all host threads"},
+                         "sample": f"each step sorts all 2^{args.log2n} keys with the reference's "
+                                   "LSD radix-16 scheme (restated in C) on all host threads"},
         "e2e": {"value": round(val, 4), "unit": "Gkeys/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -830,6 +875,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--log2n", type=int, default=28)
     ap.add_argument("--no-suite", dest="suite", action="store_false")
+    ap.add_argument("--no-ref-kernels", dest="ref_kernels", action="store_false",
+                    help="skip timing the reference's own kernels at 2^20 keys")
     ap.add_argument("--serve-seconds", type=float, default=1.0,
                     help="open-loop duration of the serving workload")
     ap.add_argument("--only", choices=["abitonic", "kv", "scan", "rng", "segmented", "serve",

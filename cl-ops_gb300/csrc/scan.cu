@@ -406,23 +406,66 @@ static_assert(kNoAllocMaxElems == ((size_t)1 << 28), "no-allocation scan limit")
 std::mutex g_noalloc_mu;
 uint64_t *g_noalloc_addr[64] = {};
 
-// Device address of the scratch array on device `ordinal`, looked up on
-// the first call for that device with the device current.
-uint64_t *noalloc_scratch(int ordinal, GError **err) {
-	if (ordinal < 0 || ordinal >= 64) {
-		set_error(err, CLO_ERROR_ARGS, "Device ordinal %d out of range", ordinal);
-		return nullptr;
+// Makes `ordinal` the calling thread's current device for the guard's
+// lifetime and restores the previous one afterwards.
+struct CurrentDevice {
+	int prev = -1;
+	cudaError_t status;
+	explicit CurrentDevice(int ordinal) {
+		if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+		status = cudaSetDevice(ordinal);
 	}
+	~CurrentDevice() {
+		if (prev >= 0) cudaSetDevice(prev);
+	}
+};
+
+// Opts every (element, sum) instantiation of the scan kernel into its
+// shared memory and caches its occupancy, so that no later call does any
+// set-up work, whatever its type pair.
+template <typename InT>
+cudaError_t noalloc_prepare_in() {
+	int v = 0;
+	cudaError_t e = scan_prepare<InT, uint8_t>(&v);
+	if (e == cudaSuccess) e = scan_prepare<InT, uint16_t>(&v);
+	if (e == cudaSuccess) e = scan_prepare<InT, uint32_t>(&v);
+	if (e == cudaSuccess) e = scan_prepare<InT, uint64_t>(&v);
+	return e;
+}
+
+cudaError_t noalloc_prepare_all() {
+	cudaError_t e = noalloc_prepare_in<int8_t>();
+	if (e == cudaSuccess) e = noalloc_prepare_in<uint8_t>();
+	if (e == cudaSuccess) e = noalloc_prepare_in<int16_t>();
+	if (e == cudaSuccess) e = noalloc_prepare_in<uint16_t>();
+	if (e == cudaSuccess) e = noalloc_prepare_in<int32_t>();
+	if (e == cudaSuccess) e = noalloc_prepare_in<uint32_t>();
+	if (e == cudaSuccess) e = noalloc_prepare_in<int64_t>();
+	if (e == cudaSuccess) e = noalloc_prepare_in<uint64_t>();
+	return e;
+}
+
+// Device address of the scratch array on device `ordinal` (which must be
+// current), looked up on the first call for that device, together with
+// the set-up of every scan instantiation.
+uint64_t *noalloc_scratch(int ordinal, GError **err) {
 	std::lock_guard<std::mutex> lk(g_noalloc_mu);
 	if (g_noalloc_addr[ordinal] == nullptr) {
-		cudaError_t e = cudaSetDevice(ordinal);
 		void *p = nullptr;
-		if (e == cudaSuccess) e = cudaGetSymbolAddress(&p, g_scan_noalloc_scratch);
+		cudaError_t e = cudaGetSymbolAddress(&p, g_scan_noalloc_scratch);
 		if (e != cudaSuccess || p == nullptr) {
 			cudaGetLastError();
 			set_error(err, CLO_ERROR_LIBRARY,
 				"cudaGetSymbolAddress of the no-allocation scan scratch failed on "
 				"device %d: %s", ordinal, cudaGetErrorString(e));
+			return nullptr;
+		}
+		e = noalloc_prepare_all();
+		if (e != cudaSuccess) {
+			cudaGetLastError();
+			set_error(err, CLO_ERROR_LIBRARY,
+				"No-allocation scan set-up failed on device %d: %s", ordinal,
+				cudaGetErrorString(e));
 			return nullptr;
 		}
 		g_noalloc_addr[ordinal] = (uint64_t *)p;
@@ -496,9 +539,15 @@ extern "C" cl_bool clo_scan_blelloch_noalloc(CCLQueue *cq, CloType elem_type,
 		set_error(err, CLO_ERROR_ARGS, "NULL input or output pointer");
 		return CL_FALSE;
 	}
-	uint64_t *scratch = noalloc_scratch(cq->ctx->ordinal, err);
+	const int ordinal = cq->ctx->ordinal;
+	if (ordinal < 0 || ordinal >= 64) {
+		set_error(err, CLO_ERROR_ARGS, "Device ordinal %d out of range", ordinal);
+		return CL_FALSE;
+	}
+	CurrentDevice dev(ordinal);
+	if (!cuda_ok(dev.status, err, "clo_scan_blelloch_noalloc: cudaSetDevice")) return CL_FALSE;
+	uint64_t *scratch = noalloc_scratch(ordinal, err);
 	if (!scratch) return CL_FALSE;
-	cudaSetDevice(cq->ctx->ordinal);
 	const int ob = (int)clo_type_sizeof(sum_type);
 	int *st = cq->ctx->d_status;
 	const int sms = cq->ctx->sm_count;

@@ -79,9 +79,14 @@ int clo_gb300_timing_get(const char *kernel, double *total_ms,
  * most 2^28 elements (1 MiB, held on every GPU that loads the library
  * until the process exits). Larger numel is rejected with CLO_ERROR_ARGS.
  *
- * The first call on a device looks the array's device address up
- * (cudaGetSymbolAddress, with that device current); make that first call
- * before any stream capture. Every call clears the part of the array it
+ * The first call on a device does all of the entry point's set-up for
+ * that device: it looks the array's device address up
+ * (cudaGetSymbolAddress, with that device current) and prepares the scan
+ * kernel for every element and sum type, so later calls with any type
+ * pair do no set-up work. Make that first call before any stream
+ * capture. Each call makes the queue's device current for its duration
+ * and restores the caller's current device before it returns. Every call
+ * clears the part of the array it
  * uses, on cq's stream, before the scan; all calls share the one array,
  * so calls whose work overlaps on the GPU (different streams, no ordering
  * between them) race and give wrong results. Asynchronous on cq: no event

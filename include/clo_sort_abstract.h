@@ -44,8 +44,10 @@ extern const CloSortImplDef clo_sort_satradix_def;
  * macro bodies. NULL selects the defaults "((a) > (b))" and "(x)". The
  * compiled-in kernels implement the defaults; "satradix" ignores
  * `compare` exactly as the reference does (it always sorts ascending by
- * the key's unsigned bit pattern). Other snippets are rejected with
- * CLO_ERROR_ARGS. */
+ * the key's unsigned bit pattern). Other snippets are compiled, as the
+ * reference compiles its program per sorter, into a per-sorter CUDA
+ * program (NVRTC, for this device) that clo_sort_get_program returns; a
+ * snippet that does not compile is reported as CLO_ERROR_LIBRARY. */
 CloSort *clo_sort_new(const char *type, const char *options,
 	CCLContext *ctx, CloType *elem_type, CloType *key_type,
 	const char *compare, const char *get_key, const char *compiler_opts,

@@ -7,12 +7,16 @@ Nothing of the reference is copied into the repository: the kernel text
 is read at build time, rewritten mechanically (OpenCL qualifiers removed,
 vector literals turned into constructor calls, work-group-local
 declarations given per-thread static storage) and written only under
-oracle/_ref/ (git-ignored). Without the reference tree the build is
-skipped and the callers skip the live comparisons; the committed
-known-answer digests (tests/golden/) were produced from this library.
+oracle/_ref/ (git-ignored). The generated units stay in oracle/_ref/gen/,
+so a machine without the reference tree that received a copy of them
+(a checkout copied together with its git-ignored build outputs) compiles
+them as they are. With neither, the build is skipped and the callers skip
+the live comparisons; the committed known-answer digests (tests/golden/)
+were produced from this library.
 
-Usage: python oracle/build_ref.py [--force]
-Reference location: $CLO_REFERENCE_ROOT, default /root/reference.
+Usage: python oracle/build_ref.py [--force] [--reference DIR]
+Reference location: --reference, else $CLO_REFERENCE_ROOT, else the
+directory named "reference" beside the repository checkout.
 """
 import concurrent.futures as cf
 import os
@@ -53,8 +57,14 @@ CUSTOM = [(5, 5, "((a) < (b))", "(x)"),
           (9, 9, "((a) < (b))", "(x)")]
 
 
+_ROOT_OVERRIDE = None
+
+
 def ref_root():
-    return pathlib.Path(os.environ.get("CLO_REFERENCE_ROOT", "/root/reference"))
+    if _ROOT_OVERRIDE is not None:
+        return pathlib.Path(_ROOT_OVERRIDE)
+    env = os.environ.get("CLO_REFERENCE_ROOT")
+    return pathlib.Path(env) if env else HERE.parent.parent / "reference"
 
 
 def to_cxx(text):
@@ -150,23 +160,27 @@ def units():
 
 
 def build(force=False):
-    """Returns the library path, or None without the reference tree."""
-    if not (ref_root() / "src" / "cl_ops").is_dir():
-        return LIB if LIB.exists() else None
-    GEN.mkdir(parents=True, exist_ok=True)
-    srcs = []
-    for name, text in units().items():
-        p = GEN / f"{name}.cpp"
-        if not p.exists() or p.read_text() != text:
-            p.write_text(text)
-        srcs.append(p)
+    """Returns the library path, or None without the reference tree and
+    without previously generated units."""
+    if (ref_root() / "src" / "cl_ops").is_dir():
+        GEN.mkdir(parents=True, exist_ok=True)
+        srcs = []
+        for name, text in units().items():
+            p = GEN / f"{name}.cpp"
+            if not p.exists() or p.read_text() != text:
+                p.write_text(text)
+            srcs.append(p)
+    else:
+        srcs = sorted(GEN.glob("*.cpp")) if GEN.is_dir() else []
+        if not srcs:
+            return LIB if LIB.exists() else None
     srcs.append(SHIM / "clc_runner.cpp")
     shim_time = max(q.stat().st_mtime for q in SHIM.iterdir())
     if LIB.exists() and not force and all(
             LIB.stat().st_mtime > max(q.stat().st_mtime, shim_time) for q in srcs):
         return LIB
     cxx = shutil.which("g++") or "g++"
-    flags = ["-O1", "-std=c++17", "-fPIC", "-w", f"-I{SHIM}"]
+    flags = ["-O1", "-std=c++17", "-fPIC", "-pthread", "-w", f"-I{SHIM}"]
 
     def comp(src):
         obj = GEN / (src.stem + ".o")
@@ -175,9 +189,11 @@ def build(force=False):
 
     with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
         objs = list(ex.map(comp, srcs))
-    subprocess.run([cxx, "-shared", "-o", str(LIB), *map(str, objs)], check=True)
+    subprocess.run([cxx, "-shared", "-pthread", "-o", str(LIB), *map(str, objs)], check=True)
     return LIB
 
 
 if __name__ == "__main__":
+    if "--reference" in sys.argv:
+        _ROOT_OVERRIDE = sys.argv[sys.argv.index("--reference") + 1]
     print(build(force="--force" in sys.argv))

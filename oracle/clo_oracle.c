@@ -6,6 +6,7 @@
  * it, as the checker; the library never links it. See clo_oracle.h for
  * the per-function reference citations.
  */
+#define _POSIX_C_SOURCE 200809L /* pthread barriers under -std=c11 */
 #include "clo_oracle.h"
 
 #include <math.h>
@@ -116,6 +117,119 @@ DEFINE_BITONIC(bit_u64, uint64_t, PLAIN_GT, UINT64_MAX)
 DEFINE_BITONIC(bit_f16, uint16_t, HALF_GT, 0x7c00)
 DEFINE_BITONIC(bit_f32, float, PLAIN_GT, INFINITY)
 DEFINE_BITONIC(bit_f64, double, PLAIN_GT, INFINITY)
+
+/* The same network replayed by host threads, for full-size checks. A step
+ * is N/2 independent compare-exchanges, split over the threads by gid
+ * range; once a stage's stride is below half a block of kBitBlock
+ * elements, every remaining step of the stage pairs elements inside
+ * aligned blocks, so each thread runs those steps block by block (a
+ * block's gids are [b B/2, (b + 1) B/2)). Every pair is compared in the
+ * same step order as the serial replay, so the results are identical. */
+#define DEFINE_BITONIC_STEP(NAME, T, GT, MAXV)                               \
+	static void NAME##_step(void *dv, size_t glo, size_t ghi, int stage,      \
+		int step) {                                                           \
+		T *d = dv;                                                            \
+		size_t stride = (size_t)1 << (step - 1);                              \
+		for (size_t gid = glo; gid < ghi; ++gid) {                            \
+			size_t i1 = gid + (gid / stride) * stride;                        \
+			size_t i2 = i1 + stride;                                          \
+			int desc = (int)((gid >> (stage - 1)) & 1);                       \
+			T x = d[i1], y = d[i2];                                           \
+			if ((GT(x, y) ? 1 : 0) ^ desc) { d[i1] = y; d[i2] = x; }          \
+		}                                                                     \
+	}                                                                         \
+	static void NAME##_pad(void *dv, size_t from, size_t to) {               \
+		T *d = dv;                                                            \
+		for (size_t i = from; i < to; ++i) d[i] = (MAXV);                     \
+	}
+DEFINE_BITONIC_STEP(bit_i8, int8_t, PLAIN_GT, INT8_MAX)
+DEFINE_BITONIC_STEP(bit_u8, uint8_t, PLAIN_GT, UINT8_MAX)
+DEFINE_BITONIC_STEP(bit_i16, int16_t, PLAIN_GT, INT16_MAX)
+DEFINE_BITONIC_STEP(bit_u16, uint16_t, PLAIN_GT, UINT16_MAX)
+DEFINE_BITONIC_STEP(bit_i32, int32_t, PLAIN_GT, INT32_MAX)
+DEFINE_BITONIC_STEP(bit_u32, uint32_t, PLAIN_GT, UINT32_MAX)
+DEFINE_BITONIC_STEP(bit_i64, int64_t, PLAIN_GT, INT64_MAX)
+DEFINE_BITONIC_STEP(bit_u64, uint64_t, PLAIN_GT, UINT64_MAX)
+DEFINE_BITONIC_STEP(bit_f16, uint16_t, HALF_GT, 0x7c00)
+DEFINE_BITONIC_STEP(bit_f32, float, PLAIN_GT, INFINITY)
+DEFINE_BITONIC_STEP(bit_f64, double, PLAIN_GT, INFINITY)
+
+typedef void (*BitStepFn)(void *, size_t, size_t, int, int);
+typedef void (*BitPadFn)(void *, size_t, size_t);
+static const BitStepFn kBitStep[11] = {bit_i8_step, bit_u8_step, bit_i16_step,
+	bit_u16_step, bit_i32_step, bit_u32_step, bit_i64_step, bit_u64_step, bit_f16_step,
+	bit_f32_step, bit_f64_step};
+static const BitPadFn kBitPad[11] = {bit_i8_pad, bit_u8_pad, bit_i16_pad, bit_u16_pad,
+	bit_i32_pad, bit_u32_pad, bit_i64_pad, bit_u64_pad, bit_f16_pad, bit_f32_pad,
+	bit_f64_pad};
+static const int kBitSize[11] = {1, 1, 2, 2, 4, 4, 8, 8, 2, 4, 8};
+#define kBitBlock ((size_t)1 << 14)
+
+typedef struct {
+	void *d;
+	size_t N, B;
+	int logN, t, threads;
+	BitStepFn step;
+	pthread_barrier_t *bar;
+} BitJob;
+
+static void *bitonic_job(void *arg) {
+	BitJob *j = arg;
+	const size_t half = j->N / 2, T = (size_t)j->threads, t = (size_t)j->t;
+	const size_t blocks = j->N / j->B;
+	for (int stage = 1; stage <= j->logN; ++stage) {
+		int step = stage;
+		for (; step >= 1 && ((size_t)1 << step) > j->B; --step) {
+			j->step(j->d, half * t / T, half * (t + 1) / T, stage, step);
+			pthread_barrier_wait(j->bar);
+		}
+		if (step >= 1) {
+			for (size_t b = blocks * t / T; b < blocks * (t + 1) / T; ++b)
+				for (int s = step; s >= 1; --s)
+					j->step(j->d, b * (j->B / 2), (b + 1) * (j->B / 2), stage, s);
+			pthread_barrier_wait(j->bar);
+		}
+	}
+	return NULL;
+}
+
+void oracle_bitonic_sort_threaded(void *data, size_t n, int type, int threads) {
+	if (n < 2 || type < 0 || type > 10) return;
+	if (threads < 1) threads = 1;
+	if (threads > 256) threads = 256;
+	const size_t es = (size_t)kBitSize[type];
+	size_t N = 1;
+	int logN = 0;
+	while (N < n) { N <<= 1; logN++; }
+	unsigned char *d = data;
+	if (N != n) {
+		d = malloc(N * es);
+		memcpy(d, data, n * es);
+		kBitPad[type](d, n, N);
+	}
+	pthread_barrier_t bar;
+	pthread_barrier_init(&bar, NULL, (unsigned)threads);
+	BitJob jobs[256];
+	pthread_t th[256];
+	for (int t = 0; t < threads; ++t) {
+		jobs[t].d = d;
+		jobs[t].N = N;
+		jobs[t].B = N < kBitBlock ? N : kBitBlock;
+		jobs[t].logN = logN;
+		jobs[t].t = t;
+		jobs[t].threads = threads;
+		jobs[t].step = kBitStep[type];
+		jobs[t].bar = &bar;
+		if (t > 0) pthread_create(&th[t], NULL, bitonic_job, &jobs[t]);
+	}
+	bitonic_job(&jobs[0]);
+	for (int t = 1; t < threads; ++t) pthread_join(th[t], NULL);
+	pthread_barrier_destroy(&bar);
+	if (d != (unsigned char *)data) {
+		memcpy(data, d, n * es);
+		free(d);
+	}
+}
 
 void oracle_bitonic_sort(void *data, size_t n, int type) {
 	if (n < 2) return;

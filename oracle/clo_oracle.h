@@ -26,6 +26,10 @@ void oracle_radix_sort(void *keys, void *vals, size_t n, int key_bytes,
  * (key1 > key2) XOR desc. N = next power of two of n; the missing
  * elements are the type's maximum. In place. */
 void oracle_bitonic_sort(void *data, size_t n, int type);
+/* The same replay by `threads` host threads (identical results): steps
+ * split by gid range, the short-stride steps of each stage run block by
+ * block. For full-size checks. */
+void oracle_bitonic_sort_threaded(void *data, size_t n, int type, int threads);
 
 /* Rank-by-counting sort (src/cl_ops/sort/clo_sort_gselect.cl:38-57):
  * out[#{i : k_g > k_i || (k_i == k_g && i < g)}] = in[g]. */

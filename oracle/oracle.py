@@ -24,6 +24,7 @@ def lib():
         P, SZ = C.c_void_p, C.c_size_t
         _lib.oracle_radix_sort.argtypes = [P, P, SZ, C.c_int, C.c_int, C.c_int]
         _lib.oracle_bitonic_sort.argtypes = [P, SZ, C.c_int]
+        _lib.oracle_bitonic_sort_threaded.argtypes = [P, SZ, C.c_int, C.c_int]
         _lib.oracle_gselect_sort.argtypes = [P, P, SZ, C.c_int, P, P, C.c_int]
         _lib.oracle_scan.argtypes = [P, P, SZ, C.c_int, C.c_int]
         _lib.oracle_rng_init_gid.argtypes = [P, SZ, C.c_int, C.c_uint64, C.c_int]
@@ -82,6 +83,15 @@ def seg_scan(a, offsets, in_type, out_dtype, out_init=None):
 def bitonic_sort(a, clo_type):
     d = np.ascontiguousarray(a).copy()
     lib().oracle_bitonic_sort(_p(d), d.size, clo_type)
+    return d
+
+
+def bitonic_sort_threaded(a, clo_type, threads=None):
+    """bitonic_sort's network replayed by host threads (same result)."""
+    import os
+    d = np.ascontiguousarray(a).copy()
+    lib().oracle_bitonic_sort_threaded(_p(d), d.size, clo_type,
+                                       threads or os.cpu_count() or 1)
     return d
 
 

@@ -21,6 +21,7 @@
 #include <string.h>
 
 #include <functional>
+#include <vector>
 
 typedef unsigned char uchar;
 typedef signed char schar;
@@ -92,8 +93,24 @@ void barrier(int flags);
 /* Runs fn once per work-item of an NDRange of gws items in groups of lws
  * (gws a multiple of lws). local_init, when given, is called once per
  * group before its work-items start (to reset __local storage). Returns
- * false if the work-items of a group disagreed on barriers. */
+ * false if the work-items of a group disagreed on barriers.
+ *
+ * Work-groups are independent (OpenCL gives them no order), so they are
+ * spread over clc_workers() host threads, each running its groups one at a
+ * time; __local buffers that a driver passes as kernel arguments must be
+ * per worker (ClcLocal below). CLC_THREADS sets the worker count (default:
+ * the hardware threads). */
 bool clc_run(size_t gws, size_t lws, const std::function<void()> &fn,
 	const std::function<void()> &local_init = nullptr);
+size_t clc_workers();
+size_t clc_worker(); /* index of the calling worker, 0 outside clc_run */
+
+/* One __local buffer per worker: get() is the calling worker's copy. */
+template <typename T>
+struct ClcLocal {
+	std::vector<std::vector<T>> bufs;
+	explicit ClcLocal(size_t n) : bufs(clc_workers(), std::vector<T>(n)) {}
+	T *get() { return bufs[clc_worker()].data(); }
+};
 
 #endif

@@ -2,6 +2,7 @@
 reference's error codes, kernel introspection, wrapper bookkeeping, the
 bounded-wait watchdog, and full-size property checks."""
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
@@ -153,24 +154,7 @@ def test_lookback_watchdog_reports_and_context_survives(clops, ctx, queue):
         x.destroy()
 
 
-# ----------------------------------------------- full-size property checks
-@pytest.mark.slow
-def test_satradix_2pow28_u32_sorted_permutation(clops, ctx, queue):
-    n = 1 << 28
-    a = keys_u32(42, n)
-    s = clops.Sorter(ctx, "satradix", 5)
-    b = clops.Buffer.from_array(ctx, queue, a)
-    clops.wait(s.sort_device(queue, b, n))
-    got = b.read(queue, np.uint32, n)
-    assert np.all(got[1:] >= got[:-1])
-    # Same multiset: per-bucket counts of the top 16 bits and the 64-bit sum.
-    assert int(got.astype(np.uint64).sum()) == int(a.astype(np.uint64).sum())
-    np.testing.assert_array_equal(np.bincount(got >> 16, minlength=1 << 16),
-                                  np.bincount(a >> 16, minlength=1 << 16))
-    b.destroy()
-    s.destroy()
-
-
+# ----------------------------------------------- full-size checks
 @pytest.mark.slow
 def test_satradix_5x2pow27_keys_many_tile_waves(clops, ctx, queue):
     """5 x 2^27 + 777 keys: about 47k tiles with a ragged last one, run in
@@ -182,10 +166,8 @@ def test_satradix_5x2pow27_keys_many_tile_waves(clops, ctx, queue):
     b = clops.Buffer.from_array(ctx, queue, a)
     clops.wait(s.sort_device(queue, b, n))
     got = b.read(queue, np.uint32, n)
-    assert np.all(got[1:] >= got[:-1])
-    assert int(got.astype(np.uint64).sum()) == int(a.astype(np.uint64).sum())
-    np.testing.assert_array_equal(np.bincount(got >> 16, minlength=1 << 16),
-                                  np.bincount(a >> 16, minlength=1 << 16))
+    np.testing.assert_array_equal(
+        got, oracle.radix_sort_u32_threaded(a.copy(), os.cpu_count() or 1, 8))
     b.destroy()
     s.destroy()
 
@@ -205,21 +187,4 @@ def test_satradix_kv_2pow27_stable_permutation(clops, ctx, queue):
     same = gk[1:] == gk[:-1]
     assert np.all(gv[1:][same] > gv[:-1][same])  # stable
     for x in (kb, vb, s):
-        x.destroy()
-
-
-@pytest.mark.slow
-def test_scan_2pow30_checksums(clops, ctx, queue):
-    n = 1 << 30
-    a = (splitmix64(45, n) >> np.uint64(56)).astype(np.uint32)
-    sc = clops.Scanner(ctx, 5, 7)
-    bi = clops.Buffer.from_array(ctx, queue, a)
-    bo = clops.Buffer(ctx, n * 8)
-    clops.wait(sc.scan_device(queue, bi, bo, n))
-    got = bo.read(queue, np.uint64, n)
-    # Differences recover the input; the last value is the total minus the last.
-    np.testing.assert_array_equal(np.diff(got), a[:-1].astype(np.uint64))
-    assert int(got[0]) == 0
-    assert int(got[-1]) + int(a[-1]) == int(a.astype(np.uint64).sum())
-    for x in (bi, bo, sc):
         x.destroy()

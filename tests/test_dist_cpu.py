@@ -61,7 +61,7 @@ def test_reference_arm_under_torchrun_two_ranks():
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port),
            str(ROOT / "bench.py"), "--impl", "reference", "--gpus", "2",
-           "--steps", "1", "--warmup", "0"]
+           "--steps", "1", "--warmup", "0", "--log2n", "20"]
     out = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=900)
     assert out.returncode == 0, out.stderr[-3000:]
     lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]

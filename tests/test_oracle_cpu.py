@@ -89,6 +89,21 @@ def test_bitonic_oracle_sorts_and_replays_network(code, dt):
                                       ref.view(f"u{a.dtype.itemsize}"))
 
 
+@pytest.mark.parametrize("code,dt", INT_TYPES + [(9, np.float32), (10, np.float64), (8, np.float16)])
+def test_threaded_bitonic_equals_serial_replay(code, dt):
+    """The threaded replay (gid-range steps, block-local short strides)
+    gives the serial replay's bytes, NaN and signed-zero orders included,
+    on sizes below, at and above the block and ragged ones (padding)."""
+    for n in (1, 3, 1000, (1 << 14) + 3, 1 << 16, 100003):
+        a = keys_of_type(77 + n, n, dt)
+        if np.issubdtype(dt, np.floating):
+            a[::97] = np.nan
+            a[::101] = -0.0
+        for threads in (1, 3, 8):
+            got = oracle.bitonic_sort_threaded(a, code, threads)
+            assert got.tobytes() == oracle.bitonic_sort(a, code).tobytes(), (n, threads)
+
+
 @pytest.mark.parametrize("code,dt", INT_TYPES + [(9, np.float32)])
 def test_gselect_oracle_is_stable_sort(code, dt):
     for n in (1, 5, 300):

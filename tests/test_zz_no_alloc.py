@@ -13,6 +13,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
+import oracle
 from inputs import splitmix64
 
 pytestmark = pytest.mark.gpu
@@ -26,17 +27,21 @@ def _noalloc(clops):
     return f
 
 
-@pytest.mark.parametrize("in_type,in_dt,sum_type,sum_dt", [
-    (5, np.uint32, 7, np.uint64),   # uint -> ulong
-    (0, np.int8, 5, np.uint32),     # char -> uint
+@pytest.mark.parametrize("in_type,in_dt,sum_type,sum_dt,first_n", [
+    (5, np.uint32, 7, np.uint64, 1 << 28),        # uint -> ulong, every scratch slot
+    (0, np.int8, 5, np.uint32, (1 << 20) + 7),    # char -> uint
 ])
-def test_noalloc_scan_matches_allocating_scan_twice(clops, in_type, in_dt, sum_type, sum_dt):
+def test_noalloc_scan_matches_allocating_scan_twice(clops, in_type, in_dt, sum_type, sum_dt,
+                                                    first_n):
     f = _noalloc(clops)
     ctx = clops.Context(0)
     q = clops.Queue(ctx)
     try:
-        # Two calls in a row: the first uses more tiles than the second.
-        for n, seed in (((1 << 20) + 7, 45), (123457, 46)):
+        # Two calls in a row: the first uses more tiles than the second (at
+        # 2^28 elements, all 2^15 tile slots of the scratch, the last one
+        # beside the tile counter). Each result must equal the allocating
+        # entry point's and the oracle's serial scan.
+        for n, seed in ((first_n, 45), (123457, 46)):
             raw = splitmix64(seed, n) >> np.uint64(40)
             a = raw.astype(np.uint64).astype(in_dt) if in_dt != np.int8 else \
                 (raw & np.uint64(0xFF)).astype(np.uint8).view(np.int8)
@@ -48,7 +53,9 @@ def test_noalloc_scan_matches_allocating_scan_twice(clops, in_type, in_dt, sum_t
             ok = clops.call(f, q.h, in_type, sum_type, bi.ptr, got.ptr, n)
             assert ok == 1
             q.finish()
-            np.testing.assert_array_equal(got.read(q, sum_dt, n), ref.read(q, sum_dt, n))
+            out = got.read(q, sum_dt, n)
+            np.testing.assert_array_equal(out, ref.read(q, sum_dt, n))
+            np.testing.assert_array_equal(out, oracle.scan(a, in_type, sum_dt))
             for x in (bi, ref, got, sc):
                 x.destroy()
         # Beyond the static scratch: rejected before any device work.
