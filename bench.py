@@ -507,51 +507,71 @@ def run_suite(clops, ctx, q, args, only=None):
             x.destroy()
 
     def serve():
-        """Open-loop serving: Poisson arrivals at 20k requests/s (seed 49),
-        60 % sort / 30 % scan / 10 % random fill, n log-uniform in
-        [2^10, 2^26], uint / ulong 50/50, 120 GB admission budget. Primary:
-        device-resident buffers (requests read slices of a 4 GiB device pool
-        and write their own slices of a 48 GiB device output ring), against
-        the same requests as serial plain device-data calls. Secondary: the
-        same requests on host buffers (page-locked pools), against serial
-        plain host-data calls."""
+        """Open-loop serving: Poisson arrivals (seed 49), 60 % sort / 30 %
+        scan / 10 % random fill, n log-uniform in [2^10, 2^26], uint / ulong
+        50/50, 120 GB admission budget, --serve-seconds of arrivals (10 s by
+        default). Device-resident buffers (requests read slices of a 4 GiB
+        device pool and write their own slices of a 48 GiB device output
+        ring):
+          * at 20k requests/s (offered far above capacity: the aggregate
+            is the server's capacity), against the same requests as serial
+            plain device-data calls;
+          * at a load the server sustains (the same request sequence with
+            arrivals stretched to offer about 25 Gelem/s), so p50/p99 are
+            service latency, against the same arrivals served one request
+            at a time on one stream with batching off (serial plain calls
+            behind the same queue).
+        Host buffers (page-locked pools): at a sustainable load (about
+        8 Gelem/s) for the same duration, and at 20k requests/s for 2 s
+        against serial plain host-data calls. Each run reports how many
+        batches were in flight on the device at once."""
         dur = args.serve_seconds
-        rate = 20000.0
+        base_rate = 20000.0
         u = splitmix64(49, 1 << 22)
         with np.errstate(divide="ignore"):
             gaps = -np.log(np.maximum((u[0::8] >> np.uint64(11)).astype(np.float64)
-                                      / float(1 << 53), 1e-300)) / rate
-        arrivals = np.cumsum(gaps)
-        count = int(np.searchsorted(arrivals, dur))
-        arrivals = arrivals[:count]
-        kind = (u[1::8][:count] % np.uint64(10)).astype(np.int64)
-        logn = 10.0 + 16.0 * (u[2::8][:count] >> np.uint64(11)).astype(np.float64) / float(1 << 53)
+                                      / float(1 << 53), 1e-300)) / base_rate
+        base_arrivals = np.cumsum(gaps)
+        kind = (u[1::8] % np.uint64(10)).astype(np.int64)
+        logn = 10.0 + 16.0 * (u[2::8] >> np.uint64(11)).astype(np.float64) / float(1 << 53)
         nreq = np.minimum(np.exp2(logn).astype(np.int64), 1 << 26)
-        wide = (u[3::8][:count] & np.uint64(1)).astype(bool)
-        pos_in = u[4::8][:count]
-        pos_out = u[5::8][:count]
+        wide = (u[3::8] & np.uint64(1)).astype(bool)
+        pos_in = u[4::8]
+        pos_out = u[5::8]
         # (op, type / generator, sum type, n or states, draws, in bytes, out bytes)
-        specs, elems = [], 0.0
-        for i in range(count):
+        specs, elems_of = [], []
+        for i in range(base_arrivals.size):
             n = int(nreq[i])
             if kind[i] < 6:
                 code, eb = (clops.CLO_ULONG, 8) if wide[i] else (clops.CLO_UINT, 4)
                 specs.append((clops.SERVE_SORT, code, 0, n, 0, n * eb, n * eb))
-                elems += n
+                elems_of.append(n)
             elif kind[i] < 9:
                 code, eb = (clops.CLO_ULONG, 8) if wide[i] else (clops.CLO_UINT, 4)
                 specs.append((clops.SERVE_SCAN, code, clops.CLO_ULONG, n, 0, n * eb, n * 8))
-                elems += n
+                elems_of.append(n)
             else:
                 g, st, dr = i % 5, max(1, n // 16), 16
                 specs.append((clops.SERVE_RNG_FILL, g, 0, st, dr,
                               st * clops.RNG_SEED_SIZE[clops.RNG_NAMES[g]], st * dr * 4))
-                elems += st * dr
+                elems_of.append(st * dr)
+        elems_of = np.array(elems_of, dtype=np.float64)
+        mean_rate_elems = elems_of.mean() * base_rate  # offered elem/s at 20k req/s
+
+        def window(offered_gelem, seconds):
+            """Arrivals offering about offered_gelem Gelem/s (None: 20k
+            requests/s) over `seconds`: (arrival times, request count)."""
+            scale = 1.0 if offered_gelem is None else mean_rate_elems / (offered_gelem * 1e9)
+            arr = base_arrivals * scale
+            count = int(np.searchsorted(arr, seconds))
+            return arr[:count], count
+
         block = splitmix64(149, 1 << 26).view(np.uint8)  # 512 MiB of random bytes
 
-        def make(pool_in, pool_bytes, out_addr, device):
+        def make(count, pool_in, pool_bytes, out_addr, device):
             reqs = []
-            for i, (op, code, sc, n, dr, span_in, span_out) in enumerate(specs):
+            for i in range(count):
+                op, code, sc, n, dr, span_in, span_out = specs[i]
                 a = pool_in + int(pos_in[i] % np.uint64((pool_bytes - span_in) // 16)) * 16
                 bo = out_addr(i, span_out)
                 if op == clops.SERVE_RNG_FILL:
@@ -562,8 +582,9 @@ def run_suite(clops, ctx, q, args, only=None):
                                                      device=device))
             return reqs
 
-        def served(reqs):
-            srv = clops.Server(ctx, 120 << 30, streams=4)
+        def served(reqs, arrivals, streams=4, max_batch=4096):
+            srv = clops.Server(ctx, 120 << 30, streams=streams)
+            srv.configure(max_batch=max_batch)
             for r in reqs[:64]:  # warm-up: a few requests of each kind
                 srv.submit(r)
             srv.drain()
@@ -642,21 +663,28 @@ def run_suite(clops, ctx, q, args, only=None):
                     break
             return done_el / (time.perf_counter() - t0)
 
-        def report(st_, serial, buffers):
+        def report(st_, count, seconds, buffers, serial=None):
             agg = st_["elements"] / st_["span_s"] if st_["span_s"] else 0.0
-            return {
-                "buffers": buffers, "open_loop_s": dur, "offered_req_per_s": rate,
-                "requests": count, "offered_Gelem_per_s": round(elems / dur / 1e9, 2),
+            offered = float(elems_of[:count].sum())
+            out = {
+                "buffers": buffers, "open_loop_s": seconds,
+                "offered_req_per_s": round(count / seconds, 1), "requests": count,
+                "offered_Gelem_per_s": round(offered / seconds / 1e9, 2),
                 "submitted": st_["submitted"], "admitted": st_["admitted"],
                 "completed": st_["completed"], "rejected": st_["rejected"],
                 "batches": st_["batches"], "max_queued": st_["max_queued"],
                 "peak_budget_GB": round(st_["peak_bytes"] / 1e9, 2),
-                "budget_GB": 120 * 1.073741824,
+                "budget_GB": round(120 * 1.073741824, 2),
                 "p50_ms": round(st_["p50_ms"], 2), "p99_ms": round(st_["p99_ms"], 2),
                 "mean_ms": round(st_["mean_ms"], 2), "span_s": round(st_["span_s"], 3),
                 "aggregate_Gelem_per_s": round(agg / 1e9, 3),
-                "serial_plain_Gelem_per_s": round(serial / 1e9, 3),
-                "speedup_vs_serial_plain": round(agg / serial, 2) if serial else None}
+                "batches_in_flight_max": int(st_["max_concurrent_batches"]),
+                "batches_in_flight_mean": round(st_["mean_concurrent_batches"], 2),
+                "device_busy_s": round(st_["device_busy_s"], 3)}
+            if serial is not None:
+                out["serial_plain_Gelem_per_s"] = round(serial / 1e9, 3)
+                out["speedup_vs_serial_plain"] = round(agg / serial, 2) if serial else None
+            return out
 
         # Device-resident buffers.
         dpool = 4 << 30
@@ -675,8 +703,23 @@ def run_suite(clops, ctx, q, args, only=None):
             at = dout.ptr + cursor[0]
             cursor[0] += span
             return at
-        dreqs = make(din.ptr, dpool, ring_slot, True)
-        dev_res = report(served(dreqs), serial_device(dreqs), "device-resident")
+        arr, count = window(None, dur)
+        dreqs = make(count, din.ptr, dpool, ring_slot, True)
+        dev_res = report(served(dreqs, arr), count, dur, "device-resident",
+                         serial_device(dreqs))
+        arr, count = window(25.0, dur)
+        dreqs = dreqs[:count] if count <= len(dreqs) else \
+            make(count, din.ptr, dpool, ring_slot, True)
+        sus = report(served(dreqs, arr), count, dur, "device-resident")
+        one = report(served(dreqs, arr, streams=1, max_batch=1), count, dur,
+                     "device-resident, one stream, batching off")
+        sus["serial_plain_same_arrivals"] = {
+            k: one[k] for k in ("p50_ms", "p99_ms", "mean_ms", "aggregate_Gelem_per_s",
+                                "max_queued", "span_s", "batches_in_flight_max")}
+        sus["p50_speedup_vs_serial_plain"] = round(one["p50_ms"] / sus["p50_ms"], 2) \
+            if sus["p50_ms"] else None
+        sus["p99_speedup_vs_serial_plain"] = round(one["p99_ms"] / sus["p99_ms"], 2) \
+            if sus["p99_ms"] else None
         din.destroy()
         dout.destroy()
 
@@ -687,16 +730,26 @@ def run_suite(clops, ctx, q, args, only=None):
         pin = np.ctypeslib.as_array((clops.C.c_uint8 * pool_bytes).from_address(hin))
         for o in range(0, pool_bytes, block.size):
             pin[o:o + block.size] = block
-        hreqs = make(hin, pool_bytes, lambda i, span: hout + int(
-            pos_out[i] % np.uint64((pool_bytes - span) // 16)) * 16, False)
-        host_res = report(served(hreqs), serial_host(hreqs), "host (page-locked)")
+
+        def host_out(i, span):
+            return hout + int(pos_out[i] % np.uint64((pool_bytes - span) // 16)) * 16
+        arr, count = window(8.0, dur)
+        hreqs = make(count, hin, pool_bytes, host_out, False)
+        host_sus = report(served(hreqs, arr), count, dur, "host (page-locked)")
+        hsec = min(dur, 2.0)
+        arr, count = window(None, hsec)
+        hreqs = make(count, hin, pool_bytes, host_out, False)
+        host_res = report(served(hreqs, arr), count, hsec, "host (page-locked)",
+                          serial_host(hreqs))
         for x in list(sorters.values()) + list(scanners.values()):
             x.destroy()
         del pin
         clops.lib.clo_host_free(hin)
         clops.lib.clo_host_free(hout)
         res["serve_poisson_20k"] = dev_res
+        res["serve_sustained_25Gelem"] = sus
         res["serve_poisson_20k_host_buffers"] = host_res
+        res["serve_sustained_8Gelem_host_buffers"] = host_sus
 
     def c1_c3():
         """C1: 2^20 uint32 keys with the reference's radix=16 option
@@ -877,7 +930,7 @@ def main():
     ap.add_argument("--no-suite", dest="suite", action="store_false")
     ap.add_argument("--no-ref-kernels", dest="ref_kernels", action="store_false",
                     help="skip timing the reference's own kernels at 2^20 keys")
-    ap.add_argument("--serve-seconds", type=float, default=1.0,
+    ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="open-loop duration of the serving workload")
     ap.add_argument("--only", choices=["abitonic", "kv", "scan", "rng", "segmented", "serve",
                                        "c1c3"],

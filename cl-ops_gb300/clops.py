@@ -67,7 +67,9 @@ class ServeStats(C.Structure):
                                          "rejected", "batches", "max_queued")] + \
                [("budget_bytes", C.c_size_t), ("peak_bytes", C.c_size_t)] + \
                [(f, C.c_double) for f in ("p50_ms", "p99_ms", "max_ms", "mean_ms",
-                                         "elements", "span_s")]
+                                         "elements", "span_s")] + \
+               [("max_concurrent_batches", C.c_uint64), ("device_busy_s", C.c_double),
+                ("mean_concurrent_batches", C.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -133,6 +135,18 @@ _SIGS = {
     "ccl_enqueue_marker": (P, [P, P, PERR]),
     "ccl_event_elapsed_ns": (U64, [P, P, PERR]),
     "ccl_program_get_source": (C.c_char_p, [P]),
+    "ccl_program_new_from_source": (P, [P, C.c_char_p, PERR]),
+    "ccl_program_new_from_sources": (P, [P, U32, C.POINTER(C.c_char_p), C.POINTER(SZ), PERR]),
+    "ccl_program_build": (U32, [P, C.c_char_p, PERR]),
+    "ccl_program_get_build_log": (C.c_char_p, [P, PERR]),
+    "ccl_program_get_kernel": (P, [P, C.c_char_p, PERR]),
+    "ccl_program_destroy": (None, [P]),
+    "ccl_arg_new": (P, [P, SZ]),
+    "ccl_arg_destroy": (None, [P]),
+    "ccl_kernel_suggest_worksizes": (U32, [P, P, U32, C.POINTER(SZ), C.POINTER(SZ),
+                                            C.POINTER(SZ), PERR]),
+    # variadic: the fixed part only (Program.enqueue passes the rest)
+    "ccl_kernel_set_args_and_enqueue_ndrange": (P, None),
     "ccl_program_get_build_options": (C.c_char_p, [P]),
     "ccl_wrapper_memcheck": (U32, []),
     # sort
@@ -199,6 +213,7 @@ _SIGS = {
     "clo_serve_drain": (U32, [P, PERR]),
     "clo_serve_replay": (U32, [P, C.POINTER(ServeRequest), C.POINTER(C.c_double), SZ,
                                C.POINTER(U64), PERR]),
+    "clo_serve_configure": (U32, [P, SZ, SZ, SZ, PERR]),
     "clo_serve_get_stats": (None, [P, C.POINTER(ServeStats)]),
     "clo_serve_reset_stats": (None, [P]),
     "clo_serve_destroy": (None, [P]),
@@ -455,6 +470,59 @@ class Graph:
             self.h = None
 
 
+class Program:
+    """A client program built from CUDA source (ccl_program_new_from_source
+    + ccl_program_build), e.g. around the text of Rng.source()."""
+
+    def __init__(self, ctx, src, options=None):
+        self.h = call(lib.ccl_program_new_from_source, ctx.h, src.encode())
+        try:
+            call(lib.ccl_program_build, self.h, options.encode() if options else None)
+        except CloError:
+            self.destroy()
+            raise
+
+    def kernel(self, name):
+        return call(lib.ccl_program_get_kernel, self.h, name.encode())
+
+    @staticmethod
+    def suggest(kernel, real, want_gws=False):
+        """(gws or None, lws) as ccl_kernel_suggest_worksizes gives them."""
+        r, g, l_ = SZ(real), SZ(0), SZ(0)
+        call(lib.ccl_kernel_suggest_worksizes, kernel, None, 1, C.byref(r),
+             C.byref(g) if want_gws else None, C.byref(l_))
+        return (g.value if want_gws else None), l_.value
+
+    @staticmethod
+    def enqueue(kernel, q, gws, lws, *args):
+        """Launches kernel over gws work-items in groups of lws; args are
+        Buffers or raw CCLBuffer handles (their device pointers) or
+        (ctypes type, value) pairs."""
+        items = []
+        for a in args:
+            if isinstance(a, Buffer):
+                items.append(C.c_void_p(a.h))
+            elif isinstance(a, int):  # a raw CCLBuffer handle
+                items.append(C.c_void_p(a))
+            else:
+                ct, v = a
+                val = ct(v)
+                items.append(C.c_void_p(lib.ccl_arg_new(C.byref(val), C.sizeof(val))))
+        g = SZ(gws)
+        l_ = SZ(lws) if lws else None
+        e = err_ptr()
+        evt = lib.ccl_kernel_set_args_and_enqueue_ndrange(
+            C.c_void_p(kernel), C.c_void_p(q.h), C.c_uint(1), None, C.byref(g),
+            C.byref(l_) if l_ is not None else None, None, C.byref(e), *items, None)
+        check(e, "ccl_kernel_set_args_and_enqueue_ndrange")
+        return evt
+
+    def destroy(self):
+        if self.h:
+            lib.ccl_program_destroy(self.h)
+            self.h = None
+
+
 class Rng:
     def __init__(self, ctx, q, name, seed_type, count, main_seed=0, hash=None,
                  seeds=None):
@@ -474,6 +542,10 @@ class Rng:
     @property
     def seeds_buffer(self):
         return lib.clo_rng_get_device_seeds(self.h)
+
+    def source(self):
+        """The CUDA text for client kernels (clo_rng_get_source)."""
+        return lib.clo_rng_get_source(self.h).decode()
 
     def states(self, q):
         size = lib.clo_rng_get_size(self.h)
@@ -540,6 +612,10 @@ class Server:
         tickets = (U64 * n)()
         call(lib.clo_serve_replay, self.h, arr, ts, n, tickets)
         return list(tickets)
+
+    def configure(self, small_n=1 << 20, batch_elems=1 << 26, max_batch=4096):
+        """Batching policy (clo_serve_configure); max_batch=1 turns it off."""
+        call(lib.clo_serve_configure, self.h, small_n, batch_elems, max_batch)
 
     def stats(self):
         st = ServeStats()

@@ -237,6 +237,58 @@ std::shared_ptr<JitSort> jit_sort_get(CloType elem, CloType key, const char *com
 	return js;
 }
 
+cudaLibrary_t jit_build(const std::string &src, const char *file_name,
+	const std::string &options, int ordinal, std::string *log, GError **err) {
+	Nvrtc *nv = nvrtc(err);
+	if (!nv) return nullptr;
+	std::vector<std::string> words;
+	{
+		std::string w;
+		for (char c : options) {
+			if (c == ' ' || c == '\t' || c == '\n') {
+				if (!w.empty()) words.push_back(w);
+				w.clear();
+			} else {
+				w += c;
+			}
+		}
+		if (!w.empty()) words.push_back(w);
+	}
+	std::vector<const char *> opts = {"-arch=sm_103a", "-std=c++17"};
+	for (const std::string &w : words) opts.push_back(w.c_str());
+	nvrtcProgram_t prog = nullptr;
+	std::lock_guard<std::mutex> lk(g_mu);
+	if (nv->create(&prog, src.c_str(), file_name, 0, nullptr, nullptr) != 0) {
+		set_error(err, CLO_ERROR_LIBRARY, "nvrtcCreateProgram failed");
+		return nullptr;
+	}
+	const int rc = nv->compile(prog, (int)opts.size(), opts.data());
+	size_t ls = 0;
+	nv->log_size(prog, &ls);
+	std::string text(ls, '\0');
+	if (ls) nv->log(prog, &text[0]);
+	if (log) *log = text.c_str();
+	if (rc != 0) {
+		nv->destroy(&prog);
+		set_error(err, CLO_ERROR_LIBRARY, "Program build failed:\n%s", text.c_str());
+		return nullptr;
+	}
+	size_t cs = 0;
+	nv->cubin_size(prog, &cs);
+	std::vector<char> cubin(cs);
+	nv->cubin(prog, cubin.data());
+	nv->destroy(&prog);
+	cudaLibrary_t lib = nullptr;
+	cudaError_t e = cudaSetDevice(ordinal);
+	if (e == cudaSuccess)
+		e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+	if (e != cudaSuccess) {
+		cuda_ok(e, err, "loading the built program");
+		return nullptr;
+	}
+	return lib;
+}
+
 cudaError_t jit_launch(cudaKernel_t k, size_t work, void **args, cudaStream_t s,
 	int sm_count) {
 	size_t blocks = (work + 255) / 256;

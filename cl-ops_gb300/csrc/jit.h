@@ -28,6 +28,12 @@ std::string jit_sort_source(CloType elem, CloType key, const char *compare,
 std::shared_ptr<JitSort> jit_sort_get(CloType elem, CloType key, const char *compare,
 	const char *get_key, int ordinal, GError **err);
 
+// Compiles CUDA source text with NVRTC for sm_103a (plus `options`,
+// whitespace-separated) and loads it on device `ordinal`. On a compile
+// error, *log (when given) receives NVRTC's log and err says why.
+cudaLibrary_t jit_build(const std::string &src, const char *file_name,
+	const std::string &options, int ordinal, std::string *log, GError **err);
+
 // Grid-stride launch of a JIT kernel over `work` items, 256 threads.
 cudaError_t jit_launch(cudaKernel_t k, size_t work, void **args, cudaStream_t s,
 	int sm_count);

@@ -67,7 +67,8 @@ struct Item {
 struct Batch {
 	std::vector<Item *> items;
 	size_t bytes = 0;
-	cudaEvent_t ev = nullptr;
+	cudaEvent_t ev_start = nullptr;  // recorded before the batch's first operation
+	cudaEvent_t ev = nullptr;        // after its last
 	// Pinned: kMaxBatch + 1 offsets of a segmented call, then (device-
 	// resident batches) kMaxBatch input and kMaxBatch output pointers.
 	uint64_t *h_off = nullptr;
@@ -105,9 +106,17 @@ struct clo_server {
 
 	std::vector<uint64_t *> pinned_free;  // kMaxBatch + 1 offsets each
 
+	// batching policy (clo_serve_configure)
+	size_t small_n = kSmallN, batch_elems = kBatchElems, max_batch = kMaxBatch;
+
+	// Device clock origin: batches' start and end events are timed from
+	// this event, so intervals of batches on different streams compare.
+	cudaEvent_t origin = nullptr;
+
 	// statistics
 	CloServeStats st;
 	std::vector<double> lat_ms;
+	std::vector<std::pair<double, double>> busy_ms;  // per batch [start, end]
 	double t_first = 0, t_last = 0;
 };
 
@@ -117,6 +126,8 @@ size_t elem_bytes(CloType t) { return clo_type_sizeof(t); }
 
 void launch_batch(clo_server *srv, Batch *b, Lane *lane) {
 	cudaStream_t s = lane->stream;
+	cudaEventCreate(&b->ev_start);
+	cudaEventRecord(b->ev_start, s);
 	const CloServeRequest &r0 = b->items[0]->r;
 	const bool dev_data = r0.device_data != CL_FALSE;
 	const cudaMemcpyKind h2d = dev_data ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
@@ -234,7 +245,7 @@ void launch_batch(clo_server *srv, Batch *b, Lane *lane) {
 		b->failed = true;
 	}
 	if (err) clo_error_free(err);
-	cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming);
+	cudaEventCreate(&b->ev);
 	cudaEventRecord(b->ev, s);
 }
 
@@ -255,9 +266,16 @@ void lane_loop(clo_server *srv, Lane *lane) {
 			failed = true;
 		}
 		const double t = now_s();
+		float t0_ms = 0.f, t1_ms = 0.f;
+		const bool timed = b->ev_start &&
+			cudaEventElapsedTime(&t0_ms, srv->origin, b->ev_start) == cudaSuccess &&
+			cudaEventElapsedTime(&t1_ms, srv->origin, b->ev) == cudaSuccess;
+		if (!timed) cudaGetLastError();
+		if (b->ev_start) cudaEventDestroy(b->ev_start);
 		cudaEventDestroy(b->ev);
 		{
 			std::lock_guard<std::mutex> lk(srv->mu);
+			if (timed) srv->busy_ms.emplace_back((double)t0_ms, (double)t1_ms);
 			for (Item *it : b->items) {
 				it->done = true;
 				it->failed = failed;
@@ -295,7 +313,7 @@ void sched_loop(clo_server *srv) {
 					const size_t look = std::min<size_t>(srv->pending.size(), 4 * kMaxBatch);
 					for (size_t i = 0; i < look; ++i) view.push_back(srv->pending[i]->r);
 					k = clo_serve_select(view.data(), view.size(), srv->budget - srv->in_use,
-						kSmallN, kBatchElems, kMaxBatch, chosen.data());
+						srv->small_n, srv->batch_elems, srv->max_batch, chosen.data());
 					if (k > 0) break;
 				}
 				if (srv->stop && srv->pending.empty()) {
@@ -347,7 +365,7 @@ void sched_loop(clo_server *srv) {
 		Lane *lane = srv->lanes[srv->next_lane++ % srv->lanes.size()];
 		if (b->items[0]->r.op != CLO_SERVE_RNG_FILL && b->h_off == nullptr) {
 			b->failed = true;
-			cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming);
+			cudaEventCreate(&b->ev);
 			cudaEventRecord(b->ev, lane->stream);
 		} else {
 			launch_batch(srv, b, lane);
@@ -431,6 +449,12 @@ CloServer *clo_serve_new(CCLContext *ctx, size_t budget_bytes, int streams, GErr
 			return nullptr;
 		}
 		srv->lanes.push_back(l);
+	}
+	if (!cuda_ok(cudaEventCreate(&srv->origin), err, "cudaEventCreate") ||
+		!cuda_ok(cudaEventRecord(srv->origin, srv->lanes[0]->stream), err, "cudaEventRecord") ||
+		!cuda_ok(cudaEventSynchronize(srv->origin), err, "cudaEventSynchronize")) {
+		clo_serve_destroy(srv);
+		return nullptr;
 	}
 	for (Lane *l : srv->lanes) l->th = std::thread(lane_loop, srv, l);
 	srv->sched = std::thread(sched_loop, srv);
@@ -531,14 +555,59 @@ cl_bool clo_serve_replay(CloServer *srv, const CloServeRequest *reqs,
 	return CL_TRUE;
 }
 
+cl_bool clo_serve_configure(CloServer *srv, size_t small_n, size_t batch_elems,
+	size_t max_batch, GError **err) {
+	if (!srv || (err && *err)) return CL_FALSE;
+	if (max_batch < 1 || max_batch > kMaxBatch || batch_elems == 0) {
+		set_error(err, CLO_ERROR_ARGS,
+			"clo_serve_configure: max_batch must be 1..%zu and batch_elems nonzero", kMaxBatch);
+		return CL_FALSE;
+	}
+	std::lock_guard<std::mutex> lk(srv->mu);
+	srv->small_n = small_n;
+	srv->batch_elems = batch_elems;
+	srv->max_batch = max_batch;
+	return CL_TRUE;
+}
+
 void clo_serve_get_stats(CloServer *srv, CloServeStats *out) {
 	if (!srv || !out) return;
 	std::vector<double> l;
+	std::vector<std::pair<double, double>> busy;
 	{
 		std::lock_guard<std::mutex> lk(srv->mu);
 		*out = srv->st;
 		l = srv->lat_ms;
+		busy = srv->busy_ms;
 		out->span_s = srv->t_last > srv->t_first ? srv->t_last - srv->t_first : 0.0;
+	}
+	// Batches in flight on the device at once: a sweep over the batches'
+	// [start, end] device intervals. The mean is the batches' summed device
+	// time over the time at least one was in flight.
+	if (!busy.empty()) {
+		std::vector<std::pair<double, int>> ev;
+		ev.reserve(2 * busy.size());
+		double sum = 0;
+		for (auto &iv : busy) {
+			ev.emplace_back(iv.first, +1);
+			ev.emplace_back(iv.second, -1);
+			sum += iv.second - iv.first;
+		}
+		std::sort(ev.begin(), ev.end(), [](const std::pair<double, int> &a,
+			const std::pair<double, int> &b) {
+			return a.first < b.first || (a.first == b.first && a.second < b.second);
+		});
+		int cur = 0, peak = 0;
+		double union_ms = 0, last = ev[0].first;
+		for (auto &e : ev) {
+			if (cur > 0) union_ms += e.first - last;
+			last = e.first;
+			cur += e.second;
+			peak = std::max(peak, cur);
+		}
+		out->max_concurrent_batches = (cl_ulong)peak;
+		out->device_busy_s = union_ms * 1e-3;
+		out->mean_concurrent_batches = union_ms > 0 ? sum / union_ms : 0.0;
 	}
 	if (!l.empty()) {
 		std::sort(l.begin(), l.end());
@@ -562,6 +631,7 @@ void clo_serve_reset_stats(CloServer *srv) {
 	memset(&srv->st, 0, sizeof srv->st);
 	srv->st.budget_bytes = budget;
 	srv->lat_ms.clear();
+	srv->busy_ms.clear();
 	srv->t_first = srv->t_last = 0;
 }
 
@@ -586,6 +656,7 @@ void clo_serve_destroy(CloServer *srv) {
 		if (l->stream) cudaStreamDestroy(l->stream);
 		delete l;
 	}
+	if (srv->origin) cudaEventDestroy(srv->origin);
 	for (uint64_t *p : srv->pinned_free) cudaFreeHost(p);
 	for (auto &kv : srv->items) delete kv.second;
 	ccl_context_unref(srv->ctx);

@@ -21,7 +21,9 @@
  *   CCLEvent    a pair of cudaEvents bracketing one enqueued operation;
  *               owned by the queue it was enqueued on.
  *   CCLProgram  a descriptor of the compiled-in kernels a sorter/scanner
- *               uses (nothing is JIT-compiled).
+ *               uses, or a program built by NVRTC from a caller's CUDA
+ *               source (ccl_program_new_from_source).
+ *   CCLKernel   a kernel of such a program (owned by the program).
  *
  * Functions marked [addition] have no cf4ocl2 counterpart with the same
  * signature; they exist because a CUDA pointer or stream carries no
@@ -42,6 +44,8 @@ typedef struct ccl_queue CCLQueue;
 typedef struct ccl_buffer CCLBuffer;
 typedef struct ccl_event CCLEvent;
 typedef struct ccl_program CCLProgram;
+typedef struct ccl_kernel CCLKernel;
+typedef struct ccl_arg CCLArg;
 typedef struct ccl_ewl_impl *CCLEventWaitList;
 
 /* Memory flags accepted by ccl_buffer_new (OpenCL values). Only
@@ -140,9 +144,53 @@ CCLEvent *ccl_enqueue_marker(CCLQueue *cq, CCLEventWaitList *evt_wait_lst,
  * the completion of `to` (both on profiling queues); waits for `to`. */
 cl_ulong ccl_event_elapsed_ns(CCLEvent *from, CCLEvent *to, GError **err);
 
-/* ---- programs (descriptors of compiled-in kernels) -------------------- */
+/* ---- programs --------------------------------------------------------- */
 const char *ccl_program_get_source(CCLProgram *prg);
 const char *ccl_program_get_build_options(CCLProgram *prg);
+
+/* Client programs, as src/tests/test_rng.c:79-115 builds one around the
+ * text of clo_rng_get_source(). The source is CUDA; kernels that
+ * ccl_program_get_kernel looks up are declared extern "C" __global__.
+ * ccl_program_build compiles it with NVRTC for the context's device
+ * (options are passed to NVRTC); a compile error is CLO_ERROR_LIBRARY
+ * with NVRTC's log, which ccl_program_get_build_log also returns.
+ * The program refs its context; ccl_program_destroy releases it and its
+ * kernels (it ignores a sorter's or scanner's program, which its owner
+ * releases). */
+CCLProgram *ccl_program_new_from_source(CCLContext *ctx, const char *string,
+	GError **err);
+CCLProgram *ccl_program_new_from_sources(CCLContext *ctx, cl_uint count,
+	const char **strings, const size_t *lengths, GError **err);
+cl_bool ccl_program_build(CCLProgram *prg, const char *options, GError **err);
+const char *ccl_program_get_build_log(CCLProgram *prg, GError **err);
+CCLKernel *ccl_program_get_kernel(CCLProgram *prg, const char *kernel_name,
+	GError **err);
+void ccl_program_destroy(CCLProgram *prg);
+
+/* Kernel arguments (cf4ocl2 ccl_arg_*): a value's bytes, or (value NULL)
+ * a local-memory size, which adds to the launch's dynamic shared memory
+ * (reached in the kernel through extern __shared__) and takes no
+ * parameter slot. Arguments passed to an enqueue are released by it. */
+CCLArg *ccl_arg_new(void *value, size_t size);
+void ccl_arg_destroy(CCLArg *arg);
+#define ccl_arg_priv(value, type) ccl_arg_new(&(value), sizeof(type))
+#define ccl_arg_local(count, type) ccl_arg_new(NULL, (count) * sizeof(type))
+#define ccl_arg_full(value, size) ccl_arg_new((value), (size))
+
+/* One dimension only. Without a global size the suggestion is the largest
+ * work-group of at most 256 that divides the real size; with one, 256 (or
+ * the real size if smaller) and the global size rounded up to it. */
+cl_bool ccl_kernel_suggest_worksizes(CCLKernel *krnl, CCLDevice *dev, cl_uint dims,
+	const size_t *real_worksize, size_t *gws, size_t *lws, GError **err);
+/* Launches global_work_size[0] / local_work_size[0] blocks of
+ * local_work_size[0] threads (the global size must be a multiple of the
+ * local one; a NULL local size takes the suggestion above) on cq after the
+ * events of evt_wait_lst. The variadic arguments, NULL-terminated, are
+ * the kernel's parameters in order: a CCLBuffer* passes its device
+ * pointer, a CCLArg* its value. Returns the launch's event. */
+CCLEvent *ccl_kernel_set_args_and_enqueue_ndrange(CCLKernel *krnl, CCLQueue *cq,
+	cl_uint work_dim, const size_t *global_work_offset, const size_t *global_work_size,
+	const size_t *local_work_size, CCLEventWaitList *evt_wait_lst, GError **err, ...);
 
 /* True when every wrapper object created so far has been released
  * (cf4ocl2 ccl_wrapper_memcheck). */

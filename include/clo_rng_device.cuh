@@ -22,7 +22,16 @@
 #ifndef CLO_RNG_DEVICE_CUH
 #define CLO_RNG_DEVICE_CUH
 
+#ifdef __CUDACC_RTC__
+/* NVRTC (a client program built with ccl_program_build) has no C library
+ * headers: the fixed-width types it needs here. */
+typedef unsigned char uint8_t;
+typedef unsigned int uint32_t;
+typedef int int32_t;
+typedef unsigned long long uint64_t;
+#else
 #include <stdint.h>
+#endif
 
 #define CLO_RNG_HD __host__ __device__ __forceinline__
 
@@ -104,7 +113,8 @@ CLO_RNG_HD uint32_t clo_rng_step_tauslcg(uint4 *s) {
 	return s->x;
 }
 
-/* ---- client API (clo_rng_api.cl:33-105, clo_rng_workitem.cl:24-32) ---- */
+/* ---- client API (clo_rng_api.cl:33-105, clo_rng_workitem.cl:24-32):
+ * next_int, next_int2, next_int4, next_int8 ---- */
 #if defined(CLO_RNG_LCG)
 typedef uint64_t clo_statetype;
 #define CLO_RNG_STEP clo_rng_step_lcg
@@ -164,6 +174,26 @@ __device__ __forceinline__ uint4 clo_rng_next_int4(clo_statetype *states,
 	return make_uint4(clo_rng_next(states, g) % n,
 		clo_rng_next(states, w + g) % n, clo_rng_next(states, 2 * w + g) % n,
 		clo_rng_next(states, 3 * w + g) % n);
+}
+
+/* OpenCL's uint8 (eight uints, .s0 - .s7); CUDA has no 8-wide vector. */
+typedef struct {
+	uint32_t s0, s1, s2, s3, s4, s5, s6, s7;
+} clo_uint8;
+
+__device__ __forceinline__ clo_uint8 clo_rng_next_int8(clo_statetype *states,
+	uint32_t n) {
+	uint32_t g = clo_rng_gid(), w = clo_rng_global_size();
+	clo_uint8 r;
+	r.s0 = clo_rng_next(states, g) % n;
+	r.s1 = clo_rng_next(states, w + g) % n;
+	r.s2 = clo_rng_next(states, 2 * w + g) % n;
+	r.s3 = clo_rng_next(states, 3 * w + g) % n;
+	r.s4 = clo_rng_next(states, 4 * w + g) % n;
+	r.s5 = clo_rng_next(states, 5 * w + g) % n;
+	r.s6 = clo_rng_next(states, 6 * w + g) % n;
+	r.s7 = clo_rng_next(states, 7 * w + g) % n;
+	return r;
 }
 #endif /* __CUDACC__ */
 #endif /* CLO_RNG_STEP */

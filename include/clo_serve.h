@@ -55,6 +55,14 @@ typedef struct clo_serve_stats {
 	double p50_ms, p99_ms, max_ms, mean_ms;  /* latency of completed requests */
 	double elements;        /* elements (draws for RNG_FILL) completed */
 	double span_s;          /* first submission to last completion */
+	/* Device overlap, from each batch's [start, end] on the device (events
+	 * recorded on its stream before its first and after its last
+	 * operation): the most batches in flight at one time, the time at
+	 * least one was in flight, and the batches' summed device time over
+	 * that time (1.0 = no overlap). */
+	cl_ulong max_concurrent_batches;
+	double device_busy_s;
+	double mean_concurrent_batches;
 } CloServeStats;
 
 typedef struct clo_server CloServer;
@@ -86,6 +94,14 @@ cl_bool clo_serve_drain(CloServer *srv, GError **err);
  * a rejected request). */
 cl_bool clo_serve_replay(CloServer *srv, const CloServeRequest *reqs,
 	const double *arrival_s, size_t count, cl_ulong *tickets, GError **err);
+
+/* Batching policy: requests of at most small_n elements are batched, a
+ * batch holds at most batch_elems elements and max_batch (1..4096)
+ * requests. The defaults are 2^20, 2^26 and 4096; max_batch 1 turns
+ * batching off (every request runs alone through the plain kernels).
+ * Takes effect for batches formed after the call. */
+cl_bool clo_serve_configure(CloServer *srv, size_t small_n, size_t batch_elems,
+	size_t max_batch, GError **err);
 
 void clo_serve_get_stats(CloServer *srv, CloServeStats *stats);
 void clo_serve_reset_stats(CloServer *srv);

@@ -166,3 +166,59 @@ def test_serve_host_and_device_requests_together(clops, ctx, queue):
         bi.destroy()
         bo.destroy()
     srv.destroy()
+
+
+def test_batches_overlap_on_the_device_with_four_streams(clops, ctx):
+    """Requests that arrive together run as batches on the server's 4
+    streams at the same time: the device intervals of at least two batches
+    overlap (each interval runs from an event recorded before the batch's
+    first operation to one after its last, on its stream). Each result
+    still equals the oracle's."""
+    n = 1 << 22  # above the batching limit: one request per batch
+    a = [keys_of_type(4000 + i, n, np.uint32) for i in range(16)]
+    dst = [np.empty_like(x) for x in a]
+    pinned = []
+    for x in a + dst:  # page-locked, so the copies are asynchronous
+        addr = clops.lib.clo_host_alloc(x.nbytes, None)
+        pinned.append((addr, np.ctypeslib.as_array((clops.C.c_uint32 * n).from_address(addr))))
+    for (addr, arr), x in zip(pinned[:16], a):
+        arr[:] = x
+    srv = clops.Server(ctx, 8 << 30, streams=4)
+    try:
+        tickets = [srv.submit(clops.Server.request(clops.SERVE_SORT, 5, 0, n, inp=pi[0],
+                                                   out=po[0]))
+                   for pi, po in zip(pinned[:16], pinned[16:])]
+        for t in tickets:
+            srv.wait(t)
+        st = srv.stats()
+        assert st["completed"] == 16 and st["batches"] == 16
+        assert st["max_concurrent_batches"] >= 2, st
+        assert st["mean_concurrent_batches"] > 1.0, st
+        assert 0 < st["device_busy_s"] <= st["span_s"] + 1e-3
+        for (_, arr), x in zip(pinned[16:], a):
+            np.testing.assert_array_equal(arr, oracle.radix_sort(x))
+    finally:
+        srv.destroy()
+        for addr, arr in pinned:
+            del arr
+        for addr, _ in pinned:
+            clops.lib.clo_host_free(addr)
+
+
+def test_batching_off_runs_every_request_alone(clops, ctx):
+    """max_batch = 1: every request is its own batch (the plain kernels),
+    with the same results as batched serving."""
+    reqs = make_requests(clops, 60, seed=71, max_log2=14)
+    srv = clops.Server(ctx, 8 << 30, streams=1)
+    try:
+        srv.configure(max_batch=1)
+        for t in [srv.submit(r) for r, _, _, _ in reqs]:
+            srv.wait(t)
+        st = srv.stats()
+        assert st["batches"] == 60 and st["max_concurrent_batches"] == 1
+        for _, exp, dst, _ in reqs:
+            np.testing.assert_array_equal(dst, exp)
+        with pytest.raises(clops.CloError):
+            srv.configure(max_batch=0)
+    finally:
+        srv.destroy()
