@@ -495,7 +495,12 @@ def run_suite(clops, ctx, q, args, only=None):
             "sort_speedup_vs_plain": round(ms_plain_sort / best, 1),
             "sort_model_bytes": "36 B/key in segments > 8192, 8 B/key in the others",
             "sort_frac_of_peak": round(model / (best * 1e-3) / 1e9 / peak, 4),
-            "autotuner": {"chosen": variant, "variant_ms": [round(t, 3) for t in vtimes]},
+            "autotuner": {"chosen": variant, "chosen_shape": seg_shape(variant),
+                          "chosen_ms": round(vtimes[variant], 3),
+                          "default_ms": round(vtimes[0], 3),
+                          "slowest_ms": round(max(vtimes), 3),
+                          "variants_timed": len(vtimes),
+                          "variant_ms": [round(t, 3) for t in vtimes]},
             "scan_ms": round(ms_scan, 3), "scan_graph_ms": round(ms_scan_graph, 3),
             "scan_GB/s": round(12.0 * n / (min(ms_scan, ms_scan_graph) * 1e-3) / 1e9, 1),
             "scan_frac_of_peak": round(12.0 * n / (min(ms_scan, ms_scan_graph) * 1e-3)
@@ -817,6 +822,15 @@ def bench_config(n, world, ok):
     return {"workload": WORKLOAD, "n": n, "parallelism": f"replicas x{world}",
             "l2": "inputs larger than L2: a distinct 1 GiB copy per step",
             "result_check": "sorted+multiset ok" if ok else "FAILED"}
+
+
+def seg_shape(v):
+    """The segmented sort's shape for variant v (include/clo_gb300.h)."""
+    d, v = v % 2, v // 2
+    l_, v = v % 3, v // 3
+    b, a = v % 3, v // 3
+    return {"class_a": ["128x8", "256x8"][a], "class_b": ["512x16", "256x16", "1024x16"][b],
+            "long_keys_per_thread": [56, 48, 40][l_], "cta_digit_bits": [8, 4][d]}
 
 
 def cpu_port_sorts(keys, steps, warmup, cores):

@@ -28,7 +28,7 @@ CLO_ERROR_IMPL_NOT_FOUND, CLO_ERROR_UNKNOWN_TYPE, CLO_ERROR_LIBRARY = 5, 6, 7
 CLO_RNG_SEED_DEV_GID, CLO_RNG_SEED_HOST_MT, CLO_RNG_SEED_EXT_DEV, \
     CLO_RNG_SEED_EXT_HOST = range(4)
 CL_QUEUE_PROFILING_ENABLE = 1 << 1
-SEG_SORT_VARIANTS = 3  # CLO_SEG_SORT_VARIANTS
+SEG_SORT_VARIANTS = 36  # CLO_SEG_SORT_VARIANTS
 CL_MEM_READ_WRITE = 1 << 0
 
 NP_OF_TYPE = {

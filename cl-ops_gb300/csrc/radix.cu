@@ -7,7 +7,7 @@
 // the width here is a tuning choice (8 bits: 4 passes for 32-bit keys).
 //
 // Per sort:
-//   1. radix_upsweep: one read of the keys builds the 256-bin histogram
+//   1. radix_upsweep_w: one read of the keys builds the 256-bin histogram
 //      of every digit position at once.
 //   2. per digit position, radix_pass_tiles (one launch per pass), one CTA
 //      per tile (14336 32-bit keys; 5120 pairs of a 64-bit key and a
@@ -53,64 +53,50 @@ __device__ __forceinline__ uint32_t digit_of(K k, int shift) {
 }
 
 // ----------------------------------------------------------- upsweep
-// Histograms of all `passes` digit positions in one read. Up to four
-// positions count into lane columns: the (d & 1) 16-bit half of word
-// (d >> 1) * 32 + lane per position, shared by the CTA's warps through
-// atomics, so a warp's 32 increments hit 32 different banks; more positions
-// count into one 256-bin row per warp and position. Each thread keeps
-// kUpsweepInFlight 16-byte loads in flight.
-//
-// A column half receives at most kWarps x (keys per thread) increments;
-// the grid is sized so that a thread sees at most kUpsweepKeysPerThread
-// keys (8 x (4096 + 16) < 2^16).
-constexpr int kUpsweepThreads = 256;
-constexpr size_t kUpsweepKeysPerThread = 4096;
-constexpr int kUpsweepColumnPasses = 4;  // most positions counted in columns
+// Histograms of all `passes` digit positions in one read, counted into
+// lane columns shared by the CTA's warps through shared-memory adds: the
+// counter of digit d of lane l lives in bank l, so a warp's 32 adds hit 32
+// different banks whatever the digits. Each thread keeps kUpsweepInFlight
+// 16-byte loads in flight.
 constexpr int kUpsweepInFlight = 8;
 
+// 1024-thread CTAs. Up to four digit positions count into full 32-bit
+// words (digit d of lane l at word d * 32 + l per position: one byte
+// extract, one address computation and one shared add per key and
+// position, and no overflow bound); five to eight positions (64-bit keys)
+// into 16-bit halves of word (d >> 1) * 32 + l, 16 KB per position, with
+// the grid keeping a thread at kUpwHalfKeysPerThread keys so that a half,
+// which all 32 warps of a CTA add to, stays below 2^16.
+constexpr int kUpwThreads = 1024;
+constexpr size_t kUpwHalfKeysPerThread = 2000;
+
 template <int PASSES>
-constexpr size_t upsweep_smem() {
-	return PASSES <= kUpsweepColumnPasses ? (size_t)PASSES * (kRadix / 2) * 32 * 4
-										  : (size_t)PASSES * (kUpsweepThreads / 32) * kRadix * 4;
+constexpr size_t upw_smem() {
+	return (size_t)PASSES * (PASSES <= 4 ? kRadix : kRadix / 2) * 32 * 4;
 }
 
 template <typename K, int PASSES>
-__global__ void __launch_bounds__(kUpsweepThreads)
-radix_upsweep(const K *__restrict__ keys, size_t n, uint32_t *__restrict__ hist,
+__global__ void __launch_bounds__(kUpwThreads, 1)
+radix_upsweep_w(const K *__restrict__ keys, size_t n, uint32_t *__restrict__ hist,
 	int base_shift) {
-	constexpr bool COLS = PASSES <= kUpsweepColumnPasses;
-	constexpr int kWarps = kUpsweepThreads / 32;
-	constexpr int kPosWords = COLS ? (kRadix / 2) * 32 : kWarps * kRadix;
+	constexpr bool HALVES = PASSES > 4;
+	constexpr int kPosWords = (HALVES ? kRadix / 2 : kRadix) * 32;
 	extern __shared__ __align__(16) uint32_t up_smem[];
-	for (int i = threadIdx.x; i < PASSES * kPosWords; i += kUpsweepThreads) up_smem[i] = 0;
+	for (int i = threadIdx.x; i < PASSES * kPosWords; i += kUpwThreads) up_smem[i] = 0;
 	__syncthreads();
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	uint32_t *base = COLS ? up_smem + lane : up_smem + warp * kRadix;
+	const int lane = threadIdx.x & 31;
+	uint32_t *col = up_smem + lane;
 	auto count = [&](int p, K key) {
 		const uint32_t d = digit_of(key, base_shift + p * kRadixBits);
-		if (COLS) atomicAdd(base + p * kPosWords + (d >> 1) * 32, 1u << ((d & 1) << 4));
-		else atomicAdd(base + p * kPosWords + d, 1u);
+		if (HALVES) atomicAdd(col + p * kPosWords + (d >> 1) * 32, 1u << ((d & 1) << 4));
+		else atomicAdd(col + p * kPosWords + d * 32, 1u);
 	};
-	// 32-bit keys at shift 0 with four positions: the four column rows
-	// (d >> 1) and half selectors (d & 1) come out of two word-wide masks,
-	// then one byte extract, one address add and the atomic per position.
-	auto count4 = [&](uint32_t key) {
-		const uint32_t rows = (key >> 1) & 0x7F7F7F7Fu;
-		const uint32_t halves = (key & 0x01010101u) << 4;  // 0 or 16 per byte
-#pragma unroll
-		for (int p = 0; p < 4; ++p) {
-			const uint32_t row = __byte_perm(rows, 0, 0x4440 + p);
-			const uint32_t sh = __byte_perm(halves, 0, 0x4440 + p);
-			atomicAdd(base + p * kPosWords + row * 32, 1u << sh);
-		}
-	};
-	constexpr bool kFast4 = COLS && PASSES == 4 && sizeof(K) == 4;
 	constexpr int PER = 16 / sizeof(K);  // keys per 16-byte load
 	const bool aligned = ((uintptr_t)keys % 16) == 0;
 	const size_t nvec = aligned ? n / PER : 0;
 	const uint4 *kv4 = reinterpret_cast<const uint4 *>(keys);
-	const size_t stride = (size_t)gridDim.x * kUpsweepThreads;
-	size_t i = blockIdx.x * (size_t)kUpsweepThreads + threadIdx.x;
+	const size_t stride = (size_t)gridDim.x * kUpwThreads;
+	size_t i = blockIdx.x * (size_t)kUpwThreads + threadIdx.x;
 	for (; i + (kUpsweepInFlight - 1) * stride < nvec; i += kUpsweepInFlight * stride) {
 		uint4 v[kUpsweepInFlight];
 #pragma unroll
@@ -118,45 +104,37 @@ radix_upsweep(const K *__restrict__ keys, size_t n, uint32_t *__restrict__ hist,
 #pragma unroll
 		for (int u = 0; u < kUpsweepInFlight; ++u) {
 			const K *e = reinterpret_cast<const K *>(&v[u]);
-			if (kFast4 && base_shift == 0) {
 #pragma unroll
-				for (int q = 0; q < PER; ++q) count4((uint32_t)e[q]);
-			} else {
+			for (int q = 0; q < PER; ++q)
 #pragma unroll
-				for (int p = 0; p < PASSES; ++p)
-#pragma unroll
-					for (int q = 0; q < PER; ++q) count(p, e[q]);
-			}
+				for (int p = 0; p < PASSES; ++p) count(p, e[q]);
 		}
 	}
 	for (; i < nvec; i += stride) {
 		uint4 v = dev::ld_stream_v4(kv4 + i);
 		const K *e = reinterpret_cast<const K *>(&v);
 #pragma unroll
-		for (int p = 0; p < PASSES; ++p)
+		for (int q = 0; q < PER; ++q)
 #pragma unroll
-			for (int q = 0; q < PER; ++q) count(p, e[q]);
+			for (int p = 0; p < PASSES; ++p) count(p, e[q]);
 	}
-	// Remaining keys (and unaligned inputs): one key per thread.
-	for (size_t j = nvec * PER + blockIdx.x * (size_t)kUpsweepThreads + threadIdx.x; j < n;
+	for (size_t j = nvec * PER + blockIdx.x * (size_t)kUpwThreads + threadIdx.x; j < n;
 		 j += stride) {
 		const K key = keys[j];
 #pragma unroll
 		for (int p = 0; p < PASSES; ++p) count(p, key);
 	}
 	__syncthreads();
-	for (int b = threadIdx.x; b < PASSES * kRadix; b += kUpsweepThreads) {
+	for (int b = threadIdx.x; b < PASSES * kRadix; b += kUpwThreads) {
 		const int p = b / kRadix, d = b % kRadix;
+		// Digit d's 32 columns, from a rotated start (no bank conflicts).
+		const uint32_t *row = up_smem + p * kPosWords + (HALVES ? d >> 1 : d) * 32;
+		const int hs = HALVES ? (d & 1) << 4 : 0;
 		uint32_t v = 0;
-		if (COLS) {
-			// Digit d's 32 column halves, from a rotated start (no conflicts).
-			const uint32_t *row = up_smem + p * kPosWords + (d >> 1) * 32;
-			const int hs = (d & 1) << 4;
 #pragma unroll 8
-			for (int c = 0; c < 32; ++c) v += (row[(c + lane) & 31] >> hs) & 0xFFFFu;
-		} else {
-#pragma unroll
-			for (int w = 0; w < kWarps; ++w) v += up_smem[p * kPosWords + w * kRadix + d];
+		for (int c = 0; c < 32; ++c) {
+			const uint32_t w = row[(c + lane) & 31];
+			v += HALVES ? (w >> hs) & 0xFFFFu : w;
 		}
 		if (v) atomicAdd(hist + b, v);
 	}
@@ -178,8 +156,19 @@ struct PassArgs {
 // measured slower.
 constexpr int kLookWindow = 8;
 
-// Threads per CTA of the pass: one per digit in the per-tile scans.
-constexpr int kPassThreads = kRadix;
+// Threads per CTA of the pass: at least one per digit (threads below 256
+// own a digit in the per-tile scans, the lookback and the output bases).
+#ifndef CLO_RADIX_PASS_THREADS
+#define CLO_RADIX_PASS_THREADS 256
+#endif
+constexpr int kPassThreads = CLO_RADIX_PASS_THREADS;
+static_assert(kPassThreads >= 256 && kPassThreads <= 1024 && kPassThreads % 32 == 0,
+	"pass CTA size");
+// Keys per thread for one-word keys (0: the 256-thread shape scaled to the
+// CTA size).
+#ifndef CLO_RADIX_PASS_KPT1
+#define CLO_RADIX_PASS_KPT1 0
+#endif
 
 // Reads the statuses of tiles base, base-1, ..., base-W+1 for one digit
 // (independent loads, one round trip), adds them in order to `excl` up to
@@ -245,22 +234,21 @@ __device__ __forceinline__ int row_of(int r) { return r * kRowWords + (r & 1) * 
 // read and one write of each key (and value). Tiles are large (TilesCfg)
 // because each costs one lookback.
 //
-// Shared memory: 16 ranking rows and 8 count rows (row_of), the tile
-// offsets and a scan array (256 words each), 64 misc words, the staged
-// tile (keys, then values).
-template <typename K, typename V, bool HAS_V, int KPT>
+// Shared memory: a ranking row per half-warp unit and a count row per two
+// units (row_of), the tile offsets and a scan array (256 words each), 64
+// misc words, the staged tile (keys, then values).
+template <typename K, typename V, bool HAS_V, int THREADS, int KPT>
 constexpr size_t tiles_smem() {
-	return ((16 + 8) * kRowWords + 2 * kRadix + 64) * sizeof(uint32_t) +
-		(size_t)kPassThreads * KPT * (sizeof(K) + (HAS_V ? sizeof(V) : 0));
+	return ((size_t)(THREADS / 16 + THREADS / 32) * kRowWords + 2 * kRadix + 64) *
+		sizeof(uint32_t) + (size_t)THREADS * KPT * (sizeof(K) + (HAS_V ? sizeof(V) : 0));
 }
 
-template <typename K, typename V, bool HAS_V, int KPT, int MINB>
-__global__ void __launch_bounds__(kPassThreads, MINB)
+template <typename K, typename V, bool HAS_V, int THREADS, int KPT, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB)
 radix_pass_tiles(const K *__restrict__ kin, K *__restrict__ kout,
 	const V *__restrict__ vin, V *__restrict__ vout, PassArgs a, uint32_t num_tiles) {
-	constexpr int THREADS = kPassThreads;
 	constexpr int TILE = THREADS * KPT;
-	constexpr int UNITS = 16;
+	constexpr int UNITS = THREADS / 16;
 	constexpr int HALF = UNITS / 2;
 	constexpr int UKEYS = 16 * KPT;  // a unit's keys
 	static_assert(UKEYS <= 0xFFFF && TILE <= 0xFFFF, "16-bit unit and tile counts");
@@ -281,21 +269,26 @@ radix_pass_tiles(const K *__restrict__ kin, K *__restrict__ kout,
 	uint32_t *my_cnt = s_cnt + row_of(unit % HALF);
 	const uint32_t cnt_inc = 1u << ((unit / HALF) * 16);
 	const int shift = a.shift;
-	const int pd = tid;
+	// Threads below 256 (whole warps) own digit pd in the per-digit steps.
+	const bool owner = THREADS == kRadix || tid < kRadix;
+	const int pd = tid & (kRadix - 1);
 	const int dw = pd >> 5;
 
 	if (tid == 0) s_misc[0] = atomicAdd(a.tile_counter, 1u);
+	uint32_t hv = 0, hinc = 0;
+	if (owner) {
 #pragma unroll
-	for (int i = 0; i < HALF; ++i) s_cnt[row_of(i) + pd] = 0;
-	// Global digit base of this pass: exclusive scan of its histogram.
-	const uint32_t hv = a.hist[pd];
-	uint32_t hinc = hv;
+		for (int i = 0; i < HALF; ++i) s_cnt[row_of(i) + pd] = 0;
+		// Global digit base of this pass: exclusive scan of its histogram.
+		hv = a.hist[pd];
+		hinc = hv;
 #pragma unroll
-	for (int s = 1; s < 32; s <<= 1) {
-		uint32_t t = __shfl_up_sync(0xffffffffu, hinc, s);
-		if (lane >= s) hinc += t;
+		for (int s = 1; s < 32; s <<= 1) {
+			uint32_t t = __shfl_up_sync(0xffffffffu, hinc, s);
+			if (lane >= s) hinc += t;
+		}
+		if (lane == 31) s_misc[16 + dw] = hinc;
 	}
-	if (lane == 31) s_misc[16 + dw] = hinc;
 	__syncthreads();
 	const uint32_t t = s_misc[0];
 	if (t >= num_tiles) return;
@@ -317,30 +310,27 @@ radix_pass_tiles(const K *__restrict__ kin, K *__restrict__ kout,
 #pragma unroll
 	for (int j = 0; j < KPT; ++j) atomicAdd(my_cnt + digit_of(k[j], shift), cnt_inc);
 	__syncthreads();
-	// Unit prefixes of digit pd in unit order and the tile's count.
-	uint32_t c2[HALF];
-#pragma unroll
-	for (int i = 0; i < HALF; ++i) c2[i] = s_cnt[row_of(i) + pd];
-	uint32_t run = 0;
-#pragma unroll
-	for (int i = 0; i < HALF; ++i) {
-		const uint32_t lo = c2[i] & 0xFFFFu;
-		c2[i] = (c2[i] & 0xFFFF0000u) | run;
-		run += lo;
-	}
-#pragma unroll
-	for (int i = 0; i < HALF; ++i) {
-		const uint32_t hi = c2[i] >> 16;
-		c2[i] = (c2[i] & 0xFFFFu) | (run << 16);
-		run += hi;
-	}
-	const uint32_t sum = run;
-	// Publish the tile's count of digit pd (tile 0: its inclusive prefix).
+	// Unit prefixes of digit pd in unit order (written to the units' rank
+	// words, the tile offset added below) and the tile's count.
+	uint32_t sum = 0;
 	uint32_t *st = a.status + (size_t)t * kRadix + pd;
-	dev::st_relaxed_u32(st, (t == 0 ? kStPrefix : kStAgg) | sum);
-	a.status_next[(size_t)t * kRadix + pd] = 0;
-	// Tile offsets of the digits: exclusive scan of the counts.
-	{
+	if (owner) {
+		uint32_t run = 0;
+#pragma unroll
+		for (int i = 0; i < HALF; ++i) {
+			s_rank[row_of(i) + pd] = run << 16;
+			run += s_cnt[row_of(i) + pd] & 0xFFFFu;
+		}
+#pragma unroll
+		for (int i = 0; i < HALF; ++i) {
+			s_rank[row_of(i + HALF) + pd] = run << 16;
+			run += s_cnt[row_of(i) + pd] >> 16;
+		}
+		sum = run;
+		// Publish the tile's count of digit pd (tile 0: its inclusive prefix).
+		dev::st_relaxed_u32(st, (t == 0 ? kStPrefix : kStAgg) | sum);
+		a.status_next[(size_t)t * kRadix + pd] = 0;
+		// Tile offsets of the digits: exclusive scan of the counts.
 		uint32_t inc = sum;
 #pragma unroll
 		for (int d = 1; d < 32; d <<= 1) {
@@ -351,14 +341,17 @@ radix_pass_tiles(const K *__restrict__ kin, K *__restrict__ kout,
 		s_part[pd] = inc - sum;
 	}
 	__syncthreads();
-	uint32_t to = s_part[pd];
+	if (owner) {
+		uint32_t to = s_part[pd];
 #pragma unroll
-	for (int w = 0; w < 8; ++w)
-		if (w < dw) to += s_misc[8 + w];
+		for (int w = 0; w < 8; ++w)
+			if (w < dw) to += s_misc[8 + w];
 #pragma unroll
-	for (int i = 0; i < HALF; ++i) {
-		s_rank[row_of(i) + pd] = (to + (c2[i] & 0xFFFFu)) << 16;
-		s_rank[row_of(i + HALF) + pd] = (to + (c2[i] >> 16)) << 16;
+		for (int i = 0; i < UNITS; ++i) s_rank[row_of(i) + pd] += to << 16;
+		// Output index of staged position q of digit d is q + G[d] (mod
+		// 2^32), G[d] = global base + lookback prefix - tile offset; the
+		// prefix is added after the lookback.
+		s_tile_off[pd] = gbase - to;
 	}
 	__syncthreads();
 	K *sk = reinterpret_cast<K *>(s_stage);
@@ -373,7 +366,7 @@ radix_pass_tiles(const K *__restrict__ kin, K *__restrict__ kout,
 	}
 	// Lookback over the preceding tiles for digit pd (bounded waits).
 	uint32_t excl = 0;
-	if (t > 0) {
+	if (owner && t > 0) {
 		long long base = (long long)t - 1;
 		uint32_t iter = 0;
 		bool done = lookback_window<kWin>(a.status, pd, base, excl);
@@ -392,8 +385,7 @@ radix_pass_tiles(const K *__restrict__ kin, K *__restrict__ kout,
 		}
 		dev::st_relaxed_u32(st, kStPrefix | (excl + sum));
 	}
-	// Output index of staged position q of digit d is q + G[d] (mod 2^32).
-	s_tile_off[pd] = gbase + excl - to;
+	if (owner) s_tile_off[pd] += excl;
 	__syncthreads();
 #pragma unroll
 	for (int i = 0; i < KPT; ++i) {
@@ -415,27 +407,33 @@ radix_pass_tiles(const K *__restrict__ kin, K *__restrict__ kout,
 template <typename K, typename V, bool HAS_V>
 struct TilesCfg {
 	static constexpr int kWords = (int)((sizeof(K) + 3) / 4) + (HAS_V ? (int)((sizeof(V) + 3) / 4) : 0);
-	static constexpr int kKpt = kWords == 1 ? 56 : kWords == 2 ? 32 : kWords == 3 ? 20 : 16;
+	static constexpr int kThreads = kPassThreads;
+	static constexpr int kKpt256 = kWords == 1 ? 56 : kWords == 2 ? 32 : kWords == 3 ? 20 : 16;
+	static constexpr int kKpt = (kWords == 1 && CLO_RADIX_PASS_KPT1 > 0) ? CLO_RADIX_PASS_KPT1
+		: kKpt256 * 256 / kThreads;
 	static constexpr int kMinBlocks = 2;
-	static constexpr int kTile = kPassThreads * kKpt;
+	static constexpr int kTile = kThreads * kKpt;
 };
 
 template <typename K, int PASSES>
 void launch_upsweep_p(cudaStream_t s, const K *keys, size_t n, uint32_t *hist,
 	int base_shift, int sm_count) {
-	constexpr size_t smem = upsweep_smem<PASSES>();
-	auto kern = radix_upsweep<K, PASSES>;
+	constexpr size_t smem = upw_smem<PASSES>();
+	auto kern = radix_upsweep_w<K, PASSES>;
 	if (smem > 48 * 1024)
 		cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-	// Resident CTAs per SM by shared memory (228 KB per SM, 1 KB reserved
-	// per CTA), at most 4; at least enough CTAs for the per-thread key cap.
-	const int per_sm = (int)std::min<size_t>(4, (228 * 1024) / (smem + 1024));
+	// 2048 threads per SM: two CTAs where shared memory allows (228 KB per
+	// SM, 1 KB reserved per CTA); at least enough CTAs for the key cap of
+	// the 16-bit halves.
+	const int per_sm = (int)std::min<size_t>(2, (228 * 1024) / (smem + 1024));
 	size_t grid = (size_t)sm_count * std::max(per_sm, 1);
-	const size_t need = ((n * sizeof(K) + 15) / 16 + kUpsweepThreads - 1) / kUpsweepThreads;
+	const size_t need = ((n * sizeof(K) + 15) / 16 + kUpwThreads - 1) / kUpwThreads;
 	if (grid > need) grid = std::max<size_t>(need, 1);
-	const size_t cap = kUpsweepThreads * kUpsweepKeysPerThread;
-	grid = std::max(grid, (n + cap - 1) / cap);
-	kern<<<(unsigned)grid, kUpsweepThreads, smem, s>>>(keys, n, hist, base_shift);
+	if (PASSES > 4) {
+		const size_t cap = kUpwThreads * kUpwHalfKeysPerThread;
+		grid = std::max(grid, (n + cap - 1) / cap);
+	}
+	kern<<<(unsigned)grid, kUpwThreads, smem, s>>>(keys, n, hist, base_shift);
 }
 
 template <typename K>
@@ -466,8 +464,8 @@ cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
 	// One CTA per tile of TilesCfg size.
 	using TC = TilesCfg<K, V, HAS_V>;
 	const size_t ctiles = (n + TC::kTile - 1) / TC::kTile;
-	const size_t smem = tiles_smem<K, V, HAS_V, TC::kKpt>();
-	auto kern = radix_pass_tiles<K, V, HAS_V, TC::kKpt, TC::kMinBlocks>;
+	const size_t smem = tiles_smem<K, V, HAS_V, TC::kThreads, TC::kKpt>();
+	auto kern = radix_pass_tiles<K, V, HAS_V, TC::kThreads, TC::kKpt, TC::kMinBlocks>;
 	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
 		(int)smem);
 	if (e != cudaSuccess) {
@@ -532,7 +530,7 @@ cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
 			pa.shift = active[q] * kRadixBits;
 			KernelTimer t("satradix_onesweep", s,
 				2.0 * (double)n * (sizeof(K) + (HAS_V ? sizeof(V) : 0)));
-			kern<<<(unsigned)ctiles, kPassThreads, smem, s>>>(src_k, dst_k, src_v, dst_v, pa,
+			kern<<<(unsigned)ctiles, TC::kThreads, smem, s>>>(src_k, dst_k, src_v, dst_v, pa,
 				(uint32_t)ctiles);
 			t.stop();
 			launches++;
@@ -562,8 +560,8 @@ cudaError_t msd_partition_typed(const K *keys_in, K *keys_out, size_t n, int sor
 	using TC = TilesCfg<K, uint32_t, false>;
 	const int shift = sort_bits - kRadixBits;
 	const size_t ctiles = (n + TC::kTile - 1) / TC::kTile;
-	const size_t smem = tiles_smem<K, uint32_t, false, TC::kKpt>();
-	auto kern = radix_pass_tiles<K, uint32_t, false, TC::kKpt, TC::kMinBlocks>;
+	const size_t smem = tiles_smem<K, uint32_t, false, TC::kThreads, TC::kKpt>();
+	auto kern = radix_pass_tiles<K, uint32_t, false, TC::kThreads, TC::kKpt, TC::kMinBlocks>;
 	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
 		(int)smem);
 	if (e != cudaSuccess) {
@@ -601,7 +599,7 @@ cudaError_t msd_partition_typed(const K *keys_in, K *keys_out, size_t n, int sor
 		pa.shift = shift;
 		if (e == cudaSuccess) {
 			KernelTimer t("satradix_onesweep", s, 2.0 * (double)n * sizeof(K));
-			kern<<<(unsigned)ctiles, kPassThreads, smem, s>>>(keys_in, keys_out, nullptr, nullptr,
+			kern<<<(unsigned)ctiles, TC::kThreads, smem, s>>>(keys_in, keys_out, nullptr, nullptr,
 				pa, (uint32_t)ctiles);
 			t.stop();
 			e = cudaGetLastError();

@@ -34,36 +34,14 @@
 #include "clo_internal.h"
 #include "dev_common.cuh"
 #include "scan_status.cuh"
+#include "seg_common.cuh"
 #include "scan_tile.cuh"
 #include "timing.h"
 
 namespace clo {
 namespace {
 
-constexpr int kRadix = 256;
-constexpr int kRadixBits = 8;
-constexpr uint32_t kMaxSegLen = (1u << 30) - 1u;
-
-// Large-segment pass: 256 threads (one per digit in the per-tile scans),
-// 56 keys per thread (32 for 64-bit keys), 2 CTAs per SM: the plain sort's
-// tile shape, large because each tile costs one lookback.
-constexpr int kLThreads = 256;
-constexpr int kLWarps = kLThreads / 32;
-template <typename K>
-struct LCfg {
-	static constexpr int kKpt = sizeof(K) <= 4 ? 56 : 32;
-	static constexpr int kTile = kLThreads * kKpt;
-};
-
-// Tile status word of the large-segment pass: 2-bit flag | 30-bit count.
-constexpr uint32_t kStAgg = 1u << 30;
-constexpr uint32_t kStPrefix = 2u << 30;
-constexpr uint32_t kStValue = (1u << 30) - 1u;
-
-template <typename K>
-__device__ __forceinline__ uint32_t digit_of(K k, int shift) {
-	return (uint32_t)(k >> shift) & (kRadix - 1);
-}
+using namespace seg;
 
 __device__ __forceinline__ void report_bad_segment(int *st, uint32_t s) {
 	if (atomicCAS(st, 0, DEV_ERR_BAD_SEGMENTS) == 0) atomicExch(st + 1, (int)s);
@@ -178,147 +156,16 @@ __global__ void __launch_bounds__(256) seg_sort_warp(K *keys, const uint64_t *of
 	}
 }
 
-// ---------------------------------------------------------- CTA classes
-template <typename K, int THREADS, int KPT>
-struct CtaCfg {
-	static constexpr int kWarps = THREADS / 32;
-	static constexpr int kTile = THREADS * KPT;
-	static constexpr int kDigitsPerThread = THREADS >= kRadix ? 1 : kRadix / THREADS;
-	static constexpr int kDigitThreads = kRadix / kDigitsPerThread;
-	static size_t smem() {
-		return (2 * (size_t)kWarps * kRadix + 64) * sizeof(uint32_t) +
-			(size_t)kTile * sizeof(K);
-	}
-};
-
-// One CTA per segment of the list: keys stay in registers (warp-striped,
-// so index order is (warp, round, lane)); per 8-bit digit, per-warp counts,
-// a block scan of the digit totals, stable ranks through shared-memory OR
-// peer masks, and a pass through shared memory back to index order.
-// Elements past the segment end are all-ones keys: they rank last in every
-// digit, so they stay behind the segment and are never written. Warps whose
-// keys all lie past the end take no part in the passes (their counts stay
-// zero), so a segment pays only for the warps it fills.
-template <typename K, int THREADS, int KPT>
-__global__ void __launch_bounds__(THREADS) seg_sort_cta(K *keys, const uint64_t *off,
-	const uint32_t *list, const uint32_t *count, int passes) {
-	using Cfg = CtaCfg<K, THREADS, KPT>;
-	constexpr int W = Cfg::kWarps;
-	constexpr int TILE = Cfg::kTile;
-	constexpr int DPT = Cfg::kDigitsPerThread;
-	constexpr int DT = Cfg::kDigitThreads;
-	extern __shared__ __align__(16) unsigned char smem[];
-	uint32_t *s_hist = reinterpret_cast<uint32_t *>(smem);  // [W][256]
-	uint32_t *s_match = s_hist + W * kRadix;                // [W][256]
-	uint32_t *s_misc = s_match + W * kRadix;                // [64]
-	K *sk = reinterpret_cast<K *>(s_misc + 64);             // [TILE]
-
-	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-	uint32_t *my_hist = s_hist + warp * kRadix;
-	uint32_t *my_match = s_match + warp * kRadix;
-	const uint32_t lt = dev::lanemask_lt();
-	for (int i = lane; i < kRadix; i += 32) my_match[i] = 0;
-	const uint32_t cnt = *count;
-	const uint32_t wb = (uint32_t)warp * (KPT * 32);
-
-	for (uint32_t li = blockIdx.x; li < cnt; li += gridDim.x) {
-		const uint32_t s = list[li];
-		const uint64_t base = off[s];
-		const uint32_t len = (uint32_t)(off[s + 1] - base);
-		// Warps holding part of the segment, and the keys they hold.
-		const bool active = wb < len;
-		const uint32_t held = std::min<uint32_t>(TILE, (len + KPT * 32 - 1) / (KPT * 32) * (KPT * 32));
-		K k[KPT];
-#pragma unroll
-		for (int j = 0; j < KPT; ++j) {
-			const uint32_t idx = wb + j * 32 + lane;
-			k[j] = idx < len ? keys[base + idx] : (K)~(K)0;
-		}
-		for (int p = 0; p < passes; ++p) {
-			const int shift = p * kRadixBits;
-			for (int i = lane; i < kRadix; i += 32) my_hist[i] = 0;
-			__syncwarp();
-			if (active) {
-#pragma unroll
-				for (int j = 0; j < KPT; ++j) atomicAdd(my_hist + digit_of(k[j], shift), 1u);
-			}
-			__syncthreads();
-			// Digit totals (DPT consecutive digits per thread), the scan of
-			// the threads' sums within each warp, and whether one digit holds
-			// every key (then this digit leaves the order unchanged).
-			uint32_t tot[DPT];
-			uint32_t tsum = 0, tinc = 0;
-			bool triv = false;
-			if (tid < DT) {
-#pragma unroll
-				for (int q = 0; q < DPT; ++q) {
-					const int d = tid * DPT + q;
-					uint32_t c = 0;
-#pragma unroll
-					for (int w = 0; w < W; ++w) c += s_hist[w * kRadix + d];
-					tot[q] = c;
-					tsum += c;
-					triv = triv || c == (d == kRadix - 1 ? held : len);
-				}
-				tinc = tsum;
-#pragma unroll
-				for (int d = 1; d < 32; d <<= 1) {
-					const uint32_t t = __shfl_up_sync(0xffffffffu, tinc, d);
-					if (lane >= d) tinc += t;
-				}
-				if (lane == 31) s_misc[warp] = tinc;
-			}
-			if (__syncthreads_or(triv)) continue;
-			if (tid < DT) {
-				uint32_t run = tinc - tsum;
-				for (int w = 0; w < warp; ++w) run += s_misc[w];
-#pragma unroll
-				for (int q = 0; q < DPT; ++q) {
-					const int d = tid * DPT + q;
-					uint32_t r = run;
-#pragma unroll
-					for (int w = 0; w < W; ++w) {
-						const uint32_t c = s_hist[w * kRadix + d];
-						s_hist[w * kRadix + d] = r;
-						r += c;
-					}
-					run += tot[q];
-				}
-			}
-			__syncthreads();
-			if (active) {
-#pragma unroll
-				for (int j = 0; j < KPT; ++j) {
-					sk[dev::warp_rank_digit(my_match, my_hist, digit_of(k[j], shift), lane, lt)] =
-						k[j];
-				}
-			}
-			__syncthreads();
-			if (active) {
-#pragma unroll
-				for (int j = 0; j < KPT; ++j) k[j] = sk[wb + j * 32 + lane];
-			}
-		}
-#pragma unroll
-		for (int j = 0; j < KPT; ++j) {
-			const uint32_t idx = wb + j * 32 + lane;
-			if (idx < len) keys[base + idx] = k[j];
-		}
-		__syncthreads();
-	}
-}
-
 // ------------------------------------------------------ large segments
 // Tile -> segment map and per-tile descriptors (segment start and end,
 // tile index within the segment, large-segment rank: what a pass needs to
 // start a tile, in one round trip), and clearing of what the passes
 // accumulate into: the segment's digit histograms and the first pass's
 // tile statuses.
-template <int TILE>
 __global__ void __launch_bounds__(256) seg_tiles(const uint64_t *off,
 	const uint64_t *tstart, const uint32_t *list, const uint32_t *count,
 	uint32_t *tile_seg, ulonglong2 *tile_span, uint2 *tile_x, uint32_t *seg_hist,
-	int passes, uint32_t *status0) {
+	int passes, uint32_t *status0, uint32_t tile) {
 	const uint32_t lane = threadIdx.x & 31u;
 	const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -328,7 +175,7 @@ __global__ void __launch_bounds__(256) seg_tiles(const uint64_t *off,
 		const uint64_t ts = tstart[s];
 		const uint32_t first = (uint32_t)(ts >> 32), lr = (uint32_t)ts;
 		const uint64_t len = off[s + 1] - off[s];
-		const uint32_t ntiles = (uint32_t)((len + TILE - 1) / TILE);
+		const uint32_t ntiles = (uint32_t)((len + tile - 1) / tile);
 		const ulonglong2 span = make_ulonglong2(off[s], off[s + 1]);
 		for (uint32_t t = lane; t < ntiles; t += 32) {
 			tile_seg[first + t] = s;
@@ -349,8 +196,7 @@ __global__ void __launch_bounds__(256) seg_tiles(const uint64_t *off,
 template <typename K, int PASSES>
 __global__ void __launch_bounds__(256) seg_upsweep(const K *keys, const uint64_t *off,
 	const uint64_t *tstart, const uint32_t *tile_seg, uint32_t S,
-	uint32_t *seg_hist) {
-	constexpr int TILE = LCfg<K>::kTile;
+	uint32_t *seg_hist, uint32_t tile) {
 	__shared__ uint32_t h[PASSES * kRadix];
 	__shared__ uint64_t s_a, s_e;
 	__shared__ uint32_t s_lr;
@@ -360,10 +206,10 @@ __global__ void __launch_bounds__(256) seg_upsweep(const K *keys, const uint64_t
 		if (threadIdx.x == 0) {
 			const uint32_t s = tile_seg[t];
 			const uint64_t ts = tstart[s];
-			const uint64_t a = off[s] + (uint64_t)(t - (uint32_t)(ts >> 32)) * TILE;
+			const uint64_t a = off[s] + (uint64_t)(t - (uint32_t)(ts >> 32)) * tile;
 			const uint64_t e = off[s + 1];
 			s_a = a;
-			s_e = a + TILE < e ? a + TILE : e;
+			s_e = a + tile < e ? a + tile : e;
 			s_lr = (uint32_t)ts;
 		}
 		__syncthreads();
@@ -382,253 +228,18 @@ __global__ void __launch_bounds__(256) seg_upsweep(const K *keys, const uint64_t
 	}
 }
 
-struct SegPassArgs {
-	const uint64_t *off;
-	const uint64_t *tstart;
-	const uint32_t *tile_seg;
-	const ulonglong2 *tile_span;  // segment [start, end) of each tile
-	const uint2 *tile_x;          // (tile index within the segment, rank)
-	const uint32_t *seg_hist;  // + pass * 256; stride passes * 256 per segment
-	uint32_t hist_stride;
-	uint32_t *status;
-	uint32_t *status_next;
-	uint32_t *counter;
-	int *dev_status;
-	uint32_t S;
-	int shift;
-};
-
-// Reads tiles base, base-1, ... (W of them, one round trip) for one digit
-// and adds them to `excl` up to the first inclusive prefix.
-template <int W>
-__device__ __forceinline__ bool seg_lookback_window(const uint32_t *status, int digit,
-	long long &base, uint32_t &excl) {
-	uint32_t sv[W];
-#pragma unroll
-	for (int i = 0; i < W; ++i) {
-		const long long j = base - i;
-		sv[i] = j >= 0 ? dev::ld_relaxed_u32(status + (size_t)j * kRadix + digit) : kStPrefix;
-	}
-	int consumed = W;
-	bool done = false;
-#pragma unroll
-	for (int i = 0; i < W; ++i) {
-		if (!done && consumed == W) {
-			if ((sv[i] & ~kStValue) == 0) {
-				consumed = i;
-			} else {
-				excl += sv[i] & kStValue;
-				if (sv[i] & kStPrefix) done = true;
-			}
-		}
-	}
-	if (!done) base -= consumed;
-	return done;
-}
-
-// Ranking rows (one per half-warp unit) and count rows: 256 digits each,
-// 264 words apart, odd rows 8 words later, so the two units of a warp hold
-// a digit 16 banks apart.
-constexpr int kSegRowWords = kRadix + 8;
-__device__ __forceinline__ int seg_row(int r) { return r * kSegRowWords + (r & 1) * 8; }
-constexpr int kLUnits = 2 * kLWarps;  // 16 half-warp units per tile
-constexpr int kSegLookWindow = 8;     // predecessor statuses per round trip
-
-// One pass over all tiles of all large segments, by persistent CTAs that
-// take tiles in order from a counter (the next tile and its descriptor are
-// claimed during the write-out). Per tile as the plain sort's pass: keys
-// loaded in half-warp units (a unit's (round, lane) order is index order),
-// unit counts in 16-bit halves of 8 count rows (units u and u + 8 share
-// row u), the tile's counts published before it is ranked (a segment's
-// first tile publishes an inclusive prefix at once, so lookbacks stop at
-// the segment's start), ranking with dev::unit_rank_digit (the unit's word
-// per digit holds its next tile position in the upper 16 bits and the
-// round's peer mask in the lower 16), staging, then a lookback in windows
-// of kSegLookWindow and a write-out with one base per digit.
-template <typename K>
-__global__ void __launch_bounds__(kLThreads, 2)
-seg_pass(const K *__restrict__ kin, K *__restrict__ kout, SegPassArgs a) {
-	constexpr int KPT = LCfg<K>::kKpt;
-	constexpr int TILE = LCfg<K>::kTile;
-	constexpr int UKEYS = 16 * KPT;          // a unit's keys in one tile
-	constexpr int HALF = kLUnits / 2;        // 8 count rows
-	static_assert(TILE <= 0xFFFF, "16-bit unit and tile counts");
-	extern __shared__ __align__(16) unsigned char smem[];
-	uint32_t *s_rank = reinterpret_cast<uint32_t *>(smem);     // [16] rows
-	uint32_t *s_cnt = s_rank + kLUnits * kSegRowWords;         // [8] rows
-	uint32_t *s_tile_off = s_cnt + HALF * kSegRowWords;        // [256]
-	uint32_t *s_part = s_tile_off + kRadix;                    // [256]
-	uint32_t *s_misc = s_part + kRadix;                        // [64]
-	uint64_t *s_seg = reinterpret_cast<uint64_t *>(s_misc + 64);  // [2]
-	unsigned char *s_stage = reinterpret_cast<unsigned char *>(s_seg + 2);
-
-	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-	const int unit = 2 * warp + (lane >> 4);
-	const uint32_t l16 = lane & 15;
-	const uint32_t lt16 = (1u << l16) - 1u;
-	uint32_t *my_rank = s_rank + seg_row(unit);
-	uint32_t *my_cnt = s_cnt + seg_row(unit % HALF);
-	const uint32_t cnt_inc = 1u << ((unit / HALF) * 16);
-	const int pd = tid;        // the digit this thread scans
-	const int dw = tid >> 5;   // the warp that owns digit pd
-	const int shift = a.shift;
-#pragma unroll
-	for (int i = 0; i < HALF; ++i) s_cnt[seg_row(i) + pd] = 0;
-	const uint32_t T = (uint32_t)(a.tstart[a.S] >> 32);
-	// Thread 0 takes the next tile and its descriptor (one round trip after
-	// the claim); after the first tile this overlaps the write-out.
-	auto claim = [&]() {
-		const uint32_t t = atomicAdd(a.counter, 1u);
-		s_misc[0] = t;
-		if (t < T) {
-			const ulonglong2 span = a.tile_span[t];
-			const uint2 x = a.tile_x[t];
-			s_misc[1] = x.x;   // tile index within the segment
-			s_misc[2] = x.y;   // large-segment rank
-			s_seg[0] = span.x;
-			s_seg[1] = span.y;
-		}
-	};
-	if (tid == 0) claim();
-	__syncthreads();
-
-	for (;;) {
-		const uint32_t tile = s_misc[0];
-		if (tile >= T) break;
-		const uint32_t ti = s_misc[1];
-		const uint32_t lr = s_misc[2];
-		const uint64_t seg_a = s_seg[0], seg_e = s_seg[1];
-		const uint64_t ubase = seg_a + (uint64_t)ti * TILE + (uint64_t)unit * UKEYS;
-
-		K k[KPT];
-#pragma unroll
-		for (int j = 0; j < KPT; ++j) {
-			const uint64_t idx = ubase + (uint64_t)j * 16 + l16;
-			k[j] = idx < seg_e ? kin[idx] : (K)~(K)0;
-		}
-		// Digit base within the segment: exclusive scan of its histogram.
-		const uint32_t hv = a.seg_hist[(size_t)lr * a.hist_stride + pd];
-		uint32_t hinc = hv;
-#pragma unroll
-		for (int d = 1; d < 32; d <<= 1) {
-			const uint32_t t = __shfl_up_sync(0xffffffffu, hinc, d);
-			if (lane >= d) hinc += t;
-		}
-		if (lane == 31) s_misc[16 + dw] = hinc;
-#pragma unroll
-		for (int j = 0; j < KPT; ++j) atomicAdd(my_cnt + digit_of(k[j], shift), cnt_inc);
-		__syncthreads();
-		uint32_t gbase = hinc - hv;
-#pragma unroll
-		for (int w = 0; w < 8; ++w)
-			if (w < dw) gbase += s_misc[16 + w];
-		// Unit prefixes of digit pd in unit order (low halves: units
-		// 0..7, high halves: units 8..15); rows cleared as they are read.
-		uint32_t c2[HALF];
-#pragma unroll
-		for (int i = 0; i < HALF; ++i) {
-			c2[i] = s_cnt[seg_row(i) + pd];
-			s_cnt[seg_row(i) + pd] = 0;
-		}
-		uint32_t run = 0;
-#pragma unroll
-		for (int i = 0; i < HALF; ++i) {
-			const uint32_t lo = c2[i] & 0xFFFFu;
-			c2[i] = (c2[i] & 0xFFFF0000u) | run;
-			run += lo;
-		}
-#pragma unroll
-		for (int i = 0; i < HALF; ++i) {
-			const uint32_t hi = c2[i] >> 16;
-			c2[i] = (c2[i] & 0xFFFFu) | (run << 16);
-			run += hi;
-		}
-		const uint32_t sum = run;
-		uint32_t *st = a.status + (size_t)tile * kRadix + pd;
-		dev::st_relaxed_u32(st, (ti == 0 ? kStPrefix : kStAgg) | sum);
-		a.status_next[(size_t)tile * kRadix + pd] = 0;
-		{
-			uint32_t inc = sum;
-#pragma unroll
-			for (int d = 1; d < 32; d <<= 1) {
-				const uint32_t t = __shfl_up_sync(0xffffffffu, inc, d);
-				if (lane >= d) inc += t;
-			}
-			if (lane == 31) s_misc[8 + dw] = inc;
-			s_part[pd] = inc - sum;
-		}
-		__syncthreads();
-		uint32_t to = s_part[pd];
-#pragma unroll
-		for (int w = 0; w < 8; ++w)
-			if (w < dw) to += s_misc[8 + w];
-#pragma unroll
-		for (int i = 0; i < HALF; ++i) {
-			s_rank[seg_row(i) + pd] = (to + (c2[i] & 0xFFFFu)) << 16;
-			s_rank[seg_row(i + HALF) + pd] = (to + (c2[i] >> 16)) << 16;
-		}
-		__syncthreads();
-		K *sk = reinterpret_cast<K *>(s_stage);
-#pragma unroll
-		for (int j = 0; j < KPT; ++j) {
-			const uint32_t pos = dev::unit_rank_digit(my_rank + digit_of(k[j], shift), l16, lt16);
-			if (pos < (uint32_t)TILE) sk[pos] = k[j];
-		}
-		// Lookback over the segment's preceding tiles (bounded waits).
-		uint32_t excl = 0;
-		if (ti > 0) {
-			long long base = (long long)tile - 1;
-			uint32_t iter = 0;
-			bool done = seg_lookback_window<kSegLookWindow>(a.status, pd, base, excl);
-			while (!done && base >= 0) {
-				uint32_t sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + pd);
-				while ((sv & ~kStValue) == 0) {
-					if (++iter >= dev::kSpinLimit) break;
-					dev::backoff(iter);
-					sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + pd);
-				}
-				if ((sv & ~kStValue) == 0) {
-					dev::report_timeout(a.dev_status, DEV_ERR_LOOKBACK_TIMEOUT, (int)tile);
-					break;
-				}
-				done = seg_lookback_window<kSegLookWindow>(a.status, pd, base, excl);
-			}
-			dev::st_relaxed_u32(st, kStPrefix | (excl + sum));
-		}
-		// Output offset (within the segment) of staged position q of digit
-		// d is q + G[d] (modulo 2^32).
-		s_tile_off[pd] = gbase + excl - to;
-		__syncthreads();
-		if (tid == 0) claim();
-#pragma unroll
-		for (int i = 0; i < KPT; ++i) {
-			const int q = i * kLThreads + tid;
-			const K key = sk[q];
-			const uint64_t o = seg_a + (uint32_t)(s_tile_off[digit_of(key, shift)] + (uint32_t)q);
-			if (o < seg_e) kout[o] = key;
-		}
-		__syncthreads();
-	}
-}
-
-template <typename K>
-size_t seg_pass_smem() {
-	return ((size_t)(kLUnits + kLUnits / 2) * kSegRowWords + 3 * kRadix + 64) * sizeof(uint32_t) +
-		2 * sizeof(uint64_t) + (size_t)LCfg<K>::kTile * sizeof(K);
-}
-
 // Copies the large segments back from the alternate buffer (odd number of
 // passes).
 template <typename K>
 __global__ void __launch_bounds__(256) seg_copy_large(K *dst, const K *src,
-	const uint64_t *off, const uint64_t *tstart, const uint32_t *tile_seg, uint32_t S) {
-	constexpr int TILE = LCfg<K>::kTile;
+	const uint64_t *off, const uint64_t *tstart, const uint32_t *tile_seg, uint32_t S,
+	uint32_t tile) {
 	const uint32_t T = (uint32_t)(tstart[S] >> 32);
 	for (uint32_t t = blockIdx.x; t < T; t += gridDim.x) {
 		const uint32_t s = tile_seg[t];
-		const uint64_t a = off[s] + (uint64_t)(t - (uint32_t)(tstart[s] >> 32)) * TILE;
+		const uint64_t a = off[s] + (uint64_t)(t - (uint32_t)(tstart[s] >> 32)) * tile;
 		const uint64_t e = off[s + 1];
-		const uint64_t end = a + TILE < e ? a + TILE : e;
+		const uint64_t end = a + tile < e ? a + tile : e;
 		for (uint64_t i = a + threadIdx.x; i < end; i += blockDim.x) dst[i] = src[i];
 	}
 }
@@ -650,89 +261,19 @@ __global__ void __launch_bounds__(256) seg_copy_short(K *dst, const K *src,
 	}
 }
 
-// Class layouts the autotuner chooses from: (threads, keys per thread) of
-// classes A and B for keys of up to 4 bytes; 8-byte keys halve the keys
-// per thread.
-struct Variant {
-	int a_threads, a_kpt, b_threads, b_kpt;
-};
-constexpr Variant kVariants[] = {
-	{128, 8, 512, 16},
-	{256, 8, 512, 16},
-	{128, 8, 256, 16},
-};
-constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
-
-template <typename K, int THREADS, int KPT>
-cudaError_t launch_cta_class(K *keys, const uint64_t *off, const uint32_t *list,
-	const uint32_t *count, int passes, uint32_t max_blocks, CCLContext *ctx,
-	cudaStream_t s) {
-	using Cfg = CtaCfg<K, THREADS, KPT>;
-	const size_t smem = Cfg::smem();
-	auto kern = seg_sort_cta<K, THREADS, KPT>;
-	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		(int)smem);
-	if (e != cudaSuccess) return e;
-	int occ = 0;
-	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, THREADS, smem);
-	if (e != cudaSuccess) return e;
-	uint32_t grid = (uint32_t)std::max(1, occ) * (uint32_t)ctx->sm_count;
-	if (grid > max_blocks) grid = std::max<uint32_t>(max_blocks, 1);
-	KernelTimer t("seg_sort_cta", s, 0.0);
-	kern<<<grid, THREADS, smem, s>>>(keys, off, list, count, passes);
-	t.stop();
-	count_launches(1);
-	return cudaGetLastError();
-}
-
-template <typename K, int KPT_DIV>
-cudaError_t launch_variant_classes(int variant, K *keys, const uint64_t *off,
-	const uint32_t *lists, const uint32_t *counts, uint32_t S, int passes,
-	uint64_t n_cap, CCLContext *ctx, cudaStream_t s) {
-	// Blocks beyond the number of segments that can exist would only exit.
-	auto cap = [&](int tile_lo) {
-		return (uint32_t)std::min<uint64_t>(S, n_cap / (uint64_t)(tile_lo + 1) + 1);
-	};
-	cudaError_t e = cudaSuccess;
-	switch (variant) {
-	case 1:
-		e = launch_cta_class<K, 256, 8 / KPT_DIV>(keys, off, lists + (size_t)S, counts + 1,
-			passes, cap(32), ctx, s);
-		if (e == cudaSuccess)
-			e = launch_cta_class<K, 512, 16 / KPT_DIV>(keys, off, lists + 2 * (size_t)S,
-				counts + 2, passes, cap(256 * 8 / KPT_DIV), ctx, s);
-		break;
-	case 2:
-		e = launch_cta_class<K, 128, 8 / KPT_DIV>(keys, off, lists + (size_t)S, counts + 1,
-			passes, cap(32), ctx, s);
-		if (e == cudaSuccess)
-			e = launch_cta_class<K, 256, 16 / KPT_DIV>(keys, off, lists + 2 * (size_t)S,
-				counts + 2, passes, cap(128 * 8 / KPT_DIV), ctx, s);
-		break;
-	default:
-		e = launch_cta_class<K, 128, 8 / KPT_DIV>(keys, off, lists + (size_t)S, counts + 1,
-			passes, cap(32), ctx, s);
-		if (e == cudaSuccess)
-			e = launch_cta_class<K, 512, 16 / KPT_DIV>(keys, off, lists + 2 * (size_t)S,
-				counts + 2, passes, cap(128 * 8 / KPT_DIV), ctx, s);
-		break;
-	}
-	return e;
-}
-
 template <typename K>
 void launch_seg_upsweep(int passes, uint32_t grid, cudaStream_t s, const K *keys,
 	const uint64_t *off, const uint64_t *tstart, const uint32_t *tile_seg, uint32_t S,
-	uint32_t *seg_hist) {
+	uint32_t *seg_hist, uint32_t tile) {
 	switch (passes) {
-	case 1: seg_upsweep<K, 1><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist); break;
-	case 2: seg_upsweep<K, 2><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist); break;
-	case 3: seg_upsweep<K, 3><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist); break;
-	case 4: seg_upsweep<K, 4><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist); break;
-	case 5: seg_upsweep<K, 5><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist); break;
-	case 6: seg_upsweep<K, 6><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist); break;
-	case 7: seg_upsweep<K, 7><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist); break;
-	default: seg_upsweep<K, 8><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist); break;
+	case 1: seg_upsweep<K, 1><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist, tile); break;
+	case 2: seg_upsweep<K, 2><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist, tile); break;
+	case 3: seg_upsweep<K, 3><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist, tile); break;
+	case 4: seg_upsweep<K, 4><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist, tile); break;
+	case 5: seg_upsweep<K, 5><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist, tile); break;
+	case 6: seg_upsweep<K, 6><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist, tile); break;
+	case 7: seg_upsweep<K, 7><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist, tile); break;
+	default: seg_upsweep<K, 8><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist, tile); break;
 	}
 }
 
@@ -740,15 +281,13 @@ template <typename K>
 cudaError_t seg_sort_typed(K *keys, uint64_t n_cap, const uint64_t *off, uint32_t S,
 	int sort_bits, int variant, CCLContext *ctx, cudaStream_t s, GError **err,
 	K *alt_ext, bool *in_alt) {
-	constexpr int KPT_DIV = sizeof(K) > 4 ? 2 : 1;
-	constexpr int LTILE = LCfg<K>::kTile;
+	const SegShape sh = seg_shape(variant);
+	const uint32_t LTILE = long_tile<K>(sh.long_idx);
 	const int passes = sort_bits / kRadixBits;
 	if (in_alt) *in_alt = false;
 	if (S == 0 || passes == 0 || n_cap < 2) return cudaSuccess;
-	if (variant < 0 || variant >= kNumVariants) variant = 0;
-	const Variant &v = kVariants[variant];
-	const uint32_t max_a = (uint32_t)(v.a_threads * (v.a_kpt / KPT_DIV));
-	const uint32_t max_b = (uint32_t)(v.b_threads * (v.b_kpt / KPT_DIV));
+	const uint32_t max_a = class_a_max<K>(sh);
+	const uint32_t max_b = class_b_max<K>(sh);
 	// Bounds the host can derive without reading the offsets.
 	const uint64_t L_bound = std::min<uint64_t>(S, n_cap / (max_b + 1));
 	const uint64_t T_bound = n_cap / LTILE + L_bound + 1;
@@ -814,15 +353,14 @@ cudaError_t seg_sort_typed(K *keys, uint64_t n_cap, const uint64_t *off, uint32_
 		e = cudaGetLastError();
 	}
 	if (e == cudaSuccess)
-		e = launch_variant_classes<K, KPT_DIV>(variant, keys, off, lists, counts, S,
-			passes, n_cap, ctx, s);
+		e = seg_launch_cta_classes<K>(sh, keys, off, lists, counts, S, sort_bits, n_cap, ctx, s);
 	if (e == cudaSuccess && L_bound > 0) {
 		const uint32_t *list3 = lists + 3 * (size_t)S;
 		{
 			const uint32_t grid = (uint32_t)std::min<uint64_t>((L_bound + 7) / 8,
 				(uint64_t)ctx->sm_count * 8);
-			seg_tiles<LTILE><<<grid, 256, 0, s>>>(off, tstart, list3, counts + 3, tile_seg,
-				tile_span, tile_x, seg_hist, passes, st[0]);
+			seg_tiles<<<grid, 256, 0, s>>>(off, tstart, list3, counts + 3, tile_seg,
+				tile_span, tile_x, seg_hist, passes, st[0], LTILE);
 			launches++;
 			e = cudaGetLastError();
 		}
@@ -830,21 +368,12 @@ cudaError_t seg_sort_typed(K *keys, uint64_t n_cap, const uint64_t *off, uint32_
 			const uint32_t grid = (uint32_t)std::min<uint64_t>(T_bound,
 				(uint64_t)ctx->sm_count * 8);
 			KernelTimer t("seg_upsweep", s, 0.0);
-			launch_seg_upsweep<K>(passes, grid, s, keys, off, tstart, tile_seg, S, seg_hist);
+			launch_seg_upsweep<K>(passes, grid, s, keys, off, tstart, tile_seg, S, seg_hist,
+				LTILE);
 			t.stop();
 			launches++;
 			e = cudaGetLastError();
 		}
-		const size_t smem = seg_pass_smem<K>();
-		auto kern = seg_pass<K>;
-		if (e == cudaSuccess)
-			e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-				(int)smem);
-		int occ = 0;
-		if (e == cudaSuccess)
-			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kLThreads, smem);
-		const uint32_t pgrid = (uint32_t)std::min<uint64_t>(T_bound,
-			(uint64_t)std::max(occ, 1) * ctx->sm_count);
 		K *src = keys, *dst = alt;
 		for (int p = 0; p < passes && e == cudaSuccess; ++p) {
 			SegPassArgs pa;
@@ -861,11 +390,7 @@ cudaError_t seg_sort_typed(K *keys, uint64_t n_cap, const uint64_t *off, uint32_
 			pa.dev_status = ctx->d_status;
 			pa.S = S;
 			pa.shift = p * kRadixBits;
-			KernelTimer t("seg_pass", s, 0.0);
-			kern<<<pgrid, kLThreads, smem, s>>>(src, dst, pa);
-			t.stop();
-			launches++;
-			e = cudaGetLastError();
+			e = seg_launch_pass<K>(sh, src, dst, pa, T_bound, ctx, s);
 			std::swap(src, dst);
 		}
 		if (e == cudaSuccess && (passes & 1) && alt_ext && in_alt) {
@@ -880,7 +405,7 @@ cudaError_t seg_sort_typed(K *keys, uint64_t n_cap, const uint64_t *off, uint32_
 		} else if (e == cudaSuccess && (passes & 1)) {
 			const uint32_t grid = (uint32_t)std::min<uint64_t>(T_bound,
 				(uint64_t)ctx->sm_count * 8);
-			seg_copy_large<K><<<grid, 256, 0, s>>>(keys, alt, off, tstart, tile_seg, S);
+			seg_copy_large<K><<<grid, 256, 0, s>>>(keys, alt, off, tstart, tile_seg, S, LTILE);
 			launches++;
 			e = cudaGetLastError();
 		}
@@ -1323,7 +848,7 @@ cudaError_t seg_move_launch(void *flat, void *const *ptrs, const uint64_t *off, 
 
 }  // namespace
 
-int seg_sort_num_variants() { return kNumVariants; }
+int seg_sort_num_variants() { return kSegVariants; }
 
 cudaError_t seg_sort(void *keys, uint64_t n_cap, const uint64_t *off, size_t S,
 	int key_bytes, int sort_bits, int variant, CCLContext *ctx, cudaStream_t s,

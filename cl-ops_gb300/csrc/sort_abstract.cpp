@@ -194,8 +194,8 @@ struct SatradixData {
 	std::string scan_type;
 	std::string scan_opts;
 	CloScan *scanner;
-	// Class layout of segmented sorts (segvariant= option, or the
-	// autotuner's choice).
+	// Shape of segmented sorts (segvariant= option, or the autotuner's
+	// choice).
 	int seg_variant;
 };
 

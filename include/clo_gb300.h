@@ -117,22 +117,29 @@ cl_bool clo_scan_blelloch_noalloc(CCLQueue *cq, CloType elem_type,
  * "satradix" sorters accept it; others set CLO_ERROR_ARGS. The buffer
  * capacity (its size / element size) bounds the offsets. Segments go by
  * length to a warp (<= 32 elements), a CTA (two classes of shared-memory
- * radix sort) or the multi-CTA onesweep passes; the CTA class layout is
- * the sorter's "segvariant=<n>" option or the autotuner's choice. */
+ * radix sort) or the multi-CTA onesweep passes. The shape -- the two CTA
+ * classes' layouts (threads x keys per thread, which also set the class
+ * boundaries), the CTA classes' digit width (8 or 4 bits) and the keys
+ * per thread of the long-segment passes' tiles -- is the sorter's
+ * "segvariant=<n>" option or the autotuner's choice; variant 0 is the
+ * default shape. */
 CCLEvent *clo_sort_segmented_with_device_data(CloSort *sorter, CCLQueue *cq_exec,
 	CCLBuffer *data, CCLBuffer *offsets, size_t num_segments, GError **err);
 cl_bool clo_sort_segmented_with_host_data(CloSort *sorter, CCLQueue *cq_exec,
 	void *data, size_t numel, const cl_ulong *offsets, size_t num_segments,
 	GError **err);
 
-/* Number of CTA class layouts of the segmented sort. */
-#define CLO_SEG_SORT_VARIANTS 3
+/* Number of segmented-sort shapes: class A layout (128 x 8, 256 x 8) x
+ * class B layout (512 x 16, 256 x 16, 1024 x 16) x long-pass keys per
+ * thread (56, 48, 40; 32, 28, 24 for 8-byte keys) x CTA-class digit bits
+ * (8, 4); variant = ((a * 3 + b) * 3 + l) * 2 + d. */
+#define CLO_SEG_SORT_VARIANTS 36
 
-/* Autotuner: times every class layout on a copy of `data` with these
- * offsets (best of two runs each), stores the fastest in the sorter for
- * its later segmented sorts and returns its index (-1 on error). The
- * caller's data is not modified. times_ms, when not NULL, receives
- * CLO_SEG_SORT_VARIANTS times in milliseconds. Blocking. */
+/* Autotuner: times every shape on a copy of `data` with these offsets
+ * (best of two runs each), stores the fastest in the sorter for its later
+ * segmented sorts and returns its index (-1 on error). The caller's data
+ * is not modified. times_ms, when not NULL, receives CLO_SEG_SORT_VARIANTS
+ * times in milliseconds. Blocking. */
 cl_int clo_sort_segmented_tune(CloSort *sorter, CCLQueue *cq_exec,
 	CCLBuffer *data, CCLBuffer *offsets, size_t num_segments, double *times_ms,
 	GError **err);

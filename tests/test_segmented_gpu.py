@@ -24,16 +24,26 @@ def _seg_sort(clops, ctx, q, code, a, off, options=None, key_type=None, buf_extr
     return out
 
 
-# Lengths that hit every class boundary of every variant (32, 512, 1024,
-# 2048, 4096, 8192), the large-segment pass's tile edges (14336 keys of up
-# to 32 bits, 8192 of 64 bits; one to three tiles), empty and single
-# segments.
+# Lengths that hit every class boundary of every shape (32; class A 512,
+# 1024, 2048; class B 2048, 4096, 8192, 16384), the long-segment pass's
+# tile edges (10240, 12288, 14336 keys of up to 32 bits; 6144, 7168, 8192
+# of 64 bits; one to three tiles), empty and single segments.
 EDGE_LENS = [0, 1, 2, 31, 32, 33, 0, 511, 512, 513, 1023, 1024, 1025, 2047, 2048, 2049,
-             4095, 4096, 4097, 8191, 8192, 8193, 14335, 14336, 14337, 16384, 16385,
-             28672, 28673, 40000, 3, 0, 1]
+             4095, 4096, 4097, 6143, 6144, 6145, 7167, 7168, 7169, 8191, 8192, 8193,
+             10239, 10240, 10241, 12287, 12288, 12289, 14335, 14336, 14337, 16383, 16384,
+             16385, 20480, 20481, 24576, 24577, 28672, 28673, 40000, 3, 0, 1]
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
+# Every class A / class B layout, long-pass tile and CTA digit width
+# appears in at least one of these shapes (variant = ((a * 3 + b) * 3 + l)
+# * 2 + d): the default, 4-bit CTA digits, 256 x 8 class A with a 48-key
+# long tile, 256 x 16 class B with a 40-key tile, 1024 x 16 class B with
+# 4-bit digits, and the last shape.
+SHAPES = [0, 1, ((1 * 3 + 0) * 3 + 1) * 2, ((0 * 3 + 1) * 3 + 2) * 2,
+          ((0 * 3 + 2) * 3 + 0) * 2 + 1, 35]
+
+
+@pytest.mark.parametrize("variant", SHAPES)
 @pytest.mark.parametrize("code,dt", [(5, np.uint32), (4, np.int32), (7, np.uint64),
                                      (6, np.int64), (1, np.uint8), (3, np.uint16)])
 def test_seg_sort_edge_lengths(clops, ctx, queue, variant, code, dt):
@@ -46,7 +56,7 @@ def test_seg_sort_edge_lengths(clops, ctx, queue, variant, code, dt):
     np.testing.assert_array_equal(got[int(off[-1]):], a[int(off[-1]):])
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", range(36))
 def test_seg_sort_lognormal_u32(clops, ctx, queue, variant):
     lens = lognormal_lengths(3000, 6.0, 2.0, 1, 1 << 18, seed=48)
     off = offsets_of(lens)
@@ -123,7 +133,7 @@ def test_seg_sort_rejects_bad_offsets_and_other_sorters(clops, ctx, queue):
     assert ei.value.code == clops.CLO_ERROR_ARGS
     g.destroy()
     with pytest.raises(clops.CloError):
-        clops.Sorter(ctx, "satradix", UINT, options="segvariant=9")
+        clops.Sorter(ctx, "satradix", UINT, options="segvariant=36")
 
 
 def test_seg_sort_tune_picks_a_variant_and_keeps_data(clops, ctx, queue):
