@@ -336,10 +336,13 @@ def run_suite(clops, ctx, q, args, only=None):
         s = clops.Sorter(ctx, "abitonic", clops.CLO_UINT)
         ms_copy = timed(lambda: copy(pristine, b, a.nbytes))
         ms = timed(lambda: (copy(pristine, b, a.nbytes), s.sort_device(q, b, n))) - ms_copy
+        # For uint32 keys the network's output is the ascending order.
+        ok = bool(np.array_equal(b.read(q, np.uint32, n), np.sort(a)))
         res["abitonic_2pow26_u32"] = {
             "Gkeys/s": round(n / (ms * 1e-3) / 1e9, 3), "ms": round(ms, 3),
             "canonical_bytes_GB": 17.7,
-            "frac_of_peak_canonical": round(17.7e9 / (ms * 1e-3) / 1e9 / peak, 4)}
+            "frac_of_peak_canonical": round(17.7e9 / (ms * 1e-3) / 1e9 / peak, 4),
+            "result_check": "equal to np.sort" if ok else "FAILED"}
         for x in (s, b, pristine):
             x.destroy()
 
@@ -356,10 +359,19 @@ def run_suite(clops, ctx, q, args, only=None):
             copy(vp, vb, v.nbytes)
         ms_copy = timed(restore)
         ms = timed(lambda: (restore(), s.sort_kv_device(q, kb, vb, clops.CLO_UINT, n))) - ms_copy
+        # Values are the original indices. Keys ascending, values a
+        # permutation carrying each key, and ties in index order: together
+        # the stable sort's output exactly.
+        gk, gv = kb.read(q, np.uint64, n), vb.read(q, np.uint32, n)
+        same = gk[1:] == gk[:-1]
+        ok = bool(np.all(gk[1:] >= gk[:-1]) and np.array_equal(k[gv], gk)
+                  and np.all(np.bincount(gv, minlength=n) == 1)
+                  and np.all(gv[1:][same] > gv[:-1][same]))
         res[f"satradix_kv_2pow{n.bit_length() - 1}_u64_u32"] = {
             "Gpairs/s": round(n / (ms * 1e-3) / 1e9, 3), "ms": round(ms, 3),
             "model_bytes_per_pair": 200,
-            "frac_of_peak": round(200.0 * n / (ms * 1e-3) / 1e9 / peak, 4)}
+            "frac_of_peak": round(200.0 * n / (ms * 1e-3) / 1e9 / peak, 4),
+            "result_check": "stable sort of the pairs" if ok else "FAILED"}
         for x in (kp, vp, kb, vb, s):
             x.destroy()
 

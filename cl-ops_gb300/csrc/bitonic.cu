@@ -388,68 +388,21 @@ abitonic_tile_sort_r(T *data) {
 	rstore_l0(g, r, s, tid);
 }
 
-// Steps 14..1 of `stage` (> 14) for every tile, by persistent CTAs (one
-// per SM) that bulk-copy the next tile into a landing buffer in shared
-// memory while the current tile's compare-exchanges run: the copy engine
-// streams tile t + 1 in during tile t's register phases and transposes,
-// and the results leave with 16-byte stores from registers. The landing
-// buffer is read in layout L(9) (a warp's 32 accesses are 32 consecutive
-// words) and released, then refilled, before the current tile's phases.
-// Every wait is bounded; a wait that runs out is reported in the context's
-// status word, after which the CTA waits (bounded) for its copy and ends.
+// Steps 14..1 of `stage` (> 14) for every tile.
 template <typename T>
-constexpr size_t finish_tma_pad_bytes() {
-	return (((size_t)(1u << kRLog) + (1u << kRLog) / 32 + 1) * sizeof(T) + 127) / 128 * 128;
-}
-template <typename T>
-constexpr size_t finish_tma_smem() {
-	return finish_tma_pad_bytes<T>() + ((size_t)1 << kRLog) * sizeof(T) + 16;
-}
-
-template <typename T>
-__global__ void __launch_bounds__(kRThreads, 1)
-abitonic_tile_finish_tma(T *data, int stage, uint32_t tiles, int *dev_status) {
-	constexpr uint32_t kTileBytes = (1u << kRLog) * sizeof(T);
-	extern __shared__ __align__(128) unsigned char smem_raw[];
+__global__ void __launch_bounds__(kRThreads, 2)
+abitonic_tile_finish_r(T *data, int stage) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
 	T *s = reinterpret_cast<T *>(smem_raw);
-	T *land = reinterpret_cast<T *>(smem_raw + finish_tma_pad_bytes<T>());
-	uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + finish_tma_pad_bytes<T>() + kTileBytes);
 	const uint32_t tid = threadIdx.x;
-	uint32_t tile = blockIdx.x;
-	if (tile >= tiles) return;
-	if (tid == 0) {
-		dev::mbar_init(bar, 1);
-		dev::fence_mbar_init();
-	}
-	__syncthreads();
-	if (tid == 0) {
-		dev::mbar_arrive_expect_tx(bar, kTileBytes);
-		dev::bulk_load(land, data + ((size_t)tile << kRLog), kTileBytes, bar);
-	}
-	uint32_t parity = 0;
-	for (; tile < tiles; tile += gridDim.x) {
-		const bool ok = dev::mbar_wait(bar, parity);
-		if (!__syncthreads_and(ok)) {
-			if (tid == 0) dev::report_timeout(dev_status, DEV_ERR_COPY_TIMEOUT, (int)tile);
-			dev::mbar_wait(bar, parity);  // the copy in flight, bounded
-			return;
-		}
-		parity ^= 1u;
-		T r[kRN];
+	const size_t tile_base = (size_t)blockIdx.x << kRLog;
+	T *g = data + tile_base;
+	T r[kRN];
 #pragma unroll
-		for (int m = 0; m < kRN; ++m) r[m] = land[lidx<9>(tid, m)];
-		__syncthreads();
-		const uint32_t next = tile + gridDim.x;
-		if (tid == 0 && next < tiles) {
-			dev::fence_proxy_async_shared();
-			dev::mbar_arrive_expect_tx(bar, kTileBytes);
-			dev::bulk_load(land, data + ((size_t)next << kRLog), kTileBytes, bar);
-		}
-		const size_t tile_base = (size_t)tile << kRLog;
-		if ((tile_base >> stage) & 1) full_stage_uniform<true>(r, s, tid);
-		else full_stage_uniform<false>(r, s, tid);
-		rstore_l0(data + tile_base, r, s, tid);
-	}
+	for (int m = 0; m < kRN; ++m) r[m] = g[lidx<9>(tid, m)];
+	if ((tile_base >> stage) & 1) full_stage_uniform<true>(r, s, tid);
+	else full_stage_uniform<false>(r, s, tid);
+	rstore_l0(g, r, s, tid);
 }
 
 template <typename T>
@@ -486,7 +439,7 @@ int default_tile_log2() {
 
 template <typename T>
 cudaError_t run_abitonic(T *d, size_t N, int max_ps, int max_sfs,
-	CCLContext *ctx, cudaStream_t s, unsigned &launches) {
+	cudaStream_t s, unsigned &launches) {
 	const int logN = ilog2(N);
 	int t = std::min(default_tile_log2<T>(), logN);
 	if (max_sfs >= 1 && max_sfs < t) t = max_sfs;
@@ -518,8 +471,8 @@ cudaError_t run_abitonic(T *d, size_t N, int max_ps, int max_sfs,
 			e = cudaFuncSetAttribute(abitonic_tile_sort_r<T>,
 				cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 			if (e == cudaSuccess)
-				e = cudaFuncSetAttribute(abitonic_tile_finish_tma<T>,
-					cudaFuncAttributeMaxDynamicSharedMemorySize, (int)finish_tma_smem<T>());
+				e = cudaFuncSetAttribute(abitonic_tile_finish_r<T>,
+					cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 			if (e != cudaSuccess) return e;
 		}
 	}
@@ -556,9 +509,7 @@ cudaError_t run_abitonic(T *d, size_t N, int max_ps, int max_sfs,
 		}
 		KernelTimer tf("abitonic_tile_finish", s, pass_bytes);
 		if constexpr (sizeof(T) <= 4) {
-			if (rtiles)
-				abitonic_tile_finish_tma<T><<<(unsigned)std::min<size_t>(tiles, ctx->sm_count),
-					kRThreads, finish_tma_smem<T>(), s>>>(d, stage, (uint32_t)tiles, ctx->d_status);
+			if (rtiles) abitonic_tile_finish_r<T><<<(unsigned)tiles, kRThreads, smem, s>>>(d, stage);
 		}
 		if (!rtiles) abitonic_tile_finish<T><<<(unsigned)tiles, threads, smem, s>>>(d, t, stage, maxg);
 		tf.stop();
@@ -606,7 +557,7 @@ cudaError_t bitonic_typed(void *data, size_t n, bool simple, int max_ps,
 	}
 	if (e == cudaSuccess)
 		e = simple ? run_sbitonic<T>(d, N, s, launches)
-				   : run_abitonic<T>(d, N, max_ps, max_sfs, ctx, s, launches);
+				   : run_abitonic<T>(d, N, max_ps, max_sfs, s, launches);
 	if (tmp) {
 		if (e == cudaSuccess)
 			e = cudaMemcpyAsync(data, tmp, n * sizeof(T), cudaMemcpyDeviceToDevice, s);

@@ -111,52 +111,5 @@ __device__ __forceinline__ uint32_t unit_rank_digit(uint32_t *w, uint32_t l16,
 	return (v >> 16) + below;
 }
 
-// ------------------------------------------------ bulk copies (TMA)
-// One-dimensional bulk copy global -> shared of this CTA, completing on an
-// mbarrier (no tensor map, no multicast). Both addresses 16-byte aligned,
-// size a multiple of 16 bytes.
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-	return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(bar)), "r"(count)
-		: "memory");
-}
-// Makes an mbarrier's initialisation visible to the bulk-copy unit.
-__device__ __forceinline__ void fence_mbar_init() {
-	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-// Orders this thread's earlier shared-memory accesses before later bulk
-// copies into shared memory.
-__device__ __forceinline__ void fence_proxy_async_shared() {
-	asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
-	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-		:: "r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-	uint32_t ok;
-	asm volatile(
-		"{\n\t.reg .pred p;\n\t"
-		"mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-		"selp.u32 %0, 1, 0, p;\n\t}"
-		: "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
-	return ok != 0;
-}
-// Bounded wait for the phase of the given parity: false after kSpinLimit
-// tries (each try may suspend the thread for a short while).
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-	for (uint32_t i = 0; i < kSpinLimit; ++i)
-		if (mbar_try_wait(bar, parity)) return true;
-	return false;
-}
-__device__ __forceinline__ void bulk_load(void *dst_smem, const void *src, uint32_t bytes,
-	uint64_t *bar) {
-	asm volatile(
-		"cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-		:: "r"(smem_u32(dst_smem)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
-}
-
 }  // namespace dev
 }  // namespace clo
