@@ -128,6 +128,10 @@ bool cuda_ok(cudaError_t e, GError **err, const char *what) {
 	if (e == cudaSuccess) return true;
 	set_error(err, CLO_ERROR_LIBRARY, "%s: CUDA error %d (%s)", what, (int)e,
 		cudaGetErrorString(e));
+	// The error is reported here; clear the runtime's last-error state so a
+	// later cudaGetLastError (after another call's launch) does not return
+	// it again. A sticky error stays whatever is done here.
+	cudaGetLastError();
 	return false;
 }
 

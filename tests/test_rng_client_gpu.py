@@ -94,6 +94,14 @@ def test_client_program_errors(clops, ctx, queue):
     try:
         with pytest.raises(clops.CloError):
             prg.kernel("missing")
+        # A reported error does not resurface in the next call.
+        sc = clops.Scanner(ctx, 0, 1)
+        a = np.arange(100, dtype=np.int8)
+        bi, bo = clops.Buffer.from_array(ctx, queue, a), clops.Buffer(ctx, 100)
+        clops.wait(sc.scan_device(queue, bi, bo, 100))
+        np.testing.assert_array_equal(bo.read(queue, np.uint8, 100), oracle.scan(a, 0, np.uint8))
+        for x in (bi, bo, sc):
+            x.destroy()
         k = prg.kernel("k")
         out = clops.Buffer(ctx, 4 * 1000)
         with pytest.raises(clops.CloError) as ei:
