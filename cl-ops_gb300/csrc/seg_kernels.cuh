@@ -251,13 +251,6 @@ seg_pass(const K *__restrict__ kin, K *__restrict__ kout, SegPassArgs a) {
 		const uint64_t seg_a = s_seg[0], seg_e = s_seg[1];
 		const uint64_t ubase = seg_a + (uint64_t)ti * TILE + (uint64_t)unit * UKEYS;
 
-		// Keys of this unit inside the segment; a segment's last tile is
-		// partial, and keys past its end are neither counted nor ranked
-		// (rounds wholly past it are skipped by the whole warp: the upper
-		// unit of a warp never holds a key below the lower unit's).
-		const int64_t left = (int64_t)(seg_e - ubase);
-		const uint32_t nvalid = left <= 0 ? 0u : left >= UKEYS ? (uint32_t)UKEYS : (uint32_t)left;
-		const uint32_t wvalid = __shfl_sync(0xffffffffu, nvalid, 0);
 		K k[KPT];
 #pragma unroll
 		for (int j = 0; j < KPT; ++j) {
@@ -274,8 +267,7 @@ seg_pass(const K *__restrict__ kin, K *__restrict__ kout, SegPassArgs a) {
 		}
 		if (lane == 31) s_misc[16 + dw] = hinc;
 #pragma unroll
-		for (int j = 0; j < KPT; ++j)
-			if ((uint32_t)j * 16 + l16 < nvalid) atomicAdd(my_cnt + digit_of(k[j], shift), cnt_inc);
+		for (int j = 0; j < KPT; ++j) atomicAdd(my_cnt + digit_of(k[j], shift), cnt_inc);
 		__syncthreads();
 		uint32_t gbase = hinc - hv;
 #pragma unroll
@@ -328,15 +320,10 @@ seg_pass(const K *__restrict__ kin, K *__restrict__ kout, SegPassArgs a) {
 		}
 		__syncthreads();
 		K *sk = reinterpret_cast<K *>(s_stage);
-		// Keys past the end (digit 255, last in index order) rank after the
-		// tile's last digit run, at positions the write-out never reads.
 #pragma unroll
 		for (int j = 0; j < KPT; ++j) {
-			if ((uint32_t)j * 16 < wvalid) {
-				const uint32_t pos = dev::unit_rank_digit(my_rank + digit_of(k[j], shift), l16,
-					lt16);
-				if (pos < (uint32_t)TILE) sk[pos] = k[j];
-			}
+			const uint32_t pos = dev::unit_rank_digit(my_rank + digit_of(k[j], shift), l16, lt16);
+			if (pos < (uint32_t)TILE) sk[pos] = k[j];
 		}
 		// Lookback over the segment's preceding tiles (bounded waits).
 		uint32_t excl = 0;
@@ -364,17 +351,12 @@ seg_pass(const K *__restrict__ kin, K *__restrict__ kout, SegPassArgs a) {
 		s_tile_off[pd] = gbase + excl - to;
 		__syncthreads();
 		if (tid == 0) claim();
-		const uint64_t tile_a = seg_a + (uint64_t)ti * TILE;
-		const uint32_t tile_keys = seg_e - tile_a < (uint64_t)TILE ? (uint32_t)(seg_e - tile_a)
-			: (uint32_t)TILE;
 #pragma unroll
 		for (int i = 0; i < KPT; ++i) {
-			const uint32_t q = (uint32_t)(i * kLThreads + tid);
-			if (q < tile_keys) {
-				const K key = sk[q];
-				const uint64_t o = seg_a + (uint32_t)(s_tile_off[digit_of(key, shift)] + q);
-				if (o < seg_e) kout[o] = key;
-			}
+			const int q = i * kLThreads + tid;
+			const K key = sk[q];
+			const uint64_t o = seg_a + (uint32_t)(s_tile_off[digit_of(key, shift)] + (uint32_t)q);
+			if (o < seg_e) kout[o] = key;
 		}
 		__syncthreads();
 	}

@@ -191,72 +191,40 @@ __global__ void __launch_bounds__(256) seg_tiles(const uint64_t *off,
 	}
 }
 
-// Histograms of every digit position of every large segment. CTAs of 1024
-// threads take chunks of kUpChunk consecutive tiles (a segment's tiles are
-// consecutive) and count into lane columns: the counter of digit d of lane
-// l is the (d & 1) 16-bit half of word (d >> 1) * 32 + l of the position's
-// 16 KB, so a warp's 32 adds hit 32 banks whatever the digits. When the
-// segment changes, and at the chunk's end, the columns are summed into the
-// segment's global histogram and cleared. A half counts at most one chunk
-// of keys of one lane over 32 warps (8 x 14336 / 32 < 2^16).
-constexpr int kUpThreads = 1024;
-constexpr uint32_t kUpChunk = 8;
-
-template <int PASSES>
-constexpr size_t seg_up_smem() {
-	return (size_t)PASSES * (kRadix / 2) * 32 * 4;
-}
-
+// Histograms of every digit position of every large segment: one CTA per
+// tile at a time, shared-memory counts added to the segment's histograms.
 template <typename K, int PASSES>
-__global__ void __launch_bounds__(kUpThreads) seg_upsweep(const K *keys, const uint64_t *tstart,
-	const uint32_t *tile_seg, const ulonglong2 *tile_span, const uint2 *tile_x, uint32_t S,
+__global__ void __launch_bounds__(256) seg_upsweep(const K *keys, const uint64_t *off,
+	const uint64_t *tstart, const uint32_t *tile_seg, uint32_t S,
 	uint32_t *seg_hist, uint32_t tile) {
-	constexpr int kPosWords = (kRadix / 2) * 32;
-	extern __shared__ __align__(16) uint32_t cols[];
+	__shared__ uint32_t h[PASSES * kRadix];
+	__shared__ uint64_t s_a, s_e;
+	__shared__ uint32_t s_lr;
 	const uint32_t T = (uint32_t)(tstart[S] >> 32);
-	const int lane = threadIdx.x & 31;
-	for (int i = threadIdx.x; i < PASSES * kPosWords; i += kUpThreads) cols[i] = 0;
-	__syncthreads();
-	auto flush = [&](uint32_t lr) {
-		__syncthreads();
-		uint32_t *dst = seg_hist + (size_t)lr * PASSES * kRadix;
-		for (int b = threadIdx.x; b < PASSES * kRadix; b += kUpThreads) {
-			const int p = b / kRadix, d = b % kRadix;
-			const uint32_t *row = cols + p * kPosWords + (d >> 1) * 32;
-			const int hs = (d & 1) << 4;
-			uint32_t v = 0;
-#pragma unroll 8
-			for (int c = 0; c < 32; ++c) v += (row[(c + lane) & 31] >> hs) & 0xFFFFu;
-			if (v) atomicAdd(dst + b, v);
+	for (uint32_t t = blockIdx.x; t < T; t += gridDim.x) {
+		for (int i = threadIdx.x; i < PASSES * kRadix; i += blockDim.x) h[i] = 0;
+		if (threadIdx.x == 0) {
+			const uint32_t s = tile_seg[t];
+			const uint64_t ts = tstart[s];
+			const uint64_t a = off[s] + (uint64_t)(t - (uint32_t)(ts >> 32)) * tile;
+			const uint64_t e = off[s + 1];
+			s_a = a;
+			s_e = a + tile < e ? a + tile : e;
+			s_lr = (uint32_t)ts;
 		}
 		__syncthreads();
-		for (int i = threadIdx.x; i < PASSES * kPosWords; i += kUpThreads) cols[i] = 0;
-		__syncthreads();
-	};
-	for (uint32_t c0 = blockIdx.x * kUpChunk; c0 < T; c0 += gridDim.x * kUpChunk) {
-		const uint32_t c1 = c0 + kUpChunk < T ? c0 + kUpChunk : T;
-		uint32_t cur = tile_seg[c0];
-		uint32_t lr = tile_x[c0].y;
-		for (uint32_t t = c0; t < c1; ++t) {
-			const uint32_t sg = tile_seg[t];
-			if (sg != cur) {
-				flush(lr);
-				cur = sg;
-				lr = tile_x[t].y;
-			}
-			const ulonglong2 span = tile_span[t];
-			const uint64_t a = span.x + (uint64_t)tile_x[t].x * tile;
-			const uint64_t e = a + tile < span.y ? a + tile : span.y;
-			for (uint64_t i = a + threadIdx.x; i < e; i += kUpThreads) {
-				const K key = keys[i];
+		const uint64_t a = s_a, e = s_e;
+		for (uint64_t i = a + threadIdx.x; i < e; i += blockDim.x) {
+			const K key = keys[i];
 #pragma unroll
-				for (int p = 0; p < PASSES; ++p) {
-					const uint32_t d = digit_of(key, p * kRadixBits);
-					atomicAdd(cols + p * kPosWords + (d >> 1) * 32 + lane, 1u << ((d & 1) << 4));
-				}
-			}
+			for (int p = 0; p < PASSES; ++p)
+				atomicAdd(&h[p * kRadix + digit_of(key, p * kRadixBits)], 1u);
 		}
-		flush(lr);
+		__syncthreads();
+		uint32_t *dst = seg_hist + (size_t)s_lr * PASSES * kRadix;
+		for (int i = threadIdx.x; i < PASSES * kRadix; i += blockDim.x)
+			if (h[i]) atomicAdd(dst + i, h[i]);
+		__syncthreads();
 	}
 }
 
@@ -293,35 +261,19 @@ __global__ void __launch_bounds__(256) seg_copy_short(K *dst, const K *src,
 	}
 }
 
-template <typename K, int PASSES>
-void launch_seg_upsweep_p(uint32_t grid, cudaStream_t s, const K *keys, const uint64_t *tstart,
-	const uint32_t *tile_seg, const ulonglong2 *tile_span, const uint2 *tile_x, uint32_t S,
-	uint32_t *seg_hist, uint32_t tile) {
-	constexpr size_t smem = seg_up_smem<PASSES>();
-	auto kern = seg_upsweep<K, PASSES>;
-	if (smem > 48 * 1024)
-		cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-	kern<<<grid, kUpThreads, smem, s>>>(keys, tstart, tile_seg, tile_span, tile_x, S, seg_hist,
-		tile);
-}
-
 template <typename K>
-void launch_seg_upsweep(int passes, uint64_t t_bound, int sm_count, cudaStream_t s,
-	const K *keys, const uint64_t *tstart, const uint32_t *tile_seg, const ulonglong2 *tile_span,
-	const uint2 *tile_x, uint32_t S, uint32_t *seg_hist, uint32_t tile) {
-	// Two CTAs per SM up to four positions (64 KB each), one beyond.
-	const uint64_t per_sm = passes <= 4 ? 2 : 1;
-	const uint32_t grid = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(
-		(t_bound + kUpChunk - 1) / kUpChunk, per_sm * (uint64_t)sm_count));
+void launch_seg_upsweep(int passes, uint32_t grid, cudaStream_t s, const K *keys,
+	const uint64_t *off, const uint64_t *tstart, const uint32_t *tile_seg, uint32_t S,
+	uint32_t *seg_hist, uint32_t tile) {
 	switch (passes) {
-	case 1: launch_seg_upsweep_p<K, 1>(grid, s, keys, tstart, tile_seg, tile_span, tile_x, S, seg_hist, tile); break;
-	case 2: launch_seg_upsweep_p<K, 2>(grid, s, keys, tstart, tile_seg, tile_span, tile_x, S, seg_hist, tile); break;
-	case 3: launch_seg_upsweep_p<K, 3>(grid, s, keys, tstart, tile_seg, tile_span, tile_x, S, seg_hist, tile); break;
-	case 4: launch_seg_upsweep_p<K, 4>(grid, s, keys, tstart, tile_seg, tile_span, tile_x, S, seg_hist, tile); break;
-	case 5: launch_seg_upsweep_p<K, 5>(grid, s, keys, tstart, tile_seg, tile_span, tile_x, S, seg_hist, tile); break;
-	case 6: launch_seg_upsweep_p<K, 6>(grid, s, keys, tstart, tile_seg, tile_span, tile_x, S, seg_hist, tile); break;
-	case 7: launch_seg_upsweep_p<K, 7>(grid, s, keys, tstart, tile_seg, tile_span, tile_x, S, seg_hist, tile); break;
-	default: launch_seg_upsweep_p<K, 8>(grid, s, keys, tstart, tile_seg, tile_span, tile_x, S, seg_hist, tile); break;
+	case 1: seg_upsweep<K, 1><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist, tile); break;
+	case 2: seg_upsweep<K, 2><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist, tile); break;
+	case 3: seg_upsweep<K, 3><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist, tile); break;
+	case 4: seg_upsweep<K, 4><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist, tile); break;
+	case 5: seg_upsweep<K, 5><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist, tile); break;
+	case 6: seg_upsweep<K, 6><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist, tile); break;
+	case 7: seg_upsweep<K, 7><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist, tile); break;
+	default: seg_upsweep<K, 8><<<grid, 256, 0, s>>>(keys, off, tstart, tile_seg, S, seg_hist, tile); break;
 	}
 }
 
@@ -413,9 +365,11 @@ cudaError_t seg_sort_typed(K *keys, uint64_t n_cap, const uint64_t *off, uint32_
 			e = cudaGetLastError();
 		}
 		if (e == cudaSuccess) {
+			const uint32_t grid = (uint32_t)std::min<uint64_t>(T_bound,
+				(uint64_t)ctx->sm_count * 8);
 			KernelTimer t("seg_upsweep", s, 0.0);
-			launch_seg_upsweep<K>(passes, T_bound, ctx->sm_count, s, keys, tstart, tile_seg,
-				tile_span, tile_x, S, seg_hist, LTILE);
+			launch_seg_upsweep<K>(passes, grid, s, keys, off, tstart, tile_seg, S, seg_hist,
+				LTILE);
 			t.stop();
 			launches++;
 			e = cudaGetLastError();
