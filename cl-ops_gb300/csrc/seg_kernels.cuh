@@ -6,6 +6,7 @@
 #pragma once
 
 #include <algorithm>
+#include <type_traits>
 
 #include "dev_common.cuh"
 #include "seg_common.cuh"
@@ -249,115 +250,142 @@ seg_pass(const K *__restrict__ kin, K *__restrict__ kout, SegPassArgs a) {
 		const uint32_t ti = s_misc[1];
 		const uint32_t lr = s_misc[2];
 		const uint64_t seg_a = s_seg[0], seg_e = s_seg[1];
-		const uint64_t ubase = seg_a + (uint64_t)ti * TILE + (uint64_t)unit * UKEYS;
+		// One copy of the tile's steps for full tiles and one for a
+		// segment's partial last tile.
+		auto do_tile = [&](auto partial_tag) {
+			constexpr bool PARTIAL = decltype(partial_tag)::value;
+			const uint64_t ubase = seg_a + (uint64_t)ti * TILE + (uint64_t)unit * UKEYS;
 
-		K k[KPT];
+			// A segment's last tile is partial: its keys past the segment's end
+			// are neither counted nor ranked, and rounds wholly past the end
+			// are skipped by the whole warp (the upper unit of a warp never
+			// holds a key below the lower unit's). Full tiles take none of
+			// these tests.
+			uint32_t nvalid = UKEYS, wvalid = UKEYS;
+			if constexpr (PARTIAL) {
+				const int64_t left = (int64_t)(seg_e - ubase);
+				nvalid = left <= 0 ? 0u : left >= UKEYS ? (uint32_t)UKEYS : (uint32_t)left;
+				wvalid = __shfl_sync(0xffffffffu, nvalid, 0);
+			}
+			K k[KPT];
 #pragma unroll
-		for (int j = 0; j < KPT; ++j) {
-			const uint64_t idx = ubase + (uint64_t)j * 16 + l16;
-			k[j] = idx < seg_e ? kin[idx] : (K)~(K)0;
-		}
-		// Digit base within the segment: exclusive scan of its histogram.
-		const uint32_t hv = a.seg_hist[(size_t)lr * a.hist_stride + pd];
-		uint32_t hinc = hv;
-#pragma unroll
-		for (int d = 1; d < 32; d <<= 1) {
-			const uint32_t t = __shfl_up_sync(0xffffffffu, hinc, d);
-			if (lane >= d) hinc += t;
-		}
-		if (lane == 31) s_misc[16 + dw] = hinc;
-#pragma unroll
-		for (int j = 0; j < KPT; ++j) atomicAdd(my_cnt + digit_of(k[j], shift), cnt_inc);
-		__syncthreads();
-		uint32_t gbase = hinc - hv;
-#pragma unroll
-		for (int w = 0; w < 8; ++w)
-			if (w < dw) gbase += s_misc[16 + w];
-		// Unit prefixes of digit pd in unit order (low halves: units
-		// 0..7, high halves: units 8..15); rows cleared as they are read.
-		uint32_t c2[HALF];
-#pragma unroll
-		for (int i = 0; i < HALF; ++i) {
-			c2[i] = s_cnt[seg_row(i) + pd];
-			s_cnt[seg_row(i) + pd] = 0;
-		}
-		uint32_t run = 0;
-#pragma unroll
-		for (int i = 0; i < HALF; ++i) {
-			const uint32_t lo = c2[i] & 0xFFFFu;
-			c2[i] = (c2[i] & 0xFFFF0000u) | run;
-			run += lo;
-		}
-#pragma unroll
-		for (int i = 0; i < HALF; ++i) {
-			const uint32_t hi = c2[i] >> 16;
-			c2[i] = (c2[i] & 0xFFFFu) | (run << 16);
-			run += hi;
-		}
-		const uint32_t sum = run;
-		uint32_t *st = a.status + (size_t)tile * kRadix + pd;
-		dev::st_relaxed_u32(st, (ti == 0 ? kStPrefix : kStAgg) | sum);
-		a.status_next[(size_t)tile * kRadix + pd] = 0;
-		{
-			uint32_t inc = sum;
+			for (int j = 0; j < KPT; ++j) {
+				const uint64_t idx = ubase + (uint64_t)j * 16 + l16;
+				if constexpr (PARTIAL) k[j] = idx < seg_e ? kin[idx] : (K)~(K)0;
+				else k[j] = kin[idx];
+			}
+			// Digit base within the segment: exclusive scan of its histogram.
+			const uint32_t hv = a.seg_hist[(size_t)lr * a.hist_stride + pd];
+			uint32_t hinc = hv;
 #pragma unroll
 			for (int d = 1; d < 32; d <<= 1) {
-				const uint32_t t = __shfl_up_sync(0xffffffffu, inc, d);
-				if (lane >= d) inc += t;
+				const uint32_t t = __shfl_up_sync(0xffffffffu, hinc, d);
+				if (lane >= d) hinc += t;
 			}
-			if (lane == 31) s_misc[8 + dw] = inc;
-			s_part[pd] = inc - sum;
-		}
-		__syncthreads();
-		uint32_t to = s_part[pd];
+			if (lane == 31) s_misc[16 + dw] = hinc;
 #pragma unroll
-		for (int w = 0; w < 8; ++w)
-			if (w < dw) to += s_misc[8 + w];
+			for (int j = 0; j < KPT; ++j)
+				if (!PARTIAL || (uint32_t)j * 16 + l16 < nvalid)
+					atomicAdd(my_cnt + digit_of(k[j], shift), cnt_inc);
+			__syncthreads();
+			uint32_t gbase = hinc - hv;
 #pragma unroll
-		for (int i = 0; i < HALF; ++i) {
-			s_rank[seg_row(i) + pd] = (to + (c2[i] & 0xFFFFu)) << 16;
-			s_rank[seg_row(i + HALF) + pd] = (to + (c2[i] >> 16)) << 16;
-		}
-		__syncthreads();
-		K *sk = reinterpret_cast<K *>(s_stage);
+			for (int w = 0; w < 8; ++w)
+				if (w < dw) gbase += s_misc[16 + w];
+			// Unit prefixes of digit pd in unit order (low halves: units
+			// 0..7, high halves: units 8..15); rows cleared as they are read.
+			uint32_t c2[HALF];
 #pragma unroll
-		for (int j = 0; j < KPT; ++j) {
-			const uint32_t pos = dev::unit_rank_digit(my_rank + digit_of(k[j], shift), l16, lt16);
-			if (pos < (uint32_t)TILE) sk[pos] = k[j];
-		}
-		// Lookback over the segment's preceding tiles (bounded waits).
-		uint32_t excl = 0;
-		if (ti > 0) {
-			long long base = (long long)tile - 1;
-			uint32_t iter = 0;
-			bool done = seg_lookback_window<kSegLookWindow>(a.status, pd, base, excl);
-			while (!done && base >= 0) {
-				uint32_t sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + pd);
-				while ((sv & ~kStValue) == 0) {
-					if (++iter >= dev::kSpinLimit) break;
-					dev::backoff(iter);
-					sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + pd);
-				}
-				if ((sv & ~kStValue) == 0) {
-					dev::report_timeout(a.dev_status, DEV_ERR_LOOKBACK_TIMEOUT, (int)tile);
-					break;
-				}
-				done = seg_lookback_window<kSegLookWindow>(a.status, pd, base, excl);
+			for (int i = 0; i < HALF; ++i) {
+				c2[i] = s_cnt[seg_row(i) + pd];
+				s_cnt[seg_row(i) + pd] = 0;
 			}
-			dev::st_relaxed_u32(st, kStPrefix | (excl + sum));
-		}
-		// Output offset (within the segment) of staged position q of digit
-		// d is q + G[d] (modulo 2^32).
-		s_tile_off[pd] = gbase + excl - to;
-		__syncthreads();
-		if (tid == 0) claim();
+			uint32_t run = 0;
 #pragma unroll
-		for (int i = 0; i < KPT; ++i) {
-			const int q = i * kLThreads + tid;
-			const K key = sk[q];
-			const uint64_t o = seg_a + (uint32_t)(s_tile_off[digit_of(key, shift)] + (uint32_t)q);
-			if (o < seg_e) kout[o] = key;
-		}
+			for (int i = 0; i < HALF; ++i) {
+				const uint32_t lo = c2[i] & 0xFFFFu;
+				c2[i] = (c2[i] & 0xFFFF0000u) | run;
+				run += lo;
+			}
+#pragma unroll
+			for (int i = 0; i < HALF; ++i) {
+				const uint32_t hi = c2[i] >> 16;
+				c2[i] = (c2[i] & 0xFFFFu) | (run << 16);
+				run += hi;
+			}
+			const uint32_t sum = run;
+			uint32_t *st = a.status + (size_t)tile * kRadix + pd;
+			dev::st_relaxed_u32(st, (ti == 0 ? kStPrefix : kStAgg) | sum);
+			a.status_next[(size_t)tile * kRadix + pd] = 0;
+			{
+				uint32_t inc = sum;
+#pragma unroll
+				for (int d = 1; d < 32; d <<= 1) {
+					const uint32_t t = __shfl_up_sync(0xffffffffu, inc, d);
+					if (lane >= d) inc += t;
+				}
+				if (lane == 31) s_misc[8 + dw] = inc;
+				s_part[pd] = inc - sum;
+			}
+			__syncthreads();
+			uint32_t to = s_part[pd];
+#pragma unroll
+			for (int w = 0; w < 8; ++w)
+				if (w < dw) to += s_misc[8 + w];
+#pragma unroll
+			for (int i = 0; i < HALF; ++i) {
+				s_rank[seg_row(i) + pd] = (to + (c2[i] & 0xFFFFu)) << 16;
+				s_rank[seg_row(i + HALF) + pd] = (to + (c2[i] >> 16)) << 16;
+			}
+			__syncthreads();
+			K *sk = reinterpret_cast<K *>(s_stage);
+#pragma unroll
+			for (int j = 0; j < KPT; ++j) {
+				if (!PARTIAL || (uint32_t)j * 16 < wvalid) {
+					const uint32_t pos = dev::unit_rank_digit(my_rank + digit_of(k[j], shift), l16,
+						lt16);
+					if (pos < (uint32_t)TILE) sk[pos] = k[j];
+				}
+			}
+			// Lookback over the segment's preceding tiles (bounded waits).
+			uint32_t excl = 0;
+			if (ti > 0) {
+				long long base = (long long)tile - 1;
+				uint32_t iter = 0;
+				bool done = seg_lookback_window<kSegLookWindow>(a.status, pd, base, excl);
+				while (!done && base >= 0) {
+					uint32_t sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + pd);
+					while ((sv & ~kStValue) == 0) {
+						if (++iter >= dev::kSpinLimit) break;
+						dev::backoff(iter);
+						sv = dev::ld_relaxed_u32(a.status + (size_t)base * kRadix + pd);
+					}
+					if ((sv & ~kStValue) == 0) {
+						dev::report_timeout(a.dev_status, DEV_ERR_LOOKBACK_TIMEOUT, (int)tile);
+						break;
+					}
+					done = seg_lookback_window<kSegLookWindow>(a.status, pd, base, excl);
+				}
+				dev::st_relaxed_u32(st, kStPrefix | (excl + sum));
+			}
+			// Output offset (within the segment) of staged position q of digit
+			// d is q + G[d] (modulo 2^32).
+			s_tile_off[pd] = gbase + excl - to;
+			__syncthreads();
+			if (tid == 0) claim();
+			const uint32_t tile_keys = PARTIAL ? (uint32_t)(seg_e - (seg_a + (uint64_t)ti * TILE))
+				: (uint32_t)TILE;
+#pragma unroll
+			for (int i = 0; i < KPT; ++i) {
+				const int q = i * kLThreads + tid;
+				if (PARTIAL && (uint32_t)q >= tile_keys) continue;
+				const K key = sk[q];
+				const uint64_t o = seg_a + (uint32_t)(s_tile_off[digit_of(key, shift)] + (uint32_t)q);
+				if (o < seg_e) kout[o] = key;
+			}
+		};
+		if (seg_e - (seg_a + (uint64_t)ti * TILE) >= (uint64_t)TILE) do_tile(std::false_type{});
+		else do_tile(std::true_type{});
 		__syncthreads();
 	}
 }
