@@ -193,6 +193,7 @@ __global__ void __launch_bounds__(256) seg_tiles(const uint64_t *off,
 
 // Histograms of every digit position of every large segment: one CTA per
 // tile at a time, shared-memory counts added to the segment's histograms.
+constexpr int kSegUpLoads = 8;
 template <typename K, int PASSES>
 __global__ void __launch_bounds__(256) seg_upsweep(const K *keys, const uint64_t *off,
 	const uint64_t *tstart, const uint32_t *tile_seg, uint32_t S,
@@ -214,12 +215,21 @@ __global__ void __launch_bounds__(256) seg_upsweep(const K *keys, const uint64_t
 		}
 		__syncthreads();
 		const uint64_t a = s_a, e = s_e;
-		for (uint64_t i = a + threadIdx.x; i < e; i += blockDim.x) {
-			const K key = keys[i];
+		auto count = [&](K key) {
 #pragma unroll
 			for (int p = 0; p < PASSES; ++p)
 				atomicAdd(&h[p * kRadix + digit_of(key, p * kRadixBits)], 1u);
+		};
+		// kSegUpLoads loads in flight per thread, then their counts.
+		uint64_t i = a + threadIdx.x;
+		for (; i + (uint64_t)(kSegUpLoads - 1) * blockDim.x < e; i += (uint64_t)kSegUpLoads * blockDim.x) {
+			K kk[kSegUpLoads];
+#pragma unroll
+			for (int u = 0; u < kSegUpLoads; ++u) kk[u] = keys[i + (uint64_t)u * blockDim.x];
+#pragma unroll
+			for (int u = 0; u < kSegUpLoads; ++u) count(kk[u]);
 		}
+		for (; i < e; i += blockDim.x) count(keys[i]);
 		__syncthreads();
 		uint32_t *dst = seg_hist + (size_t)s_lr * PASSES * kRadix;
 		for (int i = threadIdx.x; i < PASSES * kRadix; i += blockDim.x)
