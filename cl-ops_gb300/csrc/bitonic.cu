@@ -267,11 +267,21 @@ __host__ __device__ constexpr uint32_t loff(int m) {
 
 template <int FROM, int TO, typename T>
 __device__ __forceinline__ void rtranspose(T (&r)[kRN], T *s, uint32_t tid) {
-	__syncthreads();
+	// L(0) and L(4) give a half-warp the same 512 consecutive elements
+	// (index bits 9..13 are its thread bits 4..8), so a transpose between
+	// them stays inside the warp's own part of the tile and needs only the
+	// warp to synchronise; the part's previous readers were this warp's
+	// threads (a transpose into L(0) or L(4) reads only the reader's part,
+	// and one into L(9) is always followed by one out of it, which starts
+	// with a CTA barrier).
+	constexpr bool kLocal = (FROM == 0 || FROM == 4) && (TO == 0 || TO == 4);
+	if constexpr (kLocal) __syncwarp();
+	else __syncthreads();
 	T *sf = s + lbase<FROM>(tid);
 #pragma unroll
 	for (int m = 0; m < kRN; ++m) sf[loff<FROM>(m)] = r[m];
-	__syncthreads();
+	if constexpr (kLocal) __syncwarp();
+	else __syncthreads();
 	const T *st = s + lbase<TO>(tid);
 #pragma unroll
 	for (int m = 0; m < kRN; ++m) r[m] = st[loff<TO>(m)];
