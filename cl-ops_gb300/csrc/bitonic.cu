@@ -15,7 +15,7 @@
 // abitonic groups the steps:
 //   - abitonic_tile_sort: each shared-memory tile of 2^t elements runs
 //     stages 1..t (the stage-t direction comes from the tile's index);
-//   - abitonic_global_steps<g>: g (<= 5) consecutive steps with strides
+//   - abitonic_global_steps<g>: g (<= 6) consecutive steps with strides
 //     >= the tile, 2^g elements per thread held in registers;
 //   - abitonic_tile_finish: the remaining steps t..1 of a stage in shared
 //     memory.
@@ -86,7 +86,7 @@ sbitonic_step(T *data, size_t half_n, int stage, int step) {
 // ------------------------------------------------- abitonic global steps
 // Steps step .. step-G+1 of `stage`, 2^G elements per thread.
 template <typename T, int G>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, G >= 6 ? 2 : 1)
 abitonic_global_steps(T *data, size_t groups, int stage, int step) {
 	size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
 	if (q >= groups) return;
@@ -97,16 +97,20 @@ abitonic_global_steps(T *data, size_t groups, int stage, int step) {
 	const size_t inc = (size_t)1 << lo_bits;
 	const bool desc = (base >> stage) & 1;
 	T r[1 << G];
+	T *p = data + base;
 #pragma unroll
-	for (int m = 0; m < (1 << G); ++m) r[m] = data[base + m * inc];
+	for (int m = 0; m < (1 << G); ++m) r[m] = p[m * inc];
 #pragma unroll
 	for (int s = G - 1; s >= 0; --s) {
 #pragma unroll
 		for (int m = 0; m < (1 << G); ++m)
 			if (!(m & (1 << s))) cmpxchg(r[m], r[m | (1 << s)], desc);
 	}
+	// With 64 elements a thread, the store addresses are computed afresh
+	// rather than kept from the loads (64 more live registers).
+	if constexpr (G >= 6) asm volatile("" : "+l"(p));
 #pragma unroll
-	for (int m = 0; m < (1 << G); ++m) data[base + m * inc] = r[m];
+	for (int m = 0; m < (1 << G); ++m) p[m * inc] = r[m];
 }
 
 // ------------------------------------------------- shared-memory tiles
@@ -343,17 +347,32 @@ __device__ __forceinline__ void full_stage_uniform(T (&r)[kRN], T *s, uint32_t t
 	rphase<0, 4, 0>(r, dir);
 }
 
+// A thread's 32 consecutive 4-byte elements move as 32-byte vectors when
+// the tile is 32-byte aligned (half the requests of 16-byte vectors, whose
+// lanes 128 bytes apart each touch a line of their own), else as 16-byte
+// vectors.
 template <typename T>
 __device__ __forceinline__ void rload_l0(T (&r)[kRN], const T *g, T *s, uint32_t tid) {
 	if constexpr (sizeof(T) == 4) {
-		const uint4 *src = reinterpret_cast<const uint4 *>(g + ((size_t)tid << kRE));
+		const T *src = g + ((size_t)tid << kRE);
+		if (((uintptr_t)g % 32) == 0) {
 #pragma unroll
-		for (int q = 0; q < kRN / 4; ++q) {
-			const uint4 v = src[q];
-			r[4 * q + 0] = __builtin_bit_cast(T, v.x);
-			r[4 * q + 1] = __builtin_bit_cast(T, v.y);
-			r[4 * q + 2] = __builtin_bit_cast(T, v.z);
-			r[4 * q + 3] = __builtin_bit_cast(T, v.w);
+			for (int q = 0; q < kRN / 8; ++q) {
+				uint32_t w[8];
+				dev::ld_v8(src + 8 * q, w);
+#pragma unroll
+				for (int e = 0; e < 8; ++e) r[8 * q + e] = __builtin_bit_cast(T, w[e]);
+			}
+		} else {
+			const uint4 *src4 = reinterpret_cast<const uint4 *>(src);
+#pragma unroll
+			for (int q = 0; q < kRN / 4; ++q) {
+				const uint4 v = src4[q];
+				r[4 * q + 0] = __builtin_bit_cast(T, v.x);
+				r[4 * q + 1] = __builtin_bit_cast(T, v.y);
+				r[4 * q + 2] = __builtin_bit_cast(T, v.z);
+				r[4 * q + 3] = __builtin_bit_cast(T, v.w);
+			}
 		}
 	} else {
 #pragma unroll
@@ -365,13 +384,24 @@ __device__ __forceinline__ void rload_l0(T (&r)[kRN], const T *g, T *s, uint32_t
 template <typename T>
 __device__ __forceinline__ void rstore_l0(T *g, T (&r)[kRN], T *s, uint32_t tid) {
 	if constexpr (sizeof(T) == 4) {
-		uint4 *dst = reinterpret_cast<uint4 *>(g + ((size_t)tid << kRE));
+		T *dst = g + ((size_t)tid << kRE);
+		if (((uintptr_t)g % 32) == 0) {
 #pragma unroll
-		for (int q = 0; q < kRN / 4; ++q)
-			dst[q] = make_uint4(__builtin_bit_cast(uint32_t, r[4 * q + 0]),
-				__builtin_bit_cast(uint32_t, r[4 * q + 1]),
-				__builtin_bit_cast(uint32_t, r[4 * q + 2]),
-				__builtin_bit_cast(uint32_t, r[4 * q + 3]));
+			for (int q = 0; q < kRN / 8; ++q) {
+				uint32_t w[8];
+#pragma unroll
+				for (int e = 0; e < 8; ++e) w[e] = __builtin_bit_cast(uint32_t, r[8 * q + e]);
+				dev::st_v8(dst + 8 * q, w);
+			}
+		} else {
+			uint4 *dst4 = reinterpret_cast<uint4 *>(dst);
+#pragma unroll
+			for (int q = 0; q < kRN / 4; ++q)
+				dst4[q] = make_uint4(__builtin_bit_cast(uint32_t, r[4 * q + 0]),
+					__builtin_bit_cast(uint32_t, r[4 * q + 1]),
+					__builtin_bit_cast(uint32_t, r[4 * q + 2]),
+					__builtin_bit_cast(uint32_t, r[4 * q + 3]));
+		}
 	} else {
 		rtranspose<0, 9>(r, s, tid);
 #pragma unroll
@@ -454,12 +484,14 @@ cudaError_t run_abitonic(T *d, size_t N, int max_ps, int max_sfs,
 	int t = std::min(default_tile_log2<T>(), logN);
 	if (max_sfs >= 1 && max_sfs < t) t = max_sfs;
 	// Steps per register round: at most 4 (16 elements per thread) in the
-	// shared-memory tiles; in the global passes 5 (32) for types of up to 4
-	// bytes when the maxps option allows the most grouping (the network,
-	// hence the result, is the same for any grouping; 5 in the tiles would
-	// leave one 512-thread CTA per SM).
+	// shared-memory tiles; in the global passes 6 (64) for 2- and 4-byte
+	// types and 5 (32) for 1-byte types (which spill at 64) when the maxps
+	// option allows the most grouping (the network, hence the result, is
+	// the same for any grouping; 5 in the tiles would leave one 512-thread
+	// CTA per SM). A global pass moves the whole array whatever its step
+	// count, so fewer, longer passes cut the bytes.
 	const int maxg = std::max(1, std::min(4, max_ps));
-	const int gmaxg = max_ps >= 4 && sizeof(T) <= 4 ? 5 : maxg;
+	const int gmaxg = max_ps >= 4 && sizeof(T) <= 4 ? (sizeof(T) == 1 ? 5 : 6) : maxg;
 	const uint32_t tile_n = 1u << t;
 	const size_t smem = (size_t)(tile_n + tile_n / 32 + 1) * sizeof(T);
 	const int threads = (int)std::min<uint32_t>(kTileThreads, std::max<uint32_t>(tile_n / 2, 32));
@@ -507,6 +539,10 @@ cudaError_t run_abitonic(T *d, size_t N, int max_ps, int max_sfs,
 			unsigned blocks = (unsigned)((groups + 255) / 256);
 			KernelTimer tm("abitonic_global_steps", s, pass_bytes);
 			switch (g) {
+			case 6:
+				if constexpr (sizeof(T) == 2 || sizeof(T) == 4)
+					abitonic_global_steps<T, 6><<<blocks, 256, 0, s>>>(d, groups, stage, j);
+				break;
 			case 5: abitonic_global_steps<T, 5><<<blocks, 256, 0, s>>>(d, groups, stage, j); break;
 			case 4: abitonic_global_steps<T, 4><<<blocks, 256, 0, s>>>(d, groups, stage, j); break;
 			case 3: abitonic_global_steps<T, 3><<<blocks, 256, 0, s>>>(d, groups, stage, j); break;

@@ -81,6 +81,7 @@ enum DevError : int {
 	DEV_OK = 0,
 	DEV_ERR_LOOKBACK_TIMEOUT = 1,  // decoupled-lookback wait hit its cap
 	DEV_ERR_BAD_SEGMENTS = 2,      // segment offsets decrease or pass the buffer
+	DEV_ERR_COPY_TIMEOUT = 3,      // a bulk copy's completion wait hit its cap
 };
 
 // Error helpers (GError semantics: *err must be NULL on entry; err may be

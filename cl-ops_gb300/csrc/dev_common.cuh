@@ -44,6 +44,18 @@ __device__ __forceinline__ void st_stream_v4(uint4 *p, uint4 v) {
 		:: "l"(p), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w) : "memory");
 }
 
+// 32-byte vector load/store (eight 32-bit words; 32-byte aligned address).
+__device__ __forceinline__ void ld_v8(const void *p, uint32_t (&w)[8]) {
+	asm volatile("ld.global.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+		: "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]),
+		  "=r"(w[6]), "=r"(w[7]) : "l"(p));
+}
+__device__ __forceinline__ void st_v8(void *p, const uint32_t (&w)[8]) {
+	asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};"
+		:: "l"(p), "r"(w[0]), "r"(w[1]), "r"(w[2]), "r"(w[3]), "r"(w[4]), "r"(w[5]),
+		   "r"(w[6]), "r"(w[7]) : "memory");
+}
+
 // Spin budget of every bounded wait: with the nanosleep back-off below and
 // the re-read of the flag each round this is about a second of waiting
 // before a wait gives up.
@@ -57,6 +69,47 @@ __device__ __forceinline__ void backoff(uint32_t iter) {
 __device__ __forceinline__ void report_timeout(int *status, int code,
 	int detail) {
 	if (atomicCAS(status, 0, code) == 0) atomicExch(status + 1, detail);
+}
+
+// ---------------------------------------------------------------- bulk copies
+// One-dimensional bulk copies global -> shared (the copy engine, not the
+// load/store pipe), completing on a CTA-local mbarrier. Addresses 16-byte
+// aligned, sizes multiples of 16 bytes. No multicast.
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+	return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(bar)), "r"(count)
+		: "memory");
+	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+		:: "r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
+	uint64_t *bar) {
+	asm volatile(
+		"cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+		:: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+	uint32_t ok;
+	asm volatile(
+		"{\n\t.reg .pred p;\n\t"
+		"mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+		"selp.u32 %0, 1, 0, p;\n\t}"
+		: "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+	return ok != 0;
+}
+// Waits for phase `parity` of the barrier with a bounded number of tries;
+// false when it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+	for (uint32_t iter = 0; iter < kSpinLimit; ++iter) {
+		if (mbar_try_wait(bar, parity)) return true;
+		backoff(iter);
+	}
+	return false;
 }
 
 // old = atomicAdd(p, v) on shared memory for the lanes where `pred` holds,

@@ -13,7 +13,8 @@
 //      per tile (14336 32-bit keys; 5120 pairs of a 64-bit key and a
 //      32-bit value), tiles claimed in order from a counter:
 //      a. keys are loaded in half-warp units (a unit's keys are in index
-//         order), the tile's digit counts are published for the decoupled
+//         order; full tiles of 32-bit keys arrive by bulk copy into shared
+//         memory), the tile's digit counts are published for the decoupled
 //         lookback before the tile is ranked;
 //      b. keys are ranked among equal digits of their unit, stably (lanes
 //         in order, rounds in order): peers found through a shared-memory
@@ -169,6 +170,11 @@ static_assert(kPassThreads >= 256 && kPassThreads <= 1024 && kPassThreads % 32 =
 #ifndef CLO_RADIX_PASS_KPT1
 #define CLO_RADIX_PASS_KPT1 0
 #endif
+// Resident CTAs per SM the pass is compiled for (registers a thread:
+// 65536 / (CTAs x threads)).
+#ifndef CLO_RADIX_PASS_MINB
+#define CLO_RADIX_PASS_MINB 2
+#endif
 
 // Reads the statuses of tiles base, base-1, ..., base-W+1 for one digit
 // (independent loads, one round trip), adds them in order to `excl` up to
@@ -237,10 +243,33 @@ __device__ __forceinline__ int row_of(int r) { return r * kRowWords + (r & 1) * 
 // Shared memory: a ranking row per half-warp unit and a count row per two
 // units (row_of), the tile offsets and a scan array (256 words each), 64
 // misc words, the staged tile (keys, then values).
+// Keys-only passes over 32-bit keys take each full tile in with bulk
+// copies (one per half-warp unit, into the staging area, each unit's keys
+// padded to 16 banks from its warp neighbour's; the copy engine, not the
+// load/store pipe) and read their keys from shared memory: one conflict-
+// free wavefront a warp round instead of two global ones (the two units of
+// a warp are 3.5 KB apart). 0.808 -> 0.794 ms a pass at 2^28.
+#ifndef CLO_RADIX_BULK_LOAD
+#define CLO_RADIX_BULK_LOAD 1
+#endif
+template <typename K, bool HAS_V>
+constexpr bool bulk_tile_load() {
+	return CLO_RADIX_BULK_LOAD && sizeof(K) == 4 && !HAS_V;
+}
+// Landing-area words per unit: the unit's keys, plus 16 words when that
+// would otherwise put both units of a warp in the same banks.
+template <int KPT>
+constexpr int land_unit_words() {
+	return 16 * KPT + ((16 * KPT) % 32 == 0 ? 16 : 0);
+}
+
 template <typename K, typename V, bool HAS_V, int THREADS, int KPT>
 constexpr size_t tiles_smem() {
+	const size_t stage = (size_t)THREADS * KPT * (sizeof(K) + (HAS_V ? sizeof(V) : 0));
+	const size_t land = bulk_tile_load<K, HAS_V>()
+		? (size_t)(THREADS / 16) * land_unit_words<KPT>() * sizeof(K) : 0;
 	return ((size_t)(THREADS / 16 + THREADS / 32) * kRowWords + 2 * kRadix + 64) *
-		sizeof(uint32_t) + (size_t)THREADS * KPT * (sizeof(K) + (HAS_V ? sizeof(V) : 0));
+		sizeof(uint32_t) + (stage > land ? stage : land);
 }
 
 template <typename K, typename V, bool HAS_V, int THREADS, int KPT, int MINB>
@@ -274,7 +303,23 @@ radix_pass_tiles(const K *__restrict__ kin, K *__restrict__ kout,
 	const int pd = tid & (kRadix - 1);
 	const int dw = pd >> 5;
 
-	if (tid == 0) s_misc[0] = atomicAdd(a.tile_counter, 1u);
+	constexpr bool BULK = bulk_tile_load<K, HAS_V>();
+	constexpr int LW = land_unit_words<KPT>();
+	uint64_t *bar = reinterpret_cast<uint64_t *>(s_misc + 32);
+	const bool bulk_ok = BULK && ((uintptr_t)kin % 16) == 0;
+	if (tid == 0) {
+		const uint32_t tt = atomicAdd(a.tile_counter, 1u);
+		s_misc[0] = tt;
+		if (bulk_ok && tt < num_tiles && (size_t)(tt + 1) * TILE <= a.n) {
+			dev::mbar_init(bar, 1);
+			dev::mbar_expect_tx(bar, (uint32_t)(TILE * sizeof(K)));
+			const K *src = kin + (size_t)tt * TILE;
+			K *land = reinterpret_cast<K *>(s_stage);
+#pragma unroll 1
+			for (int u = 0; u < UNITS; ++u)
+				dev::bulk_g2s(land + u * LW, src + u * UKEYS, (uint32_t)(UKEYS * sizeof(K)), bar);
+		}
+	}
 	uint32_t hv = 0, hinc = 0;
 	if (owner) {
 #pragma unroll
@@ -301,11 +346,21 @@ radix_pass_tiles(const K *__restrict__ kin, K *__restrict__ kout,
 	K k[KPT];
 	V v[HAS_V ? KPT : 1];
 	const size_t ubase = (size_t)t * TILE + (size_t)unit * UKEYS;
+	if (bulk_ok && (size_t)(t + 1) * TILE <= a.n) {
+		if (!dev::mbar_wait_bounded(bar, 0)) {
+			if (tid == 0) dev::report_timeout(a.dev_status, DEV_ERR_COPY_TIMEOUT, (int)t);
+			dev::mbar_wait_bounded(bar, 0);  // the copies still in flight
+		}
+		const K *land = reinterpret_cast<const K *>(s_stage) + unit * LW;
 #pragma unroll
-	for (int j = 0; j < KPT; ++j) {
-		const size_t idx = ubase + (size_t)j * 16 + l16;
-		k[j] = idx < a.n ? kin[idx] : (K)~(K)0;
-		if constexpr (HAS_V) v[j] = idx < a.n ? vin[idx] : (V)0;
+		for (int j = 0; j < KPT; ++j) k[j] = land[j * 16 + l16];
+	} else {
+#pragma unroll
+		for (int j = 0; j < KPT; ++j) {
+			const size_t idx = ubase + (size_t)j * 16 + l16;
+			k[j] = idx < a.n ? kin[idx] : (K)~(K)0;
+			if constexpr (HAS_V) v[j] = idx < a.n ? vin[idx] : (V)0;
+		}
 	}
 #pragma unroll
 	for (int j = 0; j < KPT; ++j) atomicAdd(my_cnt + digit_of(k[j], shift), cnt_inc);
@@ -411,7 +466,7 @@ struct TilesCfg {
 	static constexpr int kKpt256 = kWords == 1 ? 56 : kWords == 2 ? 32 : kWords == 3 ? 20 : 16;
 	static constexpr int kKpt = (kWords == 1 && CLO_RADIX_PASS_KPT1 > 0) ? CLO_RADIX_PASS_KPT1
 		: kKpt256 * 256 / kThreads;
-	static constexpr int kMinBlocks = 2;
+	static constexpr int kMinBlocks = CLO_RADIX_PASS_MINB;
 	static constexpr int kTile = kThreads * kKpt;
 };
 
