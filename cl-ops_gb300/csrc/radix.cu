@@ -243,31 +243,40 @@ __device__ __forceinline__ int row_of(int r) { return r * kRowWords + (r & 1) * 
 // Shared memory: a ranking row per half-warp unit and a count row per two
 // units (row_of), the tile offsets and a scan array (256 words each), 64
 // misc words, the staged tile (keys, then values).
-// Keys-only passes over 32-bit keys take each full tile in with bulk
-// copies (one per half-warp unit, into the staging area, each unit's keys
-// padded to 16 banks from its warp neighbour's; the copy engine, not the
-// load/store pipe) and read their keys from shared memory: one conflict-
-// free wavefront a warp round instead of two global ones (the two units of
-// a warp are 3.5 KB apart). 0.808 -> 0.794 ms a pass at 2^28.
+// Full tiles of 32- or 64-bit keys (with 32-bit values, if any) are taken
+// in with bulk copies (per half-warp unit one of its keys and one of its
+// values, into the staging area; the copy engine, not the load/store
+// pipe) and read from shared memory: a warp round of 32-bit elements is
+// one conflict-free wavefront instead of two global ones (the two units
+// of a warp are KPT x 64 bytes apart). 32-bit keys: 0.808 -> 0.790 ms a
+// pass at 2^28.
 #ifndef CLO_RADIX_BULK_LOAD
 #define CLO_RADIX_BULK_LOAD 1
 #endif
-template <typename K, bool HAS_V>
+template <typename K, typename V, bool HAS_V>
 constexpr bool bulk_tile_load() {
-	return CLO_RADIX_BULK_LOAD && sizeof(K) == 4 && !HAS_V;
+	return CLO_RADIX_BULK_LOAD && (sizeof(K) == 4 || sizeof(K) == 8) &&
+		(!HAS_V || sizeof(V) == 4);
 }
-// Landing-area words per unit: the unit's keys, plus 16 words when that
-// would otherwise put both units of a warp in the same banks.
-template <int KPT>
-constexpr int land_unit_words() {
-	return 16 * KPT + ((16 * KPT) % 32 == 0 ? 16 : 0);
+// Landing-area elements per unit: the unit's elements, plus 16 where 4-byte
+// elements of both units of a warp would otherwise fall in the same banks.
+template <int KPT, int BYTES>
+constexpr int land_unit_elems() {
+	return 16 * KPT + (BYTES == 4 && (16 * KPT) % 32 == 0 ? 16 : 0);
+}
+// Landing-area bytes of the keys (the values follow them).
+template <typename K, int THREADS, int KPT>
+constexpr size_t land_key_bytes() {
+	return (size_t)(THREADS / 16) * land_unit_elems<KPT, (int)sizeof(K)>() * sizeof(K);
 }
 
 template <typename K, typename V, bool HAS_V, int THREADS, int KPT>
 constexpr size_t tiles_smem() {
 	const size_t stage = (size_t)THREADS * KPT * (sizeof(K) + (HAS_V ? sizeof(V) : 0));
-	const size_t land = bulk_tile_load<K, HAS_V>()
-		? (size_t)(THREADS / 16) * land_unit_words<KPT>() * sizeof(K) : 0;
+	const size_t land = bulk_tile_load<K, V, HAS_V>()
+		? land_key_bytes<K, THREADS, KPT>() + (HAS_V
+			? (size_t)(THREADS / 16) * land_unit_elems<KPT, (int)sizeof(V)>() * sizeof(V) : 0)
+		: 0;
 	return ((size_t)(THREADS / 16 + THREADS / 32) * kRowWords + 2 * kRadix + 64) *
 		sizeof(uint32_t) + (stage > land ? stage : land);
 }
@@ -303,21 +312,29 @@ radix_pass_tiles(const K *__restrict__ kin, K *__restrict__ kout,
 	const int pd = tid & (kRadix - 1);
 	const int dw = pd >> 5;
 
-	constexpr bool BULK = bulk_tile_load<K, HAS_V>();
-	constexpr int LW = land_unit_words<KPT>();
+	constexpr bool BULK = bulk_tile_load<K, V, HAS_V>();
+	constexpr int LK = land_unit_elems<KPT, (int)sizeof(K)>();
+	constexpr int LV = land_unit_elems<KPT, (int)sizeof(V)>();
 	uint64_t *bar = reinterpret_cast<uint64_t *>(s_misc + 32);
-	const bool bulk_ok = BULK && ((uintptr_t)kin % 16) == 0;
+	const bool bulk_ok = BULK && ((uintptr_t)kin % 16) == 0 &&
+		(!HAS_V || ((uintptr_t)vin % 16) == 0);
+	K *land_k = reinterpret_cast<K *>(s_stage);
+	V *land_v = reinterpret_cast<V *>(s_stage + land_key_bytes<K, THREADS, KPT>());
 	if (tid == 0) {
 		const uint32_t tt = atomicAdd(a.tile_counter, 1u);
 		s_misc[0] = tt;
 		if (bulk_ok && tt < num_tiles && (size_t)(tt + 1) * TILE <= a.n) {
 			dev::mbar_init(bar, 1);
-			dev::mbar_expect_tx(bar, (uint32_t)(TILE * sizeof(K)));
-			const K *src = kin + (size_t)tt * TILE;
-			K *land = reinterpret_cast<K *>(s_stage);
+			dev::mbar_expect_tx(bar, (uint32_t)(TILE * (sizeof(K) + (HAS_V ? sizeof(V) : 0))));
+			const size_t t0 = (size_t)tt * TILE;
 #pragma unroll 1
-			for (int u = 0; u < UNITS; ++u)
-				dev::bulk_g2s(land + u * LW, src + u * UKEYS, (uint32_t)(UKEYS * sizeof(K)), bar);
+			for (int u = 0; u < UNITS; ++u) {
+				dev::bulk_g2s(land_k + u * LK, kin + t0 + u * UKEYS,
+					(uint32_t)(UKEYS * sizeof(K)), bar);
+				if constexpr (HAS_V)
+					dev::bulk_g2s(land_v + u * LV, vin + t0 + u * UKEYS,
+						(uint32_t)(UKEYS * sizeof(V)), bar);
+			}
 		}
 	}
 	uint32_t hv = 0, hinc = 0;
@@ -351,9 +368,11 @@ radix_pass_tiles(const K *__restrict__ kin, K *__restrict__ kout,
 			if (tid == 0) dev::report_timeout(a.dev_status, DEV_ERR_COPY_TIMEOUT, (int)t);
 			dev::mbar_wait_bounded(bar, 0);  // the copies still in flight
 		}
-		const K *land = reinterpret_cast<const K *>(s_stage) + unit * LW;
 #pragma unroll
-		for (int j = 0; j < KPT; ++j) k[j] = land[j * 16 + l16];
+		for (int j = 0; j < KPT; ++j) {
+			k[j] = land_k[unit * LK + j * 16 + l16];
+			if constexpr (HAS_V) v[j] = land_v[unit * LV + j * 16 + l16];
+		}
 	} else {
 #pragma unroll
 		for (int j = 0; j < KPT; ++j) {
