@@ -475,14 +475,24 @@ radix_pass_tiles(const K *__restrict__ kin, K *__restrict__ kout,
 
 // Tile shape of the pass by the 32-bit register words a key (and value)
 // takes: keys per thread and resident CTAs per SM, each the measured best
-// at 2^27 - 2^28 elements (larger tiles mean fewer lookbacks; the limit is
-// 128 registers a thread without spills). 32-bit keys: 14336-key tiles;
-// 64-bit keys with 32-bit values: 5120 pairs.
+// at 2^27 - 2^28 elements (larger tiles spread the per-tile work -- row
+// clears and scans, the lookback -- over more keys; the limits are 128
+// registers a thread without spills and two CTAs' shared memory per SM).
+// 32-bit keys: 14336-key tiles; 64-bit keys or 32-bit pairs: 10240;
+// 64-bit keys with 32-bit values (bulk-loaded): 7168 pairs, 5120 for the
+// 12-byte pairs loaded lane by lane.
 template <typename K, typename V, bool HAS_V>
 struct TilesCfg {
 	static constexpr int kWords = (int)((sizeof(K) + 3) / 4) + (HAS_V ? (int)((sizeof(V) + 3) / 4) : 0);
 	static constexpr int kThreads = kPassThreads;
-	static constexpr int kKpt256 = kWords == 1 ? 56 : kWords == 2 ? 32 : kWords == 3 ? 20 : 16;
+#ifndef CLO_RADIX_PASS_KPT2
+#define CLO_RADIX_PASS_KPT2 40
+#endif
+#ifndef CLO_RADIX_PASS_KPT3
+#define CLO_RADIX_PASS_KPT3 28
+#endif
+	static constexpr int kKpt256 = kWords == 1 ? 56 : kWords == 2 ? CLO_RADIX_PASS_KPT2
+		: kWords == 3 ? (bulk_tile_load<K, V, HAS_V>() ? CLO_RADIX_PASS_KPT3 : 20) : 16;
 	static constexpr int kKpt = (kWords == 1 && CLO_RADIX_PASS_KPT1 > 0) ? CLO_RADIX_PASS_KPT1
 		: kKpt256 * 256 / kThreads;
 	static constexpr int kMinBlocks = CLO_RADIX_PASS_MINB;

@@ -28,7 +28,8 @@ def _sort_dev(clops, ctx, q, algo, code, a, options=None, key_type=None):
 # ------------------------------------------------------------- satradix
 @pytest.mark.parametrize("code,dt", INT)
 @pytest.mark.parametrize("n", [0, 1, 2, 3, 31, 33, 1000, 4095, 4096, 4097, 8191, 8192,
-                               8193, 14335, 14336, 14337, 28673, 65537, 300001])
+                               8193, 10240, 10241, 14335, 14336, 14337, 20481, 28673,
+                               65537, 300001])
 def test_satradix_matches_oracle(clops, ctx, queue, code, dt, n):
     a = keys_of_type(100 + n + code, n, dt)
     got = _sort_dev(clops, ctx, queue, "satradix", code, a)
@@ -70,7 +71,8 @@ def test_satradix_u64_low20(clops, ctx, queue):
 @pytest.mark.parametrize("kcode,kdt,vcode,vdt", [
     (5, np.uint32, 5, np.uint32), (7, np.uint64, 5, np.uint32),
     (5, np.uint32, 7, np.uint64), (7, np.uint64, 7, np.uint64), (4, np.int32, 9, np.float32)])
-@pytest.mark.parametrize("n", [1, 1000, 4097, 5119, 5121, 8193, 10241, 250007])
+@pytest.mark.parametrize("n", [1, 1000, 4097, 5119, 5121, 7167, 7168, 7169, 8193, 10239,
+                               10240, 10241, 14337, 20481, 250007])
 def test_satradix_kv_stable(clops, ctx, queue, kcode, kdt, vcode, vdt, n):
     k = keys_of_type(31 + n, n, kdt)
     k = (k.view(f"u{k.dtype.itemsize}") & np.array(0x0303, dtype=f"u{k.dtype.itemsize}")).view(kdt)
