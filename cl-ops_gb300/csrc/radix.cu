@@ -10,7 +10,7 @@
 //   1. radix_upsweep_w: one read of the keys builds the 256-bin histogram
 //      of every digit position at once.
 //   2. per digit position, radix_pass_tiles (one launch per pass), one CTA
-//      per tile (14336 32-bit keys; 5120 pairs of a 64-bit key and a
+//      per tile (15360 32-bit keys; 7168 pairs of a 64-bit key and a
 //      32-bit value), tiles claimed in order from a counter:
 //      a. keys are loaded in half-warp units (a unit's keys are in index
 //         order; full tiles of 32-bit keys arrive by bulk copy into shared
@@ -478,7 +478,7 @@ radix_pass_tiles(const K *__restrict__ kin, K *__restrict__ kout,
 // at 2^27 - 2^28 elements (larger tiles spread the per-tile work -- row
 // clears and scans, the lookback -- over more keys; the limits are 128
 // registers a thread without spills and two CTAs' shared memory per SM).
-// 32-bit keys: 14336-key tiles; 64-bit keys or 32-bit pairs: 10240;
+// 32-bit keys: 15360-key tiles; 64-bit keys or 32-bit pairs: 10240;
 // 64-bit keys with 32-bit values (bulk-loaded): 7168 pairs, 5120 for the
 // 12-byte pairs loaded lane by lane.
 template <typename K, typename V, bool HAS_V>
@@ -491,7 +491,7 @@ struct TilesCfg {
 #ifndef CLO_RADIX_PASS_KPT3
 #define CLO_RADIX_PASS_KPT3 28
 #endif
-	static constexpr int kKpt256 = kWords == 1 ? 56 : kWords == 2 ? CLO_RADIX_PASS_KPT2
+	static constexpr int kKpt256 = kWords == 1 ? 60 : kWords == 2 ? CLO_RADIX_PASS_KPT2
 		: kWords == 3 ? (bulk_tile_load<K, V, HAS_V>() ? CLO_RADIX_PASS_KPT3 : 20) : 16;
 	static constexpr int kKpt = (kWords == 1 && CLO_RADIX_PASS_KPT1 > 0) ? CLO_RADIX_PASS_KPT1
 		: kKpt256 * 256 / kThreads;

@@ -28,7 +28,8 @@ def _sort_dev(clops, ctx, q, algo, code, a, options=None, key_type=None):
 # ------------------------------------------------------------- satradix
 @pytest.mark.parametrize("code,dt", INT)
 @pytest.mark.parametrize("n", [0, 1, 2, 3, 31, 33, 1000, 4095, 4096, 4097, 8191, 8192,
-                               8193, 10240, 10241, 14335, 14336, 14337, 20481, 28673,
+                               8193, 10240, 10241, 14335, 14336, 14337, 15359, 15360, 15361,
+                               20481, 28673, 30721,
                                65537, 300001])
 def test_satradix_matches_oracle(clops, ctx, queue, code, dt, n):
     a = keys_of_type(100 + n + code, n, dt)
