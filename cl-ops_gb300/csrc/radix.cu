@@ -499,6 +499,18 @@ struct TilesCfg {
 	static constexpr int kTile = kThreads * kKpt;
 };
 
+// The shape for sorts too small to give every SM a tile of TilesCfg size
+// (2^20 32-bit keys make 69 of those for 152 SMs): a quarter of the keys
+// per thread, so the tiles spread over the whole GPU.
+template <typename K, typename V, bool HAS_V>
+struct TilesCfgSmall {
+	using Big = TilesCfg<K, V, HAS_V>;
+	static constexpr int kThreads = Big::kThreads;
+	static constexpr int kKpt = Big::kKpt / 4 < 4 ? 4 : Big::kKpt / 4;
+	static constexpr int kMinBlocks = Big::kMinBlocks;
+	static constexpr int kTile = kThreads * kKpt;
+};
+
 template <typename K, int PASSES>
 void launch_upsweep_p(cudaStream_t s, const K *keys, size_t n, uint32_t *hist,
 	int base_shift, int sm_count) {
@@ -535,18 +547,10 @@ void launch_upsweep(int passes, cudaStream_t s, const K *keys, size_t n, uint32_
 	}
 }
 
-template <typename K, typename V, bool HAS_V>
-cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
+template <typename K, typename V, bool HAS_V, typename TC>
+cudaError_t sort_tiles(void *keys, void *vals, size_t n, int passes,
 	CCLContext *ctx, cudaStream_t s, bool allow_skip, GError **err) {
-	const int passes = sort_bits / kRadixBits;
-	if (n < 2 || passes == 0) return cudaSuccess;
-	if (n >= (size_t)kStValue) {
-		set_error(err, CLO_ERROR_ARGS,
-			"satradix: %zu elements exceed the single-sort limit of 2^30 - 1", n);
-		return cudaErrorInvalidValue;
-	}
-	// One CTA per tile of TilesCfg size.
-	using TC = TilesCfg<K, V, HAS_V>;
+	// One CTA per tile of TC's size.
 	const size_t ctiles = (n + TC::kTile - 1) / TC::kTile;
 	const size_t smem = tiles_smem<K, V, HAS_V, TC::kThreads, TC::kKpt>();
 	auto kern = radix_pass_tiles<K, V, HAS_V, TC::kThreads, TC::kKpt, TC::kMinBlocks>;
@@ -632,6 +636,23 @@ cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
 	tmp_free(tmp, s);
 	if (e != cudaSuccess) cuda_ok(e, err, "satradix");
 	return e;
+}
+
+template <typename K, typename V, bool HAS_V>
+cudaError_t sort_typed(void *keys, void *vals, size_t n, int sort_bits,
+	CCLContext *ctx, cudaStream_t s, bool allow_skip, GError **err) {
+	const int passes = sort_bits / kRadixBits;
+	if (n < 2 || passes == 0) return cudaSuccess;
+	if (n >= (size_t)kStValue) {
+		set_error(err, CLO_ERROR_ARGS,
+			"satradix: %zu elements exceed the single-sort limit of 2^30 - 1", n);
+		return cudaErrorInvalidValue;
+	}
+	using Big = TilesCfg<K, V, HAS_V>;
+	if ((n + Big::kTile - 1) / Big::kTile < (size_t)ctx->sm_count)
+		return sort_tiles<K, V, HAS_V, TilesCfgSmall<K, V, HAS_V>>(keys, vals, n, passes, ctx,
+			s, allow_skip, err);
+	return sort_tiles<K, V, HAS_V, Big>(keys, vals, n, passes, ctx, s, allow_skip, err);
 }
 
 // Stable partition of n keys by the top 8 of their sort_bits low bits:

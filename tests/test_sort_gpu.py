@@ -27,7 +27,8 @@ def _sort_dev(clops, ctx, q, algo, code, a, options=None, key_type=None):
 
 # ------------------------------------------------------------- satradix
 @pytest.mark.parametrize("code,dt", INT)
-@pytest.mark.parametrize("n", [0, 1, 2, 3, 31, 33, 1000, 4095, 4096, 4097, 8191, 8192,
+@pytest.mark.parametrize("n", [0, 1, 2, 3, 31, 33, 1000, 1023, 1024, 1025, 2559, 2560, 2561,
+                               3839, 3840, 3841, 4095, 4096, 4097, 7681, 8191, 8192,
                                8193, 10240, 10241, 14335, 14336, 14337, 15359, 15360, 15361,
                                20481, 28673, 30721,
                                65537, 300001])
@@ -35,6 +36,38 @@ def test_satradix_matches_oracle(clops, ctx, queue, code, dt, n):
     a = keys_of_type(100 + n + code, n, dt)
     got = _sort_dev(clops, ctx, queue, "satradix", code, a)
     np.testing.assert_array_equal(got, oracle.radix_sort(a))
+
+
+# Sorts with at least one large tile per SM take the large tile shape
+# (15360 32-bit keys; 10240 64-bit keys; 7168 and 10240 pairs); the sizes
+# below put the last tile on each side of a tile boundary.
+@pytest.mark.parametrize("code,dt,tile", [(5, np.uint32, 15360), (7, np.uint64, 10240)])
+@pytest.mark.parametrize("extra", [-1, 0, 1])
+def test_satradix_large_tile_shape_edges(clops, ctx, queue, code, dt, tile, extra):
+    n = 160 * tile + extra
+    a = keys_of_type(7 + extra + code, n, dt)
+    np.testing.assert_array_equal(_sort_dev(clops, ctx, queue, "satradix", code, a),
+                                  oracle.radix_sort(a))
+
+
+@pytest.mark.parametrize("kcode,kdt,vcode,vdt,tile", [
+    (7, np.uint64, 5, np.uint32, 7168), (5, np.uint32, 5, np.uint32, 10240)])
+@pytest.mark.parametrize("extra", [-1, 1])
+def test_satradix_kv_large_tile_shape_edges(clops, ctx, queue, kcode, kdt, vcode, vdt, tile,
+                                            extra):
+    n = 160 * tile + extra
+    k = keys_of_type(11 + extra, n, kdt)
+    v = np.arange(n, dtype=np.uint64).astype(vdt)
+    s = clops.Sorter(ctx, "satradix", kcode)
+    kb = clops.Buffer.from_array(ctx, queue, k)
+    vb = clops.Buffer.from_array(ctx, queue, v)
+    clops.wait(s.sort_kv_device(queue, kb, vb, vcode, n))
+    rk, rv = oracle.radix_sort(k, v)
+    np.testing.assert_array_equal(kb.read(queue, kdt, n), rk)
+    np.testing.assert_array_equal(vb.read(queue, vdt, n), rv)
+    for b in (kb, vb):
+        b.destroy()
+    s.destroy()
 
 
 @pytest.mark.parametrize("code,dt", [(5, np.uint32), (7, np.uint64), (4, np.int32)])
@@ -72,8 +105,9 @@ def test_satradix_u64_low20(clops, ctx, queue):
 @pytest.mark.parametrize("kcode,kdt,vcode,vdt", [
     (5, np.uint32, 5, np.uint32), (7, np.uint64, 5, np.uint32),
     (5, np.uint32, 7, np.uint64), (7, np.uint64, 7, np.uint64), (4, np.int32, 9, np.float32)])
-@pytest.mark.parametrize("n", [1, 1000, 4097, 5119, 5121, 7167, 7168, 7169, 8193, 10239,
-                               10240, 10241, 14337, 20481, 250007])
+@pytest.mark.parametrize("n", [1, 1000, 1023, 1025, 1791, 1792, 1793, 2559, 2561, 4097, 5119,
+                               5121, 7167, 7168, 7169, 8193, 10239, 10240, 10241, 14337,
+                               20481, 250007])
 def test_satradix_kv_stable(clops, ctx, queue, kcode, kdt, vcode, vdt, n):
     k = keys_of_type(31 + n, n, kdt)
     k = (k.view(f"u{k.dtype.itemsize}") & np.array(0x0303, dtype=f"u{k.dtype.itemsize}")).view(kdt)
