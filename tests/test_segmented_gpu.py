@@ -56,6 +56,24 @@ def test_seg_sort_edge_lengths(clops, ctx, queue, variant, code, dt):
     np.testing.assert_array_equal(got[int(off[-1]):], a[int(off[-1]):])
 
 
+# Segments of whole long-pass tiles starting at every 16-byte phase of the
+# buffer, the last one ending at the buffer's end (no element after it).
+@pytest.mark.parametrize("variant,code,dt,tile", [
+    (0, 5, np.uint32, 14336), (SHAPES[2], 5, np.uint32, 12288),
+    (0, 7, np.uint64, 8192), (SHAPES[3], 7, np.uint64, 6144)])
+def test_seg_sort_whole_tiles_at_every_phase_to_the_buffer_end(clops, ctx, queue, variant, code,
+                                                                dt, tile):
+    # Starts at elements 1, 2 + 2 tiles, 3 + 4 tiles, 4 + 7 tiles (16-byte
+    # phases 1, 2, 3, 0 of 32-bit keys; odd, even, odd, even of 64-bit).
+    lens = [2 * tile, 1, 2 * tile, 1, 3 * tile, 1, tile, 2 * tile]
+    off = offsets_of(lens, start=1)
+    n = int(off[-1])
+    a = keys_of_type(77 + code, n, dt)
+    got = _seg_sort(clops, ctx, queue, code, a, off, options=f"segvariant={variant}")
+    np.testing.assert_array_equal(got, oracle.seg_sort(a, off))
+    np.testing.assert_array_equal(got[:1], a[:1])
+
+
 @pytest.mark.parametrize("variant", range(36))
 def test_seg_sort_lognormal_u32(clops, ctx, queue, variant):
     lens = lognormal_lengths(3000, 6.0, 2.0, 1, 1 << 18, seed=48)
