@@ -85,8 +85,13 @@ sbitonic_step(T *data, size_t half_n, int stage, int step) {
 
 // ------------------------------------------------- abitonic global steps
 // Steps step .. step-G+1 of `stage`, 2^G elements per thread.
+// Threads per CTA of the global passes: 128 for 7 steps (128 elements and
+// 168 registers a thread, three CTAs per SM), else 256.
+template <int G>
+constexpr int gs_threads() { return G >= 7 ? 128 : 256; }
+
 template <typename T, int G>
-__global__ void __launch_bounds__(256, G >= 6 ? 2 : 1)
+__global__ void __launch_bounds__(gs_threads<G>(), G >= 7 ? 3 : G >= 6 ? 2 : 1)
 abitonic_global_steps(T *data, size_t groups, int stage, int step) {
 	size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
 	if (q >= groups) return;
@@ -106,8 +111,8 @@ abitonic_global_steps(T *data, size_t groups, int stage, int step) {
 		for (int m = 0; m < (1 << G); ++m)
 			if (!(m & (1 << s))) cmpxchg(r[m], r[m | (1 << s)], desc);
 	}
-	// With 64 elements a thread, the store addresses are computed afresh
-	// rather than kept from the loads (64 more live registers).
+	// With 64 or more elements a thread, the store addresses are computed
+	// afresh rather than kept from the loads (as many more live registers).
 	if constexpr (G >= 6) asm volatile("" : "+l"(p));
 #pragma unroll
 	for (int m = 0; m < (1 << G); ++m) p[m * inc] = r[m];
@@ -484,14 +489,15 @@ cudaError_t run_abitonic(T *d, size_t N, int max_ps, int max_sfs,
 	int t = std::min(default_tile_log2<T>(), logN);
 	if (max_sfs >= 1 && max_sfs < t) t = max_sfs;
 	// Steps per register round: at most 4 (16 elements per thread) in the
-	// shared-memory tiles; in the global passes 6 (64) for 2- and 4-byte
-	// types and 5 (32) for 1-byte types (which spill at 64) when the maxps
-	// option allows the most grouping (the network, hence the result, is
-	// the same for any grouping; 5 in the tiles would leave one 512-thread
-	// CTA per SM). A global pass moves the whole array whatever its step
-	// count, so fewer, longer passes cut the bytes.
+	// shared-memory tiles; in the global passes 7 (128) for 4-byte types,
+	// 6 (64) for 2-byte types and 5 (32) for 1-byte types (which spill at
+	// 64) when the maxps option allows the most grouping (the network,
+	// hence the result, is the same for any grouping; 5 in the tiles would
+	// leave one 512-thread CTA per SM). A global pass moves the whole array
+	// whatever its step count, so fewer, longer passes cut the bytes.
 	const int maxg = std::max(1, std::min(4, max_ps));
-	const int gmaxg = max_ps >= 4 && sizeof(T) <= 4 ? (sizeof(T) == 1 ? 5 : 6) : maxg;
+	const int gmaxg = max_ps >= 4 && sizeof(T) <= 4
+		? (sizeof(T) == 4 ? 7 : sizeof(T) == 2 ? 6 : 5) : maxg;
 	const uint32_t tile_n = 1u << t;
 	const size_t smem = (size_t)(tile_n + tile_n / 32 + 1) * sizeof(T);
 	const int threads = (int)std::min<uint32_t>(kTileThreads, std::max<uint32_t>(tile_n / 2, 32));
@@ -537,8 +543,13 @@ cudaError_t run_abitonic(T *d, size_t N, int max_ps, int max_sfs,
 			int g = (rem + npass - 1) / npass;
 			size_t groups = N >> g;
 			unsigned blocks = (unsigned)((groups + 255) / 256);
+			const unsigned blocks7 = (unsigned)((groups + 127) / 128);
 			KernelTimer tm("abitonic_global_steps", s, pass_bytes);
 			switch (g) {
+			case 7:
+				if constexpr (sizeof(T) == 4)
+					abitonic_global_steps<T, 7><<<blocks7, gs_threads<7>(), 0, s>>>(d, groups, stage, j);
+				break;
 			case 6:
 				if constexpr (sizeof(T) == 2 || sizeof(T) == 4)
 					abitonic_global_steps<T, 6><<<blocks, 256, 0, s>>>(d, groups, stage, j);

@@ -61,36 +61,40 @@ __device__ __forceinline__ uint32_t digit_of(K k, int shift) {
 // 16-byte loads in flight.
 constexpr int kUpsweepInFlight = 8;
 
-// 1024-thread CTAs. Up to four digit positions count into full 32-bit
+// 1024-thread CTAs. The first four digit positions count into full 32-bit
 // words (digit d of lane l at word d * 32 + l per position: one byte
 // extract, one address computation and one shared add per key and
-// position, and no overflow bound); five to eight positions (64-bit keys)
-// into 16-bit halves of word (d >> 1) * 32 + l, 16 KB per position, with
-// the grid keeping a thread at kUpwHalfKeysPerThread keys so that a half,
-// which all 32 warps of a CTA add to, stays below 2^16.
+// position, and no overflow bound, 32 KB a position); positions five to
+// eight (64-bit keys) into 16-bit halves of word (d >> 1) * 32 + l, 16 KB
+// per position, with the grid keeping a thread at kUpwHalfKeysPerThread
+// keys so that a half, which all 32 warps of a CTA add to, stays below
+// 2^16 (eight positions: 192 KB, one CTA per SM).
 constexpr int kUpwThreads = 1024;
 constexpr size_t kUpwHalfKeysPerThread = 2000;
 
 template <int PASSES>
 constexpr size_t upw_smem() {
-	return (size_t)PASSES * (PASSES <= 4 ? kRadix : kRadix / 2) * 32 * 4;
+	return (size_t)(PASSES < 4 ? PASSES : 4) * kRadix * 32 * 4 +
+		(size_t)(PASSES > 4 ? PASSES - 4 : 0) * (kRadix / 2) * 32 * 4;
+}
+// Word offset of position p's columns.
+__host__ __device__ constexpr int upw_pos_base(int p) {
+	return p <= 4 ? p * kRadix * 32 : 4 * kRadix * 32 + (p - 4) * (kRadix / 2) * 32;
 }
 
 template <typename K, int PASSES>
 __global__ void __launch_bounds__(kUpwThreads, 1)
 radix_upsweep_w(const K *__restrict__ keys, size_t n, uint32_t *__restrict__ hist,
 	int base_shift) {
-	constexpr bool HALVES = PASSES > 4;
-	constexpr int kPosWords = (HALVES ? kRadix / 2 : kRadix) * 32;
 	extern __shared__ __align__(16) uint32_t up_smem[];
-	for (int i = threadIdx.x; i < PASSES * kPosWords; i += kUpwThreads) up_smem[i] = 0;
+	for (int i = threadIdx.x; i < upw_pos_base(PASSES); i += kUpwThreads) up_smem[i] = 0;
 	__syncthreads();
 	const int lane = threadIdx.x & 31;
 	uint32_t *col = up_smem + lane;
 	auto count = [&](int p, K key) {
 		const uint32_t d = digit_of(key, base_shift + p * kRadixBits);
-		if (HALVES) atomicAdd(col + p * kPosWords + (d >> 1) * 32, 1u << ((d & 1) << 4));
-		else atomicAdd(col + p * kPosWords + d * 32, 1u);
+		if (p >= 4) atomicAdd(col + upw_pos_base(p) + (d >> 1) * 32, 1u << ((d & 1) << 4));
+		else atomicAdd(col + upw_pos_base(p) + d * 32, 1u);
 	};
 	constexpr int PER = 16 / sizeof(K);  // keys per 16-byte load
 	const bool aligned = ((uintptr_t)keys % 16) == 0;
@@ -128,14 +132,15 @@ radix_upsweep_w(const K *__restrict__ keys, size_t n, uint32_t *__restrict__ his
 	__syncthreads();
 	for (int b = threadIdx.x; b < PASSES * kRadix; b += kUpwThreads) {
 		const int p = b / kRadix, d = b % kRadix;
+		const bool half = p >= 4;
 		// Digit d's 32 columns, from a rotated start (no bank conflicts).
-		const uint32_t *row = up_smem + p * kPosWords + (HALVES ? d >> 1 : d) * 32;
-		const int hs = HALVES ? (d & 1) << 4 : 0;
+		const uint32_t *row = up_smem + upw_pos_base(p) + (half ? d >> 1 : d) * 32;
+		const int hs = half ? (d & 1) << 4 : 0;
 		uint32_t v = 0;
 #pragma unroll 8
 		for (int c = 0; c < 32; ++c) {
 			const uint32_t w = row[(c + lane) & 31];
-			v += HALVES ? (w >> hs) & 0xFFFFu : w;
+			v += half ? (w >> hs) & 0xFFFFu : w;
 		}
 		if (v) atomicAdd(hist + b, v);
 	}
@@ -253,10 +258,13 @@ __device__ __forceinline__ int row_of(int r) { return r * kRowWords + (r & 1) * 
 #ifndef CLO_RADIX_BULK_LOAD
 #define CLO_RADIX_BULK_LOAD 1
 #endif
+#ifndef CLO_RADIX_BULK_V8
+#define CLO_RADIX_BULK_V8 0
+#endif
 template <typename K, typename V, bool HAS_V>
 constexpr bool bulk_tile_load() {
 	return CLO_RADIX_BULK_LOAD && (sizeof(K) == 4 || sizeof(K) == 8) &&
-		(!HAS_V || sizeof(V) == 4);
+		(!HAS_V || sizeof(V) == 4 || (CLO_RADIX_BULK_V8 && sizeof(V) == 8));
 }
 // Landing-area elements per unit: the unit's elements, plus 16 where 4-byte
 // elements of both units of a warp would otherwise fall in the same banks.
@@ -491,8 +499,12 @@ struct TilesCfg {
 #ifndef CLO_RADIX_PASS_KPT3
 #define CLO_RADIX_PASS_KPT3 28
 #endif
+#ifndef CLO_RADIX_PASS_KPT4
+#define CLO_RADIX_PASS_KPT4 16
+#endif
 	static constexpr int kKpt256 = kWords == 1 ? 60 : kWords == 2 ? CLO_RADIX_PASS_KPT2
-		: kWords == 3 ? (bulk_tile_load<K, V, HAS_V>() ? CLO_RADIX_PASS_KPT3 : 20) : 16;
+		: kWords == 3 ? (bulk_tile_load<K, V, HAS_V>() ? CLO_RADIX_PASS_KPT3 : 20)
+		: (bulk_tile_load<K, V, HAS_V>() ? CLO_RADIX_PASS_KPT4 : 16);
 	static constexpr int kKpt = (kWords == 1 && CLO_RADIX_PASS_KPT1 > 0) ? CLO_RADIX_PASS_KPT1
 		: kKpt256 * 256 / kThreads;
 	static constexpr int kMinBlocks = CLO_RADIX_PASS_MINB;
