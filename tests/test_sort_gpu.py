@@ -51,7 +51,8 @@ def test_satradix_large_tile_shape_edges(clops, ctx, queue, code, dt, tile, extr
 
 
 @pytest.mark.parametrize("kcode,kdt,vcode,vdt,tile", [
-    (7, np.uint64, 5, np.uint32, 7168), (5, np.uint32, 5, np.uint32, 10240)])
+    (7, np.uint64, 5, np.uint32, 7168), (5, np.uint32, 5, np.uint32, 10240),
+    (5, np.uint32, 7, np.uint64, 7168), (7, np.uint64, 7, np.uint64, 5120)])
 @pytest.mark.parametrize("extra", [-1, 1])
 def test_satradix_kv_large_tile_shape_edges(clops, ctx, queue, kcode, kdt, vcode, vdt, tile,
                                             extra):
