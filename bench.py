@@ -26,6 +26,7 @@ instead (the reference itself needs an OpenCL runtime, GLib and cf4ocl2,
 none of which exist here); only rank 0 works under torchrun.
 """
 import argparse
+import gc
 import json
 import os
 import pathlib
@@ -243,11 +244,15 @@ def run_ours(args):
     ain[:] = keys
     for _ in range(2):
         sorter.sort_host(q, ain, aout)
+    gc.collect()
     dist.barrier()
     t0 = time.perf_counter()
+    e2e_marks = []
     for _ in range(e2e_steps):
         sorter.sort_host(q, ain, aout)
+        e2e_marks.append(time.perf_counter())
     e2e_s = dist.max(time.perf_counter() - t0)
+    e2e_step_ms = np.diff(np.array([t0] + e2e_marks)) * 1e3
     ok = ok and bool(np.all(aout[1:] >= aout[:-1]))
     del ain, aout
     clops.lib.clo_host_free(hin)
@@ -273,6 +278,9 @@ def run_ours(args):
         "data": "synthetic (splitmix64 seed 42, uniform over [0, 2^32))",
         "config": bench_config(n, world, ok),
         "e2e": {"value": round(world * n * e2e_steps / e2e_s / 1e9, 3), "unit": "Gkeys/s",
+                "step_ms": {"min": round(float(e2e_step_ms.min()), 3),
+                            "median": round(float(np.median(e2e_step_ms)), 3),
+                            "max": round(float(e2e_step_ms.max()), 3)},
                 "h2d_bytes_per_step": n * 4, "d2h_bytes_per_step": n * 4,
                 "api": "clo_sort_with_host_data, pinned host buffers"},
         "gpu_launches": int(launches),

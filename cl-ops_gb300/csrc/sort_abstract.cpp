@@ -26,6 +26,11 @@ struct clo_sort {
 	// Kernels built by NVRTC for custom compare/get_key macros (or a key
 	// type other than the element type); null for the compiled-in path.
 	std::shared_ptr<clo::JitSort> jit;
+	// The host-data pipeline's copy-out stream and per-group events, made
+	// on first use and kept for the sorter's lifetime (no driver object is
+	// created or destroyed per call).
+	cudaStream_t copy_stream = nullptr;
+	std::vector<cudaEvent_t> group_events;
 };
 
 namespace {
@@ -630,6 +635,14 @@ CloSort *clo_sort_new(const char *type, const char *options, CCLContext *ctx,
 
 void clo_sort_destroy(CloSort *sorter) {
 	if (!sorter) return;
+	if (sorter->copy_stream || !sorter->group_events.empty()) {
+		cudaSetDevice(sorter->ctx->ordinal);
+		if (sorter->copy_stream) {
+			cudaStreamSynchronize(sorter->copy_stream);
+			cudaStreamDestroy(sorter->copy_stream);
+		}
+		for (cudaEvent_t ev : sorter->group_events) cudaEventDestroy(ev);
+	}
 	if (sorter->impl_def.finalize) sorter->impl_def.finalize(sorter);
 	if (sorter->ctx) ccl_context_unref(sorter->ctx);
 	if (sorter->prg) {
@@ -670,15 +683,22 @@ bool satradix_host_pipelined(CloSort *s, CCLQueue *q, const void *h_in, void *h_
 	const size_t eb = clo_type_sizeof(s->elem_type);
 	const int bits = satradix_sort_bits(s);
 	const int groups = 256 / kBucketsPerGroup;
-	cudaStream_t cs = q->stream, xs = nullptr;
-	if (!cuda_ok(cudaStreamCreateWithFlags(&xs, cudaStreamNonBlocking), err, "stream"))
+	cudaStream_t cs = q->stream;
+	if (!s->copy_stream &&
+		!cuda_ok(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking), err, "stream"))
 		return false;
+	while ((int)s->group_events.size() < groups) {
+		cudaEvent_t ev = nullptr;
+		if (!cuda_ok(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), err, "event"))
+			return false;
+		s->group_events.push_back(ev);
+	}
+	cudaStream_t xs = s->copy_stream;
 	const size_t off_b = (n * eb + 255) / 256 * 256;
 	const size_t off_rel = off_b + (n * eb + 255) / 256 * 256;
 	const size_t rel_words = (size_t)groups * (kBucketsPerGroup + 1);
 	char *dev = (char *)clo::tmp_alloc(ctx, off_rel + rel_words * 8, cs, err);
 	std::vector<uint64_t> h_rel(rel_words);
-	std::vector<cudaEvent_t> evs;
 	bool ok = dev != nullptr;
 	char *da = dev, *db = dev + off_b;
 	uint64_t *d_rel = (uint64_t *)(dev + off_rel);
@@ -713,10 +733,8 @@ bool satradix_host_pipelined(CloSort *s, CCLQueue *q, const void *h_in, void *h_
 				kBucketsPerGroup, (int)eb, bits - 8, 0, ctx, cs, err, da + base * eb,
 				&in_alt) == cudaSuccess;
 		if (in_alt) gp = da + base * eb;
-		cudaEvent_t ev = nullptr;
-		ok = ok && cuda_ok(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), err, "event");
 		if (!ok) break;
-		evs.push_back(ev);
+		cudaEvent_t ev = s->group_events[g];
 		ok = cuda_ok(cudaEventRecord(ev, cs), err, "event") &&
 			cuda_ok(cudaStreamWaitEvent(xs, ev, 0), err, "wait") &&
 			cuda_ok(cudaMemcpyAsync((char *)h_out + base * eb, gp, len * eb,
@@ -725,8 +743,6 @@ bool satradix_host_pipelined(CloSort *s, CCLQueue *q, const void *h_in, void *h_
 	cudaStreamSynchronize(xs);
 	cudaStreamSynchronize(cs);
 	ok = ok && clo::check_device_status(ctx, err);
-	for (cudaEvent_t ev : evs) cudaEventDestroy(ev);
-	cudaStreamDestroy(xs);
 	clo::tmp_free(dev, cs);
 	cudaStreamSynchronize(cs);
 	return ok;
