@@ -18,6 +18,11 @@ struct clo_scan {
 	CloType elem_type;
 	CloType sum_type;
 	void *data;
+	// The host-data pipeline's copy streams and events, made on first use
+	// and kept for the scanner's lifetime (no driver object is created or
+	// destroyed per call).
+	cudaStream_t copy_in = nullptr, copy_out = nullptr;
+	std::vector<cudaEvent_t> events;
 };
 
 namespace {
@@ -139,6 +144,16 @@ CloScan *clo_scan_new(const char *type, const char *options, CCLContext *ctx,
 
 void clo_scan_destroy(CloScan *scan) {
 	if (!scan) return;
+	if (scan->copy_in || scan->copy_out || !scan->events.empty()) {
+		cudaSetDevice(scan->ctx->ordinal);
+		for (cudaStream_t st : {scan->copy_in, scan->copy_out}) {
+			if (st) {
+				cudaStreamSynchronize(st);
+				cudaStreamDestroy(st);
+			}
+		}
+		for (cudaEvent_t ev : scan->events) cudaEventDestroy(ev);
+	}
 	scan->impl_def.finalize(scan);
 	if (scan->ctx) ccl_context_unref(scan->ctx);
 	if (scan->prg) {
@@ -176,19 +191,25 @@ bool scan_host_pipelined(CloScan *sc, CCLQueue *q, const void *h_in, void *h_out
 	CCLContext *ctx = sc->ctx;
 	const size_t ib = clo_type_sizeof(sc->elem_type), ob = clo_type_sizeof(sc->sum_type);
 	const size_t nc = (n + kScanChunk - 1) / kScanChunk;
-	cudaStream_t cs = q->stream, si = nullptr, so = nullptr;
-	bool ok = cuda_ok(cudaStreamCreateWithFlags(&si, cudaStreamNonBlocking), err, "stream") &&
-		cuda_ok(cudaStreamCreateWithFlags(&so, cudaStreamNonBlocking), err, "stream");
+	cudaStream_t cs = q->stream;
+	bool ok = (sc->copy_in || cuda_ok(cudaStreamCreateWithFlags(&sc->copy_in,
+		cudaStreamNonBlocking), err, "stream")) &&
+		(sc->copy_out || cuda_ok(cudaStreamCreateWithFlags(&sc->copy_out,
+		cudaStreamNonBlocking), err, "stream"));
+	cudaStream_t si = sc->copy_in, so = sc->copy_out;
 	const size_t off_out = (n * ib + 255) / 256 * 256;
 	const size_t off_carry = off_out + (n * ob + 255) / 256 * 256;
 	char *dev = ok ? (char *)clo::tmp_alloc(ctx, off_carry + (nc + 1) * 8, cs, err) : nullptr;
 	ok = ok && dev != nullptr;
-	std::vector<cudaEvent_t> evs;
-	auto event = [&]() {
-		cudaEvent_t e = nullptr;
-		if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return e;
-		evs.push_back(e);
-		return e;
+	// The call's events, in order, from the scanner's set (grown as needed).
+	size_t next_event = 0;
+	auto event = [&]() -> cudaEvent_t {
+		if (next_event == sc->events.size()) {
+			cudaEvent_t e = nullptr;
+			if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+			sc->events.push_back(e);
+		}
+		return sc->events[next_event++];
 	};
 	cudaEvent_t ready = ok ? event() : nullptr;
 	ok = ok && ready && cuda_ok(cudaMemsetAsync(dev + off_carry, 0, (nc + 1) * 8, cs), err,
@@ -215,9 +236,6 @@ bool scan_host_pipelined(CloScan *sc, CCLQueue *q, const void *h_in, void *h_out
 	if (so) cudaStreamSynchronize(so);
 	cudaStreamSynchronize(cs);
 	ok = ok && clo::check_device_status(ctx, err);
-	for (cudaEvent_t e : evs) cudaEventDestroy(e);
-	if (si) cudaStreamDestroy(si);
-	if (so) cudaStreamDestroy(so);
 	if (dev) clo::tmp_free(dev, cs);
 	cudaStreamSynchronize(cs);
 	return ok;

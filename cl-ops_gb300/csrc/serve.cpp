@@ -113,6 +113,11 @@ struct clo_server {
 	// this event, so intervals of batches on different streams compare.
 	cudaEvent_t origin = nullptr;
 
+	// Batches' events come from and return to this pool, so that no driver
+	// object is created or destroyed per batch.
+	std::mutex ev_mu;
+	std::vector<cudaEvent_t> ev_free;
+
 	// statistics
 	CloServeStats st;
 	std::vector<double> lat_ms;
@@ -124,10 +129,33 @@ namespace {
 
 size_t elem_bytes(CloType t) { return clo_type_sizeof(t); }
 
+cudaEvent_t event_get(clo_server *srv) {
+	{
+		std::lock_guard<std::mutex> lk(srv->ev_mu);
+		if (!srv->ev_free.empty()) {
+			cudaEvent_t ev = srv->ev_free.back();
+			srv->ev_free.pop_back();
+			return ev;
+		}
+	}
+	cudaEvent_t ev = nullptr;
+	if (cudaEventCreate(&ev) != cudaSuccess) {
+		cudaGetLastError();
+		return nullptr;
+	}
+	return ev;
+}
+
+void event_put(clo_server *srv, cudaEvent_t ev) {
+	if (!ev) return;
+	std::lock_guard<std::mutex> lk(srv->ev_mu);
+	srv->ev_free.push_back(ev);
+}
+
 void launch_batch(clo_server *srv, Batch *b, Lane *lane) {
 	cudaStream_t s = lane->stream;
-	cudaEventCreate(&b->ev_start);
-	cudaEventRecord(b->ev_start, s);
+	b->ev_start = event_get(srv);
+	if (b->ev_start) cudaEventRecord(b->ev_start, s);
 	const CloServeRequest &r0 = b->items[0]->r;
 	const bool dev_data = r0.device_data != CL_FALSE;
 	const cudaMemcpyKind h2d = dev_data ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
@@ -245,8 +273,8 @@ void launch_batch(clo_server *srv, Batch *b, Lane *lane) {
 		b->failed = true;
 	}
 	if (err) clo_error_free(err);
-	cudaEventCreate(&b->ev);
-	cudaEventRecord(b->ev, s);
+	b->ev = event_get(srv);
+	if (b->ev) cudaEventRecord(b->ev, s);
 }
 
 void lane_loop(clo_server *srv, Lane *lane) {
@@ -260,19 +288,23 @@ void lane_loop(clo_server *srv, Lane *lane) {
 			b = lane->q.front();
 			lane->q.pop_front();
 		}
-		bool failed = b->failed;
-		if (cudaEventSynchronize(b->ev) != cudaSuccess) {
-			cudaGetLastError();
-			failed = true;
+		bool failed = b->failed || !b->ev;
+		if (b->ev) {
+			if (cudaEventSynchronize(b->ev) != cudaSuccess) {
+				cudaGetLastError();
+				failed = true;
+			}
+		} else {
+			cudaStreamSynchronize(lane->stream);
 		}
 		const double t = now_s();
 		float t0_ms = 0.f, t1_ms = 0.f;
-		const bool timed = b->ev_start &&
+		const bool timed = b->ev_start && b->ev &&
 			cudaEventElapsedTime(&t0_ms, srv->origin, b->ev_start) == cudaSuccess &&
 			cudaEventElapsedTime(&t1_ms, srv->origin, b->ev) == cudaSuccess;
 		if (!timed) cudaGetLastError();
-		if (b->ev_start) cudaEventDestroy(b->ev_start);
-		cudaEventDestroy(b->ev);
+		event_put(srv, b->ev_start);
+		event_put(srv, b->ev);
 		{
 			std::lock_guard<std::mutex> lk(srv->mu);
 			if (timed) srv->busy_ms.emplace_back((double)t0_ms, (double)t1_ms);
@@ -365,8 +397,8 @@ void sched_loop(clo_server *srv) {
 		Lane *lane = srv->lanes[srv->next_lane++ % srv->lanes.size()];
 		if (b->items[0]->r.op != CLO_SERVE_RNG_FILL && b->h_off == nullptr) {
 			b->failed = true;
-			cudaEventCreate(&b->ev);
-			cudaEventRecord(b->ev, lane->stream);
+			b->ev = event_get(srv);
+			if (b->ev) cudaEventRecord(b->ev, lane->stream);
 		} else {
 			launch_batch(srv, b, lane);
 		}
@@ -657,6 +689,7 @@ void clo_serve_destroy(CloServer *srv) {
 		delete l;
 	}
 	if (srv->origin) cudaEventDestroy(srv->origin);
+	for (cudaEvent_t ev : srv->ev_free) cudaEventDestroy(ev);
 	for (uint64_t *p : srv->pinned_free) cudaFreeHost(p);
 	for (auto &kv : srv->items) delete kv.second;
 	ccl_context_unref(srv->ctx);
