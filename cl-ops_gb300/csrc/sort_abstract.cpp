@@ -31,6 +31,9 @@ struct clo_sort {
 	// created or destroyed per call).
 	cudaStream_t copy_stream = nullptr;
 	std::vector<cudaEvent_t> group_events;
+	// Its page-locked scratch: the partition's 256 bucket counts, then the
+	// groups' relative offsets (device <-> host copies without staging).
+	uint64_t *host_scratch = nullptr;
 };
 
 namespace {
@@ -643,6 +646,7 @@ void clo_sort_destroy(CloSort *sorter) {
 		}
 		for (cudaEvent_t ev : sorter->group_events) cudaEventDestroy(ev);
 	}
+	if (sorter->host_scratch) cudaFreeHost(sorter->host_scratch);
 	if (sorter->impl_def.finalize) sorter->impl_def.finalize(sorter);
 	if (sorter->ctx) ccl_context_unref(sorter->ctx);
 	if (sorter->prg) {
@@ -694,15 +698,19 @@ bool satradix_host_pipelined(CloSort *s, CCLQueue *q, const void *h_in, void *h_
 		s->group_events.push_back(ev);
 	}
 	cudaStream_t xs = s->copy_stream;
+	const size_t rel_words = (size_t)groups * (kBucketsPerGroup + 1);
+	if (!s->host_scratch &&
+		!cuda_ok(cudaMallocHost(&s->host_scratch, (128 + rel_words) * sizeof(uint64_t)), err,
+			"cudaMallocHost"))
+		return false;
+	uint32_t *counts = reinterpret_cast<uint32_t *>(s->host_scratch);  // 256 words
+	uint64_t *h_rel = s->host_scratch + 128;
 	const size_t off_b = (n * eb + 255) / 256 * 256;
 	const size_t off_rel = off_b + (n * eb + 255) / 256 * 256;
-	const size_t rel_words = (size_t)groups * (kBucketsPerGroup + 1);
 	char *dev = (char *)clo::tmp_alloc(ctx, off_rel + rel_words * 8, cs, err);
-	std::vector<uint64_t> h_rel(rel_words);
 	bool ok = dev != nullptr;
 	char *da = dev, *db = dev + off_b;
 	uint64_t *d_rel = (uint64_t *)(dev + off_rel);
-	uint32_t counts[256];
 	ok = ok && cuda_ok(cudaMemcpyAsync(da, h_in, n * eb, cudaMemcpyHostToDevice, cs), err,
 		"copy in");
 	ok = ok && clo::radix_msd_partition(da, db, n, (int)eb, bits, counts, ctx, cs, err) ==
@@ -715,8 +723,7 @@ bool satradix_host_pipelined(CloSort *s, CCLQueue *q, const void *h_in, void *h_
 			for (int j = 0; j <= kBucketsPerGroup; ++j)
 				h_rel[(size_t)g * (kBucketsPerGroup + 1) + j] =
 					off[g * kBucketsPerGroup + j] - off[g * kBucketsPerGroup];
-		// Pageable source: the call stages the copy before it returns.
-		ok = cuda_ok(cudaMemcpyAsync(d_rel, h_rel.data(), rel_words * 8,
+		ok = cuda_ok(cudaMemcpyAsync(d_rel, h_rel, rel_words * 8,
 			cudaMemcpyHostToDevice, cs), err, "offsets");
 	}
 	for (int g = 0; g < groups && ok; ++g) {

@@ -220,3 +220,15 @@ def test_scan_host_data_large_matches_oracle(clops, ctx, queue, in_code, in_dt, 
     sc.scan_host(queue, a, out)
     np.testing.assert_array_equal(out, oracle.scan(a, in_code, sum_dt))
     sc.destroy()
+
+
+def test_scan_host_data_large_repeated_calls_on_one_scanner(clops, ctx, queue):
+    # The chunked host-data scan keeps its copy streams and events in the
+    # scanner: a larger call after a smaller one needs more events.
+    sc = clops.Scanner(ctx, 5, 7)
+    for i, n in enumerate([(1 << 22) + 1, (1 << 25) + 99, (1 << 23) + 17]):
+        a = keys_of_type(950 + i, n, np.uint32)
+        out = np.zeros(n, np.uint64)
+        sc.scan_host(queue, a, out)
+        np.testing.assert_array_equal(out, oracle.scan(a, 5, np.uint64))
+    sc.destroy()

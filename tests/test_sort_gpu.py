@@ -228,6 +228,16 @@ def test_satradix_host_data_large_matches_oracle(clops, ctx, queue, code, dt, n)
     s.destroy()
 
 
+def test_satradix_host_data_large_repeated_calls_on_one_sorter(clops, ctx, queue):
+    # The pipelined host-data sort keeps its copy stream and events in the
+    # sorter: successive calls of different sizes reuse them.
+    s = clops.Sorter(ctx, "satradix", 5)
+    for i, n in enumerate([(1 << 22) + 3, (1 << 23) + 5, 1 << 22]):
+        a = keys_u32(600 + i, n)
+        np.testing.assert_array_equal(s.sort_host(queue, a.copy()), np.sort(a))
+    s.destroy()
+
+
 @pytest.mark.parametrize("kind", ["equal", "distinct16", "sorted"])
 def test_satradix_host_data_large_low_entropy_and_narrow_key(clops, ctx, queue, kind):
     n = 1 << 22
