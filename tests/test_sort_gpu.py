@@ -228,6 +228,40 @@ def test_satradix_host_data_large_matches_oracle(clops, ctx, queue, code, dt, n)
     s.destroy()
 
 
+def _pinned(clops, dt, n):
+    addr = clops.lib.clo_host_alloc(n * np.dtype(dt).itemsize, None)
+    return addr, np.ctypeslib.as_array((clops.C.c_uint8 * (n * np.dtype(dt).itemsize))
+                                       .from_address(addr)).view(dt)
+
+
+# Host-data sorts between page-locked buffers (the bench's end-to-end
+# form), across low-entropy inputs that leave most partition groups empty.
+@pytest.mark.parametrize("code,dt,n,kind", [
+    (5, np.uint32, (1 << 22) + 3, "uniform"), (7, np.uint64, (1 << 23) + 1, "uniform"),
+    (5, np.uint32, 1 << 22, "equal"), (5, np.uint32, (1 << 22) + 9, "distinct16"),
+    (4, np.int32, (1 << 22) + 5, "uniform")])
+def test_satradix_host_data_pinned_output(clops, ctx, queue, code, dt, n, kind):
+    if kind == "uniform":
+        a = keys_of_type(700 + code, n, dt)
+    else:
+        a = adversarial_u32(kind, n).view(dt)
+    ia, ain = _pinned(clops, dt, n)
+    oa, aout = _pinned(clops, dt, n)
+    try:
+        ain[:] = a
+        s = clops.Sorter(ctx, "satradix", code)
+        for _ in range(2):
+            aout[:] = 0
+            clops.call(clops.lib.clo_sort_with_host_data, s.h, queue.h, None, ia, oa, n, 0)
+            np.testing.assert_array_equal(aout, oracle.radix_sort(a))
+        np.testing.assert_array_equal(ain, a)
+        s.destroy()
+    finally:
+        del ain, aout
+        clops.lib.clo_host_free(ia)
+        clops.lib.clo_host_free(oa)
+
+
 def test_satradix_host_data_large_repeated_calls_on_one_sorter(clops, ctx, queue):
     # The pipelined host-data sort keeps its copy stream and events in the
     # sorter: successive calls of different sizes reuse them.
