@@ -145,6 +145,8 @@ CloScan *clo_scan_new(const char *type, const char *options, CCLContext *ctx,
 void clo_scan_destroy(CloScan *scan) {
 	if (!scan) return;
 	if (scan->copy_in || scan->copy_out || !scan->events.empty()) {
+		int prev_dev = -1;
+		if (cudaGetDevice(&prev_dev) != cudaSuccess) prev_dev = -1;
 		cudaSetDevice(scan->ctx->ordinal);
 		for (cudaStream_t st : {scan->copy_in, scan->copy_out}) {
 			if (st) {
@@ -153,6 +155,7 @@ void clo_scan_destroy(CloScan *scan) {
 			}
 		}
 		for (cudaEvent_t ev : scan->events) cudaEventDestroy(ev);
+		if (prev_dev >= 0) cudaSetDevice(prev_dev);
 	}
 	scan->impl_def.finalize(scan);
 	if (scan->ctx) ccl_context_unref(scan->ctx);

@@ -639,12 +639,15 @@ CloSort *clo_sort_new(const char *type, const char *options, CCLContext *ctx,
 void clo_sort_destroy(CloSort *sorter) {
 	if (!sorter) return;
 	if (sorter->copy_stream || !sorter->group_events.empty()) {
+		int prev_dev = -1;
+		if (cudaGetDevice(&prev_dev) != cudaSuccess) prev_dev = -1;
 		cudaSetDevice(sorter->ctx->ordinal);
 		if (sorter->copy_stream) {
 			cudaStreamSynchronize(sorter->copy_stream);
 			cudaStreamDestroy(sorter->copy_stream);
 		}
 		for (cudaEvent_t ev : sorter->group_events) cudaEventDestroy(ev);
+		if (prev_dev >= 0) cudaSetDevice(prev_dev);
 	}
 	if (sorter->host_scratch) cudaFreeHost(sorter->host_scratch);
 	if (sorter->impl_def.finalize) sorter->impl_def.finalize(sorter);
