@@ -160,7 +160,10 @@ struct PassArgs {
 // Lookback window: predecessor statuses read per round trip per digit. A
 // tile's nearest inclusive predecessor is a few tiles back; wider windows
 // measured slower.
-constexpr int kLookWindow = 8;
+#ifndef CLO_RADIX_LOOK_WINDOW
+#define CLO_RADIX_LOOK_WINDOW 8
+#endif
+constexpr int kLookWindow = CLO_RADIX_LOOK_WINDOW;
 
 // Threads per CTA of the pass: at least one per digit (threads below 256
 // own a digit in the per-tile scans, the lookback and the output bases).
