@@ -419,7 +419,10 @@ def run_suite(clops, ctx, q, args, only=None):
         res[f"blelloch_2pow{n.bit_length() - 1}_u32_u64"] = entry
 
     def rngs():
-        count, draws = 1 << 24, 64
+        # 2^24 states (with --only rng, 2^(log2n - 4) up to that: a small
+        # case for profiling).
+        count = 1 << (24 if only is None else min(24, max(args.log2n - 4, 10)))
+        draws = 64
         out = clops.Buffer(ctx, count * draws * 4)
         for name in ["lcg", "xorshift64", "xorshift128", "mwc64x", "parkmiller"]:
             size = clops.RNG_SEED_SIZE[name]
