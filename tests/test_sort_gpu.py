@@ -52,7 +52,9 @@ def test_satradix_large_tile_shape_edges(clops, ctx, queue, code, dt, tile, extr
 
 @pytest.mark.parametrize("kcode,kdt,vcode,vdt,tile", [
     (7, np.uint64, 5, np.uint32, 7168), (5, np.uint32, 5, np.uint32, 10240),
-    (5, np.uint32, 7, np.uint64, 7168), (7, np.uint64, 7, np.uint64, 5120)])
+    (5, np.uint32, 7, np.uint64, 7168), (7, np.uint64, 7, np.uint64, 5120),
+    (3, np.uint16, 7, np.uint64, 5120), (1, np.uint8, 5, np.uint32, 10240),
+    (2, np.int16, 5, np.uint32, 10240)])
 @pytest.mark.parametrize("extra", [-1, 1])
 def test_satradix_kv_large_tile_shape_edges(clops, ctx, queue, kcode, kdt, vcode, vdt, tile,
                                             extra):
@@ -105,13 +107,15 @@ def test_satradix_u64_low20(clops, ctx, queue):
 
 @pytest.mark.parametrize("kcode,kdt,vcode,vdt", [
     (5, np.uint32, 5, np.uint32), (7, np.uint64, 5, np.uint32),
-    (5, np.uint32, 7, np.uint64), (7, np.uint64, 7, np.uint64), (4, np.int32, 9, np.float32)])
+    (5, np.uint32, 7, np.uint64), (7, np.uint64, 7, np.uint64), (4, np.int32, 9, np.float32),
+    (1, np.uint8, 5, np.uint32), (3, np.uint16, 7, np.uint64)])
 @pytest.mark.parametrize("n", [1, 1000, 1023, 1025, 1791, 1792, 1793, 2559, 2561, 4097, 5119,
                                5121, 7167, 7168, 7169, 8193, 10239, 10240, 10241, 14337,
                                20481, 250007])
 def test_satradix_kv_stable(clops, ctx, queue, kcode, kdt, vcode, vdt, n):
     k = keys_of_type(31 + n, n, kdt)
-    k = (k.view(f"u{k.dtype.itemsize}") & np.array(0x0303, dtype=f"u{k.dtype.itemsize}")).view(kdt)
+    mask = 0x0303 & ((1 << (8 * k.dtype.itemsize)) - 1)
+    k = (k.view(f"u{k.dtype.itemsize}") & np.array(mask, dtype=f"u{k.dtype.itemsize}")).view(kdt)
     v = np.arange(n, dtype=np.uint64).astype(vdt)
     s = clops.Sorter(ctx, "satradix", kcode)
     kb = clops.Buffer.from_array(ctx, queue, k)
