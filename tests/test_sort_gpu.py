@@ -160,6 +160,19 @@ def test_bitonic_matches_network_replay(clops, ctx, queue, algo, code, dt, n):
     np.testing.assert_array_equal(got.view(f"u{a.dtype.itemsize}"), ref.view(f"u{a.dtype.itemsize}"))
 
 
+# Global passes group up to 7 steps (4-byte types), 6 (2-byte) or 5 (1- and
+# 8-byte); only stages of 21 steps or more (2^21 elements and up) reach the
+# 7-step grouping. 2^21 + 3 elements pad to 2^22.
+@pytest.mark.parametrize("code,dt", [(5, np.uint32), (4, np.int32), (9, np.float32),
+                                     (3, np.uint16), (0, np.int8), (7, np.uint64)])
+def test_abitonic_long_global_passes_match_network_replay(clops, ctx, queue, code, dt):
+    n = (1 << 21) + 3
+    a = keys_of_type(500 + code, n, dt)
+    got = _sort_dev(clops, ctx, queue, "abitonic", code, a)
+    ref = oracle.bitonic_sort_threaded(a, code)
+    np.testing.assert_array_equal(got.view(f"u{a.dtype.itemsize}"), ref.view(f"u{a.dtype.itemsize}"))
+
+
 @pytest.mark.parametrize("code,dt", [(8, np.float16), (9, np.float32), (10, np.float64)])
 def test_bitonic_non_total_order_is_bit_exact(clops, ctx, queue, code, dt):
     pat = np.array([0.0, -0.0, np.nan, 1.0, -1.0, np.nan, -0.0, 0.0, np.inf, -np.inf], dtype=dt)
